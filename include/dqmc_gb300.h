@@ -1,0 +1,150 @@
+/*
+ * dqmc_gb300.h -- C ABI of the GB300 DQMC sweep library (libdqmc_gb300.so).
+ *
+ * The library replaces, for the determinant quantum Monte Carlo of
+ * carstenbauer/MonteCarlo.jl, the hot path below the reference's plugin seam
+ * `update(::AbstractUpdate, mc, model, field)`: the local sweep, the
+ * Green's-function wraps, the slice-matrix chains and the UDT stabilisation
+ * (the `DQMCStack` functions).  A host in any language (the reference's Julia
+ * through `ccall`, Python through ctypes, C/C++) owns the model, lattice,
+ * parameters and measurements, and calls these entry points.
+ *
+ * Conventions
+ *   - Matrices are FP64, column-major, n x n per flavour block.  A chain with
+ *     two flavour blocks (MagneticHirsch / MagneticGHQ fields) passes and
+ *     receives 2*n*n doubles, block b at offset b*n*n: the reference's
+ *     BlockDiagonal{Float64,2,Matrix{Float64}}.  One block is the reference's
+ *     Matrix{Float64} (Density fields).
+ *   - The field configuration is int8, n x M, column-major (site fastest),
+ *     values +-1 (Hirsch) or 1..4 (Gauss-Hermite), as `field.conf`.
+ *   - Slices and chunk indices are 1-based, as in the reference.
+ *   - Host buffers are borrowed for the duration of the call; the handle owns
+ *     all device memory.  Every call returns a status (DQMC_OK = 0); the text
+ *     of the last error of the calling thread is `dqmc_last_error()`.  Nothing
+ *     throws across the ABI.
+ *   - A handle may not be used from two threads at once; distinct handles may.
+ *     Synchronous calls return when their work is complete; *_async calls
+ *     return at once and complete through dqmc_query / dqmc_synchronize.
+ *   - The library has no CPU fallback: without a usable CUDA device every
+ *     call that needs one returns DQMC_ERR_CUDA.
+ */
+#ifndef DQMC_GB300_H
+#define DQMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DQMC_GB300_ABI_VERSION 1
+
+/* status codes */
+#define DQMC_OK 0
+#define DQMC_ERR_INVALID 1   /* bad argument */
+#define DQMC_ERR_CUDA 2      /* CUDA runtime error / no device */
+#define DQMC_ERR_OOM 3       /* device allocation failed (or over the budget) */
+#define DQMC_ERR_NUMERICAL 4 /* kernel reported a non-finite or invalid state */
+#define DQMC_ERR_NOT_READY 5 /* asynchronous work still running */
+
+/* field kinds (src/flavors/DQMC/fields.jl) */
+#define DQMC_FIELD_DENSITY_HIRSCH 0  /* fields.jl:363-395 */
+#define DQMC_FIELD_MAGNETIC_HIRSCH 1 /* fields.jl:412-451 */
+#define DQMC_FIELD_DENSITY_GHQ 2     /* fields.jl:589-637 */
+#define DQMC_FIELD_MAGNETIC_GHQ 3    /* fields.jl:519-573 */
+
+/* arithmetic of the wraps and slice-matrix chains */
+#define DQMC_PREC_FP64 0  /* everything FP64 (parity path) */
+#define DQMC_PREC_MIXED 1 /* wraps in FP32-split arithmetic; UDT, reconstruction,
+                             determinant ratios and rank-1 updates in FP64 */
+
+typedef struct dqmc_handle dqmc_handle;
+
+/* One chain.  Mirrors what the reference derives in DQMC(model; beta, delta_tau,
+ * safe_mult, field) (src/flavors/DQMC/DQMC.jl:32-64, parameters.jl:84-139). */
+typedef struct {
+    int32_t n_sites;       /* N = length(lattice(model)) */
+    int32_t n_flavors;     /* unique_flavors(field, model): 1 or 2 */
+    int32_t slices;        /* M = round(beta / delta_tau) */
+    int32_t safe_mult;     /* parameters.safe_mult */
+    int32_t field;         /* DQMC_FIELD_* */
+    int32_t check_propagation_error; /* parameters.check_propagation_error */
+    double alpha;          /* field.alpha */
+    uint64_t seed;         /* key of the chain's Philox4x32-10 stream */
+} dqmc_chain_config;
+
+/* Per-chain counters (DQMCAnalysis, statistics.jl:45-51; AcceptanceStatistics,
+ * scheduler.jl:163-181). */
+typedef struct {
+    int64_t accepted;             /* accepted local moves since creation */
+    int64_t proposals;            /* proposed local moves since creation */
+    int64_t propagation_errors;   /* stabilisations with max|dG| > 1e-7 */
+    int64_t negative_probability; /* proposals with p < 0 */
+    double max_propagation_error; /* max over all stabilisations of max|dG| */
+    double max_reported_error;    /* max of the errors counted above */
+    int32_t current_slice, current_range, direction, status;
+} dqmc_stats;
+
+/* ---- lifecycle ------------------------------------------------------------
+ * Replaces: DQMC(model; ...) stack allocation, DQMCStack + initialize_stack
+ * (src/flavors/DQMC/stack.jl:113-132, 160-206).  `precision` is DQMC_PREC_*. */
+int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int precision,
+                dqmc_handle** out);
+int dqmc_destroy(dqmc_handle* h);
+const char* dqmc_last_error(void);
+int dqmc_abi_version(void);
+/* Device bytes one chain needs (stack + Green's function workspace). */
+int64_t dqmc_chain_bytes(const dqmc_chain_config* cfg, int precision);
+
+/* ---- inputs ---------------------------------------------------------------
+ * Replaces: init_hopping_matrices (stack.jl:209-249).  The four matrices are
+ * exp(-dtau T), exp(+dtau T), exp(-dtau T/2), exp(+dtau T/2), one n x n block
+ * each (shared by both flavour blocks).  chain = -1 sets every chain. */
+int dqmc_set_hopping(dqmc_handle* h, int chain, const double* exp_m_dtT, const double* exp_p_dtT,
+                     const double* exp_m_half_dtT, const double* exp_p_half_dtT);
+/* Replaces: field.conf access / copyto!(conf(field), c) (fields.jl:305-318). */
+int dqmc_set_field(dqmc_handle* h, int chain, const int8_t* conf);
+int dqmc_get_field(dqmc_handle* h, int chain, int8_t* conf);
+/* Replaces: rand!(field) (fields.jl:330, 470), drawn from the chain's stream;
+ * leaves the stream counter at n*M.  chain = -1: all chains. */
+int dqmc_init_random_field(dqmc_handle* h, int chain);
+/* Replaces: Random.seed! / the RNG state saved with a simulation (FileIO.jl:201-222). */
+int dqmc_set_rng(dqmc_handle* h, int chain, uint64_t key, uint64_t counter);
+int dqmc_get_rng(dqmc_handle* h, int chain, uint64_t* key, uint64_t* counter);
+
+/* ---- stack ----------------------------------------------------------------
+ * Replaces: reverse_build_stack + propagate in initialize_run (DQMC.jl:178-179,
+ * stack.jl:284-308, 605-730), all chains. */
+int dqmc_initialize_run(dqmc_handle* h);
+/* Replaces: build_stack (stack.jl:257-281), all chains. */
+int dqmc_build_stack(dqmc_handle* h);
+/* Replaces: propagate (stack.jl:605-730), one step, all chains. */
+int dqmc_propagate(dqmc_handle* h);
+/* Replaces: sweep_spatial (local_updates.jl:23-60) at the current slice. */
+int dqmc_sweep_spatial(dqmc_handle* h);
+
+/* ---- the hot path -----------------------------------------------------------
+ * Replaces: update(::LocalSweep, mc, model, field) (local_updates.jl:7-14, 82)
+ * called n_sweeps times, for every chain of the handle in one launch.
+ * stats (may be NULL) receives n_chains entries after the call. */
+int dqmc_sweep(dqmc_handle* h, int n_sweeps, dqmc_stats* stats);
+int dqmc_sweep_async(dqmc_handle* h, int n_sweeps);
+int dqmc_query(dqmc_handle* h);       /* DQMC_OK when idle, DQMC_ERR_NOT_READY when busy */
+int dqmc_synchronize(dqmc_handle* h);
+int dqmc_get_stats(dqmc_handle* h, int chain, dqmc_stats* out);
+
+/* ---- outputs --------------------------------------------------------------
+ * Replaces: mc.stack.greens (physical = 0) and greens!/_greens!
+ * (greens.jl:94-125, physical = 1). */
+int dqmc_get_greens(dqmc_handle* h, int chain, int physical, double* out);
+int dqmc_set_greens(dqmc_handle* h, int chain, const double* in);
+/* Replaces: calculate_greens(mc, slice, output, field, safe_mult) (stack.jl:525-583).
+ * safe_mult <= 0 uses the chain's own. */
+int dqmc_calculate_greens(dqmc_handle* h, int chain, int slice, int safe_mult, double* out);
+/* which: 0 u_stack, 1 t_stack (nf*n*n), 2 d_stack (nf*n); idx 1-based (stack.jl:13-15) */
+int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

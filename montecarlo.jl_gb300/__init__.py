@@ -1,0 +1,15 @@
+"""GB300-native DQMC sweep for the Hubbard model (MonteCarlo.jl drop-in path).
+
+Host-side mirror of the reference's user API -- ``HubbardModel``, ``DQMC``,
+``run`` (the reference's ``run!``) and the Hirsch / Gauss-Hermite fields --
+driving the CUDA library ``libdqmc_gb300.so`` through its C ABI
+(``include/dqmc_gb300.h``).  The package directory is named
+``montecarlo.jl_gb300``; it is imported under the module name
+``montecarlo_gb300`` (see ``__graft_entry__.load_package``).
+"""
+from .lattices import (Bond, Chain, CubicLattice, Honeycomb, Lattice, SquareLattice,  # noqa: F401
+                       TriangularLattice, UnitCell)
+from .model import (DENSITY_GHQ, DENSITY_HIRSCH, MAGNETIC_GHQ, MAGNETIC_HIRSCH,  # noqa: F401
+                    AttractiveHubbardModel, DensityGHQField, DensityHirschField, DQMCParameters,
+                    HubbardModel, MagneticGHQField, MagneticHirschField, RepulsiveHubbardModel,
+                    generate_chunks, hopping_exponentials)

@@ -1,0 +1,241 @@
+"""ctypes binding of libdqmc_gb300.so (include/dqmc_gb300.h).
+
+Loading fails loudly: there is no CPU fallback for the DQMC path.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libdqmc_gb300.so")
+
+DQMC_OK = 0
+DQMC_ERR_NOT_READY = 5
+PREC_FP64 = 0
+PREC_MIXED = 1
+
+ERRORS = {1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
+          4: "numerical error", 5: "not ready"}
+
+
+class DQMCError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class ChainConfig(C.Structure):
+    _fields_ = [("n_sites", C.c_int32), ("n_flavors", C.c_int32), ("slices", C.c_int32),
+                ("safe_mult", C.c_int32), ("field", C.c_int32),
+                ("check_propagation_error", C.c_int32), ("alpha", C.c_double),
+                ("seed", C.c_uint64)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("accepted", C.c_int64), ("proposals", C.c_int64),
+                ("propagation_errors", C.c_int64), ("negative_probability", C.c_int64),
+                ("max_propagation_error", C.c_double), ("max_reported_error", C.c_double),
+                ("current_slice", C.c_int32), ("current_range", C.c_int32),
+                ("direction", C.c_int32), ("status", C.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+EXPORTS = [
+    "dqmc_create", "dqmc_destroy", "dqmc_last_error", "dqmc_abi_version", "dqmc_chain_bytes",
+    "dqmc_set_hopping", "dqmc_set_field", "dqmc_get_field", "dqmc_init_random_field",
+    "dqmc_set_rng", "dqmc_get_rng", "dqmc_initialize_run", "dqmc_build_stack", "dqmc_propagate",
+    "dqmc_sweep_spatial", "dqmc_sweep", "dqmc_sweep_async", "dqmc_query", "dqmc_synchronize",
+    "dqmc_get_stats", "dqmc_get_greens", "dqmc_set_greens", "dqmc_calculate_greens",
+    "dqmc_get_stack",
+]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the CUDA library (build it first with ``build.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"{path} is missing: build the CUDA extension (montecarlo.jl_gb300/build.py); "
+            "the DQMC path has no CPU fallback")
+    L = C.CDLL(path)
+    P = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    i8p = C.POINTER(C.c_int8)
+    L.dqmc_create.argtypes = [C.c_int, C.POINTER(ChainConfig), C.c_int, C.c_int, C.POINTER(P)]
+    L.dqmc_destroy.argtypes = [P]
+    L.dqmc_last_error.restype = C.c_char_p
+    L.dqmc_chain_bytes.argtypes = [C.POINTER(ChainConfig), C.c_int]
+    L.dqmc_chain_bytes.restype = C.c_int64
+    L.dqmc_set_hopping.argtypes = [P, C.c_int, dp, dp, dp, dp]
+    L.dqmc_set_field.argtypes = [P, C.c_int, i8p]
+    L.dqmc_get_field.argtypes = [P, C.c_int, i8p]
+    L.dqmc_init_random_field.argtypes = [P, C.c_int]
+    L.dqmc_set_rng.argtypes = [P, C.c_int, C.c_uint64, C.c_uint64]
+    L.dqmc_get_rng.argtypes = [P, C.c_int, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]
+    for f in ("dqmc_initialize_run", "dqmc_build_stack", "dqmc_propagate", "dqmc_sweep_spatial",
+              "dqmc_query", "dqmc_synchronize"):
+        getattr(L, f).argtypes = [P]
+    L.dqmc_sweep.argtypes = [P, C.c_int, C.POINTER(Stats)]
+    L.dqmc_sweep_async.argtypes = [P, C.c_int]
+    L.dqmc_get_stats.argtypes = [P, C.c_int, C.POINTER(Stats)]
+    L.dqmc_get_greens.argtypes = [P, C.c_int, C.c_int, dp]
+    L.dqmc_set_greens.argtypes = [P, C.c_int, dp]
+    L.dqmc_calculate_greens.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
+    L.dqmc_get_stack.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
+    _lib = L
+    return L
+
+
+def check(code: int):
+    if code != DQMC_OK:
+        raise DQMCError(code, load().dqmc_last_error().decode(errors="replace"))
+    return code
+
+
+def dptr(a: np.ndarray):
+    assert a.dtype == np.float64 and (a.flags["C_CONTIGUOUS"] or a.flags["F_CONTIGUOUS"])
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def i8ptr(a: np.ndarray):
+    assert a.dtype == np.int8
+    return a.ctypes.data_as(C.POINTER(C.c_int8))
+
+
+def blocks_to_buf(G: np.ndarray) -> np.ndarray:
+    """(nf, n, n) -> flat column-major-per-block buffer."""
+    return np.ascontiguousarray(np.transpose(np.asarray(G, dtype=np.float64), (0, 2, 1))).ravel()
+
+
+def buf_to_blocks(buf: np.ndarray, nf: int, n: int) -> np.ndarray:
+    return np.transpose(buf.reshape(nf, n, n), (0, 2, 1)).copy()
+
+
+class Handle:
+    """Owns one dqmc_handle (a batch of chains on one device)."""
+
+    def __init__(self, configs, precision=PREC_FP64, device=0):
+        L = load()
+        arr = (ChainConfig * len(configs))(*configs)
+        self._cfg = list(configs)
+        h = C.c_void_p()
+        check(L.dqmc_create(device, arr, len(configs), precision, C.byref(h)))
+        self.h = h
+        self.n_chains = len(configs)
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().dqmc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def cfg(self, chain):
+        return self._cfg[chain]
+
+    def set_hopping(self, chain, exps):
+        e = [np.asfortranarray(x, dtype=np.float64) for x in exps]
+        check(load().dqmc_set_hopping(self.h, chain, *[dptr(x) for x in e]))
+
+    def set_field(self, chain, conf):
+        c = np.asfortranarray(conf, dtype=np.int8)
+        check(load().dqmc_set_field(self.h, chain, i8ptr(c)))
+
+    def get_field(self, chain):
+        cfg = self._cfg[chain]
+        c = np.zeros((cfg.n_sites, cfg.slices), dtype=np.int8, order="F")
+        check(load().dqmc_get_field(self.h, chain, i8ptr(c)))
+        return c
+
+    def init_random_field(self, chain=-1):
+        check(load().dqmc_init_random_field(self.h, chain))
+
+    def set_rng(self, chain, key, counter):
+        check(load().dqmc_set_rng(self.h, chain, key, counter))
+
+    def get_rng(self, chain):
+        k, c = C.c_uint64(), C.c_uint64()
+        check(load().dqmc_get_rng(self.h, chain, C.byref(k), C.byref(c)))
+        return k.value, c.value
+
+    def initialize_run(self):
+        check(load().dqmc_initialize_run(self.h))
+
+    def build_stack(self):
+        check(load().dqmc_build_stack(self.h))
+
+    def propagate(self):
+        check(load().dqmc_propagate(self.h))
+
+    def sweep_spatial(self):
+        check(load().dqmc_sweep_spatial(self.h))
+
+    def sweep(self, n_sweeps=1):
+        st = (Stats * self.n_chains)()
+        check(load().dqmc_sweep(self.h, int(n_sweeps), st))
+        return [s.as_dict() for s in st]
+
+    def sweep_async(self, n_sweeps=1):
+        check(load().dqmc_sweep_async(self.h, int(n_sweeps)))
+
+    def query(self) -> bool:
+        code = load().dqmc_query(self.h)
+        if code == DQMC_ERR_NOT_READY:
+            return False
+        check(code)
+        return True
+
+    def synchronize(self):
+        check(load().dqmc_synchronize(self.h))
+
+    def stats(self, chain):
+        s = Stats()
+        check(load().dqmc_get_stats(self.h, chain, C.byref(s)))
+        return s.as_dict()
+
+    def _mat_buf(self, chain):
+        cfg = self._cfg[chain]
+        return np.zeros(cfg.n_flavors * cfg.n_sites * cfg.n_sites)
+
+    def greens(self, chain, physical=False):
+        cfg = self._cfg[chain]
+        buf = self._mat_buf(chain)
+        check(load().dqmc_get_greens(self.h, chain, int(bool(physical)), dptr(buf)))
+        return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
+
+    def greens_into(self, chain, buf, physical=False):
+        """Download G into a preallocated flat float64 buffer (no reshaping)."""
+        check(load().dqmc_get_greens(self.h, chain, int(bool(physical)), dptr(buf)))
+
+    def set_greens(self, chain, G):
+        buf = blocks_to_buf(G)
+        check(load().dqmc_set_greens(self.h, chain, dptr(buf)))
+
+    def calculate_greens(self, chain, slice_, safe_mult=0):
+        cfg = self._cfg[chain]
+        buf = self._mat_buf(chain)
+        check(load().dqmc_calculate_greens(self.h, chain, int(slice_), int(safe_mult), dptr(buf)))
+        return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
+
+    def stack(self, chain, which, idx):
+        cfg = self._cfg[chain]
+        if which == 2:
+            out = np.zeros(cfg.n_flavors * cfg.n_sites)
+            check(load().dqmc_get_stack(self.h, chain, 2, idx, dptr(out)))
+            return out.reshape(cfg.n_flavors, cfg.n_sites)
+        buf = self._mat_buf(chain)
+        check(load().dqmc_get_stack(self.h, chain, which, idx, dptr(buf)))
+        return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)

@@ -1,0 +1,571 @@
+// C ABI of libdqmc_gb300.so (declared in include/dqmc_gb300.h): handle and
+// device-memory management, host-side tables, launches and error reporting.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/dqmc_gb300.h"
+#include "dqmc_chain.h"
+#include "dqmc_kernels.h"
+#include "philox.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string& msg) {
+    g_last_error = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+    return fail(e == cudaErrorMemoryAllocation ? DQMC_ERR_OOM : DQMC_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CUDA_TRY(expr, what)                       \
+    do {                                           \
+        cudaError_t _e = (expr);                   \
+        if (_e != cudaSuccess) return cuda_fail(_e, what); \
+    } while (0)
+
+// generate_chunks (stack.jl:154-158)
+int generate_chunks(int length, int max_chunk, int* first, int* last) {
+    int nch = (length + max_chunk - 1) / max_chunk;
+    double step = (double)length / (double)nch;
+    for (int i = 1; i <= nch; ++i) {
+        first[i - 1] = (int)nearbyint((double)(i - 1) * step) + 1;
+        last[i - 1] = (int)nearbyint((double)i * step);
+    }
+    return nch;
+}
+
+size_t mat_elems(const dqmc_chain_config& c) { return (size_t)c.n_flavors * c.n_sites * c.n_sites; }
+
+struct Layout {
+    size_t bytes;
+    size_t off_conf, off_hop, off_G, off_Gtmp, off_Ul, off_Ur, off_Tl, off_Tr, off_tmp1, off_tmp2,
+        off_currU, off_out, off_ustack, off_tstack, off_dstack, off_Dl, off_Dr, off_tempv,
+        off_pivot, off_mix;
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+Layout layout_of(const dqmc_chain_config& c, int prec) {
+    Layout L;
+    const size_t n = c.n_sites, nf = c.n_flavors, ms = mat_elems(c) * sizeof(double);
+    const int nr = (c.slices + c.safe_mult - 1) / c.safe_mult;
+    size_t o = 0;
+    L.off_conf = o; o = align256(o + n * c.slices);
+    L.off_hop = o; o = align256(o + 4 * n * n * sizeof(double));
+    size_t* mats[] = {&L.off_G, &L.off_Gtmp, &L.off_Ul, &L.off_Ur, &L.off_Tl, &L.off_Tr,
+                      &L.off_tmp1, &L.off_tmp2, &L.off_currU, &L.off_out};
+    for (size_t* m : mats) { *m = o; o = align256(o + ms); }
+    L.off_ustack = o; o = align256(o + ms * (nr + 1));
+    L.off_tstack = o; o = align256(o + ms * (nr + 1));
+    L.off_dstack = o; o = align256(o + nf * n * sizeof(double) * (nr + 1));
+    L.off_Dl = o; o = align256(o + nf * n * sizeof(double));
+    L.off_Dr = o; o = align256(o + nf * n * sizeof(double));
+    L.off_tempv = o; o = align256(o + nf * n * sizeof(double));
+    L.off_pivot = o; o = align256(o + nf * n * sizeof(int));
+    L.off_mix = o;
+    if (prec == DQMC_PREC_MIXED) o = align256(o + 4 * n * n * sizeof(float) + 2 * mat_elems(c) * sizeof(float));
+    L.bytes = o;
+    return L;
+}
+
+// Tables of the proposal / interaction exponentials, computed with the
+// reference's expressions in the reference's operation order.
+void fill_tables(DqmcChain& d, int kind, double alpha) {
+    const double s6 = sqrt(6.0);
+    const double gam[4] = {1.0 - s6 / 3.0, 1.0 + s6 / 3.0, 1.0 + s6 / 3.0, 1.0 - s6 / 3.0};
+    const double eta[4] = {-sqrt(6.0 + 2.0 * s6), -sqrt(6.0 - 2.0 * s6), sqrt(6.0 - 2.0 * s6),
+                           sqrt(6.0 + 2.0 * s6)};
+    for (int i = 0; i < 4; ++i) d.gam[i] = gam[i];
+    for (int i = 0; i < 16; ++i) { d.delta0[i] = 0.0; d.delta1[i] = 0.0; d.wboson[i] = 0.0; }
+    for (int f = 0; f < 2; ++f)
+        for (int v = 0; v < 4; ++v) { d.ev[f][v] = 0.0; d.evinv[f][v] = 0.0; }
+    const double a = alpha;
+    switch (kind) {
+    case DQMC_FIELD_DENSITY_HIRSCH:
+        for (int v = 0; v < 2; ++v) {
+            double s = v ? 1.0 : -1.0;
+            d.ev[0][v] = exp(1.0 * a * s);      // fields.jl:383
+            d.evinv[0][v] = exp(-1.0 * a * s);
+            double dE = -2.0 * a * s;           // fields.jl:389-390
+            d.delta0[v] = exp(dE) - 1;
+            d.wboson[v] = exp(-dE);             // local_updates.jl:31
+        }
+        break;
+    case DQMC_FIELD_MAGNETIC_HIRSCH:
+        for (int v = 0; v < 2; ++v) {
+            double s = v ? 1.0 : -1.0;
+            d.ev[0][v] = exp(1.0 * a * s);      // fields.jl:432
+            d.ev[1][v] = exp(-1.0 * a * s);     // fields.jl:435
+            d.evinv[0][v] = exp(-1.0 * a * s);
+            d.evinv[1][v] = exp(-(-1.0) * a * s);
+            double dE = -2.0 * a * s;           // fields.jl:441-443
+            d.delta0[v] = exp(+dE) - 1.0;
+            d.delta1[v] = exp(-dE) - 1.0;
+            d.wboson[v] = exp(-0.0);
+        }
+        break;
+    case DQMC_FIELD_DENSITY_GHQ:
+        for (int v = 0; v < 4; ++v) {
+            d.ev[0][v] = exp(+1.0 * a * eta[v]); // fields.jl:621
+            d.evinv[0][v] = exp(+(-1.0) * a * eta[v]);
+        }
+        for (int xo = 0; xo < 4; ++xo)
+            for (int xn = 0; xn < 4; ++xn) {
+                if (xo == xn) continue;
+                double dE = a * (eta[xn] - eta[xo]); // fields.jl:631-633
+                double er = exp(dE);
+                d.delta0[xo * 4 + xn] = er - 1.0;
+                d.wboson[xo * 4 + xn] = exp(-dE);
+            }
+        break;
+    default: /* DQMC_FIELD_MAGNETIC_GHQ */
+        for (int v = 0; v < 4; ++v) {
+            d.ev[0][v] = exp(+1.0 * a * eta[v]);    // fields.jl:553
+            d.ev[1][v] = exp(-1.0 * a * eta[v]);    // fields.jl:556
+            d.evinv[0][v] = exp(+(-1.0) * a * eta[v]);
+            d.evinv[1][v] = exp(-(-1.0) * a * eta[v]);
+        }
+        for (int xo = 0; xo < 4; ++xo)
+            for (int xn = 0; xn < 4; ++xn) {
+                if (xo == xn) continue;
+                double er = exp(a * (eta[xn] - eta[xo])); // fields.jl:567-569
+                d.delta0[xo * 4 + xn] = er - 1.0;
+                d.delta1[xo * 4 + xn] = 1 / er - 1.0;
+                d.wboson[xo * 4 + xn] = exp(-0.0);
+            }
+        break;
+    }
+}
+
+}  // namespace
+
+struct dqmc_handle {
+    int device = 0;
+    int precision = DQMC_PREC_FP64;
+    cudaStream_t stream = nullptr;
+    std::vector<dqmc_chain_config> cfg;
+    std::vector<Layout> lay;
+    std::vector<DqmcChain> host;  // descriptors (pointers into `arena`)
+    char* arena = nullptr;
+    DqmcChain* d_chains = nullptr;
+    bool host_dirty = false;      // host descriptors changed (must upload before launch)
+    bool busy = false;
+};
+
+namespace {
+
+int check_chain(dqmc_handle* h, int chain) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (chain < 0 || chain >= (int)h->cfg.size())
+        return fail(DQMC_ERR_INVALID, "chain index " + std::to_string(chain) + " out of range");
+    return DQMC_OK;
+}
+
+// refresh the host mirror of the mutable device state
+int pull_descriptors(dqmc_handle* h) {
+    CUDA_TRY(cudaMemcpyAsync(h->host.data(), h->d_chains, sizeof(DqmcChain) * h->host.size(),
+                             cudaMemcpyDeviceToHost, h->stream),
+             "download chain descriptors");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+int push_descriptors(dqmc_handle* h) {
+    CUDA_TRY(cudaMemcpyAsync(h->d_chains, h->host.data(), sizeof(DqmcChain) * h->host.size(),
+                             cudaMemcpyHostToDevice, h->stream),
+             "upload chain descriptors");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    h->host_dirty = false;
+    return DQMC_OK;
+}
+
+int launch(dqmc_handle* h, int op, int arg0, int arg1, bool sync) {
+    if (h->busy) {
+        int st = dqmc_synchronize(h);
+        if (st != DQMC_OK) return st;
+    }
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    if (h->host_dirty) {
+        int st = push_descriptors(h);
+        if (st != DQMC_OK) return st;
+    }
+    CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), op, arg0, arg1, h->stream),
+             "chain kernel launch");
+    if (!sync) {
+        h->busy = true;
+        return DQMC_OK;
+    }
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "chain kernel");
+    int st = pull_descriptors(h);
+    if (st != DQMC_OK) return st;
+    for (size_t i = 0; i < h->host.size(); ++i)
+        if (h->host[i].status != 0)
+            return fail(DQMC_ERR_NUMERICAL, "chain " + std::to_string(i) + " reported status " +
+                                                 std::to_string(h->host[i].status));
+    return DQMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* dqmc_last_error(void) { return g_last_error.c_str(); }
+int dqmc_abi_version(void) { return DQMC_GB300_ABI_VERSION; }
+
+int64_t dqmc_chain_bytes(const dqmc_chain_config* cfg, int precision) {
+    if (!cfg) return -1;
+    return (int64_t)layout_of(*cfg, precision).bytes;
+}
+
+int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int precision,
+                dqmc_handle** out) {
+    if (!out || !chains || n_chains <= 0) return fail(DQMC_ERR_INVALID, "dqmc_create: bad arguments");
+    *out = nullptr;
+    if (precision != DQMC_PREC_FP64 && precision != DQMC_PREC_MIXED)
+        return fail(DQMC_ERR_INVALID, "dqmc_create: unknown precision");
+    for (int i = 0; i < n_chains; ++i) {
+        const dqmc_chain_config& c = chains[i];
+        if (c.n_sites < 1 || c.n_sites > 512 || c.slices < 1 || c.safe_mult < 1 ||
+            (c.n_flavors != 1 && c.n_flavors != 2) || c.field < 0 || c.field > 3)
+            return fail(DQMC_ERR_INVALID, "dqmc_create: invalid config for chain " + std::to_string(i) +
+                                              " (need 1 <= n_sites <= 512, slices >= 1, safe_mult >= 1, "
+                                              "n_flavors in {1,2}, field in 0..3)");
+        int want_nf = (c.field == DQMC_FIELD_MAGNETIC_HIRSCH || c.field == DQMC_FIELD_MAGNETIC_GHQ) ? 2 : 1;
+        if (c.n_flavors != want_nf)
+            return fail(DQMC_ERR_INVALID, "dqmc_create: n_flavors does not match the field kind");
+        if ((c.slices + c.safe_mult - 1) / c.safe_mult > DQMC_MAX_CHUNKS)
+            return fail(DQMC_ERR_INVALID, "dqmc_create: too many stabilisation chunks (max 256)");
+        if (!(c.alpha == c.alpha)) return fail(DQMC_ERR_INVALID, "dqmc_create: alpha is NaN");
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(DQMC_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= ndev) return fail(DQMC_ERR_INVALID, "dqmc_create: bad device index");
+    CUDA_TRY(cudaSetDevice(device), "cudaSetDevice");
+    dqmc_handle* h = new dqmc_handle();
+    h->device = device;
+    h->precision = precision;
+    h->cfg.assign(chains, chains + n_chains);
+    size_t total = 0;
+    std::vector<size_t> base(n_chains);
+    for (int i = 0; i < n_chains; ++i) {
+        h->lay.push_back(layout_of(chains[i], precision));
+        base[i] = total;
+        total += h->lay.back().bytes;
+    }
+    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreate"); }
+    e = cudaMalloc((void**)&h->arena, total);
+    if (e != cudaSuccess) {
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return cuda_fail(e, "cudaMalloc chain workspace");
+    }
+    e = cudaMemsetAsync(h->arena, 0, total, h->stream);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_chains, sizeof(DqmcChain) * n_chains);
+    if (e != cudaSuccess) {
+        cudaFree(h->arena);
+        cudaStreamDestroy(h->stream);
+        delete h;
+        return cuda_fail(e, "cudaMalloc chain descriptors");
+    }
+    h->host.resize(n_chains);
+    for (int i = 0; i < n_chains; ++i) {
+        const dqmc_chain_config& c = chains[i];
+        const Layout& L = h->lay[i];
+        char* b = h->arena + base[i];
+        DqmcChain& d = h->host[i];
+        memset(&d, 0, sizeof(d));
+        d.n = c.n_sites; d.nf = c.n_flavors; d.M = c.slices; d.k = c.safe_mult; d.kind = c.field;
+        d.check_prop = c.check_propagation_error ? 1 : 0;
+        d.prec = precision;
+        d.nr = generate_chunks(c.slices, c.safe_mult, d.rfirst, d.rlast);
+        fill_tables(d, c.field, c.alpha);
+        const size_t nn = (size_t)c.n_sites * c.n_sites;
+        double* hop = (double*)(b + L.off_hop);
+        d.conf = (int8_t*)(b + L.off_conf);
+        d.eT2 = hop; d.eT2inv = hop + nn; d.eTh = hop + 2 * nn; d.eThinv = hop + 3 * nn;
+        d.G = (double*)(b + L.off_G); d.Gtmp = (double*)(b + L.off_Gtmp);
+        d.Ul = (double*)(b + L.off_Ul); d.Ur = (double*)(b + L.off_Ur);
+        d.Tl = (double*)(b + L.off_Tl); d.Tr = (double*)(b + L.off_Tr);
+        d.tmp1 = (double*)(b + L.off_tmp1); d.tmp2 = (double*)(b + L.off_tmp2);
+        d.currU = (double*)(b + L.off_currU); d.out = (double*)(b + L.off_out);
+        d.ustack = (double*)(b + L.off_ustack); d.tstack = (double*)(b + L.off_tstack);
+        d.dstack = (double*)(b + L.off_dstack);
+        d.Dl = (double*)(b + L.off_Dl); d.Dr = (double*)(b + L.off_Dr);
+        d.tempv = (double*)(b + L.off_tempv);
+        d.pivot = (int*)(b + L.off_pivot);
+        d.mixG = precision == DQMC_PREC_MIXED ? (float*)(b + L.off_mix) : nullptr;
+        d.key = c.seed; d.ctr = 0;
+        d.current_slice = 0; d.current_range = 1; d.direction = 1;
+    }
+    int st = push_descriptors(h);
+    if (st != DQMC_OK) { dqmc_destroy(h); return st; }
+    *out = h;
+    return DQMC_OK;
+}
+
+int dqmc_destroy(dqmc_handle* h) {
+    if (!h) return DQMC_OK;
+    cudaSetDevice(h->device);
+    if (h->stream) cudaStreamSynchronize(h->stream);
+    if (h->arena) cudaFree(h->arena);
+    if (h->d_chains) cudaFree(h->d_chains);
+    if (h->stream) cudaStreamDestroy(h->stream);
+    delete h;
+    return DQMC_OK;
+}
+
+int dqmc_set_hopping(dqmc_handle* h, int chain, const double* a, const double* b, const double* c,
+                     const double* d) {
+    if (!h || !a || !b || !c || !d) return fail(DQMC_ERR_INVALID, "dqmc_set_hopping: null argument");
+    int lo = chain, hi = chain + 1;
+    if (chain == -1) { lo = 0; hi = (int)h->cfg.size(); }
+    else if (int st = check_chain(h, chain)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    for (int i = lo; i < hi; ++i) {
+        const size_t nn = (size_t)h->cfg[i].n_sites * h->cfg[i].n_sites;
+        if (chain == -1 && h->cfg[i].n_sites != h->cfg[lo].n_sites)
+            return fail(DQMC_ERR_INVALID, "dqmc_set_hopping(-1): chains have different n_sites");
+        const double* src[4] = {a, b, c, d};
+        double* dst[4] = {(double*)h->host[i].eT2, (double*)h->host[i].eT2inv,
+                          (double*)h->host[i].eTh, (double*)h->host[i].eThinv};
+        for (int m = 0; m < 4; ++m)
+            CUDA_TRY(cudaMemcpyAsync(dst[m], src[m], nn * sizeof(double), cudaMemcpyHostToDevice,
+                                     h->stream),
+                     "upload hopping exponentials");
+    }
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+int dqmc_set_field(dqmc_handle* h, int chain, const int8_t* conf) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!conf) return fail(DQMC_ERR_INVALID, "dqmc_set_field: null conf");
+    const dqmc_chain_config& c = h->cfg[chain];
+    const bool ghq = c.field >= 2;
+    for (size_t i = 0; i < (size_t)c.n_sites * c.slices; ++i) {
+        int v = conf[i];
+        bool ok = ghq ? (v >= 1 && v <= 4) : (v == 1 || v == -1);
+        if (!ok) return fail(DQMC_ERR_INVALID, "dqmc_set_field: value out of range for the field kind");
+    }
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    CUDA_TRY(cudaMemcpyAsync(h->host[chain].conf, conf, (size_t)c.n_sites * c.slices,
+                             cudaMemcpyHostToDevice, h->stream),
+             "upload field");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+int dqmc_get_field(dqmc_handle* h, int chain, int8_t* conf) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!conf) return fail(DQMC_ERR_INVALID, "dqmc_get_field: null conf");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    const dqmc_chain_config& c = h->cfg[chain];
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    CUDA_TRY(cudaMemcpyAsync(conf, h->host[chain].conf, (size_t)c.n_sites * c.slices,
+                             cudaMemcpyDeviceToHost, h->stream),
+             "download field");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+int dqmc_init_random_field(dqmc_handle* h, int chain) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    int lo = chain, hi = chain + 1;
+    if (chain == -1) { lo = 0; hi = (int)h->cfg.size(); }
+    else if (int st = check_chain(h, chain)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    for (int i = lo; i < hi; ++i) {
+        const dqmc_chain_config& c = h->cfg[i];
+        const size_t cnt = (size_t)c.n_sites * c.slices;
+        std::vector<int8_t> conf(cnt);
+        DqmcChain& d = h->host[i];
+        for (size_t k = 0; k < cnt; ++k) {
+            uint64_t w = dqmc_philox_word(d.key, (uint64_t)k);
+            conf[k] = c.field >= 2 ? (int8_t)(1 + (int)(w >> 62)) : ((w >> 63) ? (int8_t)1 : (int8_t)-1);
+        }
+        d.ctr = cnt;
+        h->host_dirty = true;
+        if (int st = dqmc_set_field(h, i, conf.data())) return st;
+    }
+    return DQMC_OK;
+}
+
+int dqmc_set_rng(dqmc_handle* h, int chain, uint64_t key, uint64_t counter) {
+    if (int st = check_chain(h, chain)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    h->host[chain].key = key;
+    h->host[chain].ctr = counter;
+    h->host_dirty = true;
+    return DQMC_OK;
+}
+
+int dqmc_get_rng(dqmc_handle* h, int chain, uint64_t* key, uint64_t* counter) {
+    if (int st = check_chain(h, chain)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    if (key) *key = h->host[chain].key;
+    if (counter) *counter = h->host[chain].ctr;
+    return DQMC_OK;
+}
+
+int dqmc_initialize_run(dqmc_handle* h) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    return launch(h, DQMC_OP_BUILD, 0, 0, true);
+}
+int dqmc_build_stack(dqmc_handle* h) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    return launch(h, DQMC_OP_BUILD_FWD, 0, 0, true);
+}
+int dqmc_propagate(dqmc_handle* h) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    return launch(h, DQMC_OP_PROPAGATE, 0, 0, true);
+}
+int dqmc_sweep_spatial(dqmc_handle* h) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    return launch(h, DQMC_OP_SWEEP_SPATIAL, 0, 0, true);
+}
+
+static void fill_stats(const DqmcChain& d, dqmc_stats* s) {
+    s->accepted = d.accepted;
+    s->proposals = d.proposals;
+    s->propagation_errors = d.n_prop_err;
+    s->negative_probability = d.n_neg_p;
+    s->max_propagation_error = d.prop_err_max;
+    s->max_reported_error = d.prop_err_reported;
+    s->current_slice = d.current_slice;
+    s->current_range = d.current_range;
+    s->direction = d.direction;
+    s->status = d.status;
+}
+
+int dqmc_sweep(dqmc_handle* h, int n_sweeps, dqmc_stats* stats) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (n_sweeps < 0) return fail(DQMC_ERR_INVALID, "dqmc_sweep: n_sweeps < 0");
+    int st = launch(h, DQMC_OP_SWEEP, n_sweeps, 0, true);
+    if (st != DQMC_OK) return st;
+    if (stats)
+        for (size_t i = 0; i < h->host.size(); ++i) fill_stats(h->host[i], stats + i);
+    return DQMC_OK;
+}
+
+int dqmc_sweep_async(dqmc_handle* h, int n_sweeps) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (n_sweeps < 0) return fail(DQMC_ERR_INVALID, "dqmc_sweep_async: n_sweeps < 0");
+    return launch(h, DQMC_OP_SWEEP, n_sweeps, 0, false);
+}
+
+int dqmc_query(dqmc_handle* h) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (!h->busy) return DQMC_OK;
+    cudaError_t e = cudaStreamQuery(h->stream);
+    if (e == cudaErrorNotReady) return DQMC_ERR_NOT_READY;
+    if (e != cudaSuccess) return cuda_fail(e, "dqmc_query");
+    return dqmc_synchronize(h);
+}
+
+int dqmc_synchronize(dqmc_handle* h) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (!h->busy) return DQMC_OK;
+    h->busy = false;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "chain kernel");
+    int st = pull_descriptors(h);
+    if (st != DQMC_OK) return st;
+    for (size_t i = 0; i < h->host.size(); ++i)
+        if (h->host[i].status != 0)
+            return fail(DQMC_ERR_NUMERICAL, "chain " + std::to_string(i) + " reported status " +
+                                                 std::to_string(h->host[i].status));
+    return DQMC_OK;
+}
+
+int dqmc_get_stats(dqmc_handle* h, int chain, dqmc_stats* out) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!out) return fail(DQMC_ERR_INVALID, "dqmc_get_stats: null out");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    fill_stats(h->host[chain], out);
+    return DQMC_OK;
+}
+
+static int download_mat(dqmc_handle* h, int chain, const double* src, double* out) {
+    const size_t bytes = mat_elems(h->cfg[chain]) * sizeof(double);
+    CUDA_TRY(cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToHost, h->stream), "download matrix");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+// run `op` for one chain only: launch over a one-element descriptor array
+static int launch_one(dqmc_handle* h, int chain, int op, int arg0, int arg1) {
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    if (h->host_dirty) if (int st = push_descriptors(h)) return st;
+    CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains + chain, 1, op, arg0, arg1, h->stream),
+             "chain kernel launch");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "chain kernel");
+    return pull_descriptors(h);
+}
+
+int dqmc_get_greens(dqmc_handle* h, int chain, int physical, double* out) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!out) return fail(DQMC_ERR_INVALID, "dqmc_get_greens: null out");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    if (physical) {
+        if (int st = launch_one(h, chain, DQMC_OP_PHYSICAL, 0, 0)) return st;
+        return download_mat(h, chain, h->host[chain].out, out);
+    }
+    return download_mat(h, chain, h->host[chain].G, out);
+}
+
+int dqmc_set_greens(dqmc_handle* h, int chain, const double* in) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!in) return fail(DQMC_ERR_INVALID, "dqmc_set_greens: null in");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    CUDA_TRY(cudaMemcpyAsync(h->host[chain].G, in, mat_elems(h->cfg[chain]) * sizeof(double),
+                             cudaMemcpyHostToDevice, h->stream),
+             "upload greens");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+int dqmc_calculate_greens(dqmc_handle* h, int chain, int slice, int safe_mult, double* out) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!out) return fail(DQMC_ERR_INVALID, "dqmc_calculate_greens: null out");
+    if (slice < 0 || slice > h->cfg[chain].slices)
+        return fail(DQMC_ERR_INVALID, "dqmc_calculate_greens: slice out of range 0..M");
+    if (int st = launch_one(h, chain, DQMC_OP_GREENS_AT, slice, safe_mult)) return st;
+    return download_mat(h, chain, h->host[chain].out, out);
+}
+
+int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out) {
+    if (int st = check_chain(h, chain)) return st;
+    const DqmcChain& d = h->host[chain];
+    if (!out || which < 0 || which > 2 || idx < 1 || idx > d.nr + 1)
+        return fail(DQMC_ERR_INVALID, "dqmc_get_stack: bad arguments");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    const size_t ms = mat_elems(h->cfg[chain]);
+    if (which == 2) {
+        const size_t cnt = (size_t)d.nf * d.n;
+        CUDA_TRY(cudaMemcpyAsync(out, d.dstack + (idx - 1) * cnt, cnt * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h->stream),
+                 "download d_stack");
+        CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+        return DQMC_OK;
+    }
+    const double* base = which == 0 ? d.ustack : d.tstack;
+    return download_mat(h, chain, base + (idx - 1) * ms, out);
+}
+
+}  // extern "C"

@@ -1,0 +1,51 @@
+// Device-side description of one DQMC chain (one Markov chain of the
+// reference's DQMC: field configuration, Green's function and UDT stack).
+//
+// Layout in HBM (all FP64 matrices column-major, n x n per flavour block,
+// flavour block b of an nf-block matrix at offset b*n*n):
+//   G, Gtmp, Ul, Ur, Tl, Tr, tmp1, tmp2, currU, out    nf*n*n each
+//   ustack, tstack                                      (nr+1) * nf*n*n
+//   dstack                                              (nr+1) * nf*n
+//   Dl, Dr, tempv                                       nf*n
+//   pivot                                               nf*n (int32, 1-based)
+//   conf                                                n*M int8, site fastest
+//   eT2, eT2inv, eTh, eThinv                            n*n each (one block,
+//                                                       shared by both flavours)
+#pragma once
+#include <stdint.h>
+
+#define DQMC_MAX_CHUNKS 256
+
+struct DqmcChain {
+    // sizes
+    int n, nf, M, k, kind, nr, check_prop, prec;
+    // per-proposal tables computed on the host with the reference's
+    // expressions (fields.jl:388-393, 440-449, 563-573, 627-637):
+    //   Hirsch: index s_idx = (s > 0); GHQ: index (x_old-1)*4 + (x_new-1)
+    double delta0[16], delta1[16], wboson[16];
+    double gam[4];
+    // interaction exponentials (fields.jl:380-386, 429-438, 548-560, 618-624)
+    //   ev[f][v]: flavour block f, field value index v, power +1
+    //   evinv[f][v]: power -1.  Hirsch v = (s > 0); GHQ v = x - 1.
+    double ev[2][4], evinv[2][4];
+    // chunk ranges (generate_chunks), 1-based inclusive
+    int rfirst[DQMC_MAX_CHUNKS], rlast[DQMC_MAX_CHUNKS];
+    // buffers
+    int8_t* conf;
+    const double *eT2, *eT2inv, *eTh, *eThinv;
+    double *G, *Gtmp, *ustack, *tstack, *dstack, *Ul, *Ur, *Tl, *Tr, *Dl, *Dr, *tmp1, *tmp2,
+        *currU, *tempv, *out;
+    int* pivot;
+    float* mixG;  // FP32 scratch of the mixed-precision wrap (nf*n*n*2), or null
+    // RNG
+    uint64_t key, ctr;
+    // stack state (stack.jl:34-41)
+    int current_slice, current_range, direction, pad0;
+    // analysis (statistics.jl:9-51; stack.jl:644-653)
+    double prop_err_max, prop_err_reported;
+    long long n_prop_err, n_neg_p, accepted, proposals;
+    int status, pad1;
+};
+
+enum { DQMC_OP_SWEEP = 0, DQMC_OP_BUILD = 1, DQMC_OP_GREENS_AT = 2, DQMC_OP_PHYSICAL = 3,
+       DQMC_OP_BUILD_FWD = 4, DQMC_OP_PROPAGATE = 5, DQMC_OP_SWEEP_SPATIAL = 6 };

@@ -1,0 +1,270 @@
+// CTA-cooperative FP64 building blocks of the DQMC sweep.
+//
+// Every function here is executed by all threads of one CTA with uniform
+// control flow; one CTA owns one chain.  Matrices are column-major n x n FP64
+// blocks in global memory (L2-resident per chain), staged through shared
+// memory tiles.  On GB300 the FP64 pipe (DFMA) is the bound of this path, so
+// the functions aim at keeping DFMA issue busy and at issuing no FP64
+// instruction the reference's algorithm does not need.
+#pragma once
+#include <stdint.h>
+
+#include "dqmc_chain.h"
+#include "philox.h"
+
+#define DQMC_NT 256
+#define DQMC_NW (DQMC_NT / 32)
+#define DQMC_NMAX 512
+
+namespace dqmc {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void ident(int n, double* A) {
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
+        int i = e % n, j = e / n;
+        A[e] = (i == j) ? 1.0 : 0.0;
+    }
+}
+__device__ __forceinline__ void fill(int cnt, double* d, double v) {
+    for (int e = threadIdx.x; e < cnt; e += DQMC_NT) d[e] = v;
+}
+__device__ __forceinline__ void copy(int cnt, double* __restrict__ dst, const double* __restrict__ src) {
+    for (int e = threadIdx.x; e < cnt; e += DQMC_NT) dst[e] = src[e];
+}
+// C = Diagonal(d) * B  (real.jl:27-37)
+__device__ __forceinline__ void dleft(int n, double* __restrict__ C, const double* __restrict__ d,
+                                      const double* __restrict__ B) {
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) C[e] = d[e % n] * B[e];
+}
+// C = A * Diagonal(d)  (real.jl:16-26)
+__device__ __forceinline__ void dright(int n, double* __restrict__ C, const double* __restrict__ A,
+                                       const double* __restrict__ d) {
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) C[e] = A[e] * d[e / n];
+}
+
+// C = op(A) * op(B), op = transpose when TA / TB.  64 x 64 output tiles,
+// 4 x 4 outputs per thread, k staged 16 at a time through shared memory
+// (sm: 2 * 16 * 64 doubles).  C must not alias A or B.  Summation over k is
+// in ascending order with fused multiply-adds.
+template <bool TA, bool TB>
+__device__ __noinline__ void mm(int n, double* __restrict__ C, const double* __restrict__ A,
+                   const double* __restrict__ B, double* sm) {
+    double* sA = sm;            // [16][64]: sA[kk*64 + m]
+    double* sB = sm + 16 * 64;  // [16][64]: sB[kk*64 + j]
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    for (int n0 = 0; n0 < n; n0 += 64) {
+        for (int m0 = 0; m0 < n; m0 += 64) {
+            double acc[4][4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) acc[r][q] = 0.0;
+            for (int k0 = 0; k0 < n; k0 += 16) {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    int e = tid + t * DQMC_NT;
+                    int mm_, kk;
+                    if (!TA) { mm_ = e & 63; kk = e >> 6; } else { kk = e & 15; mm_ = e >> 4; }
+                    int gm = m0 + mm_, gk = k0 + kk;
+                    double v = 0.0;
+                    if (gm < n && gk < n) v = TA ? A[gk + (size_t)gm * n] : A[gm + (size_t)gk * n];
+                    sA[kk * 64 + mm_] = v;
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    int e = tid + t * DQMC_NT;
+                    int kk, jj;
+                    if (!TB) { kk = e & 15; jj = e >> 4; } else { jj = e & 63; kk = e >> 6; }
+                    int gk = k0 + kk, gj = n0 + jj;
+                    double v = 0.0;
+                    if (gk < n && gj < n) v = TB ? B[gj + (size_t)gk * n] : B[gk + (size_t)gj * n];
+                    sB[kk * 64 + jj] = v;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int kk = 0; kk < 16; ++kk) {
+                    double a[4], b[4];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) a[r] = sA[kk * 64 + tx + 16 * r];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) b[q] = sB[kk * 64 + ty + 16 * q];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) acc[r][q] = fma(a[r], b[q], acc[r][q]);
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int gm = m0 + tx + 16 * r, gj = n0 + ty + 16 * q;
+                    if (gm < n && gj < n) C[gm + (size_t)gj * n] = acc[r][q];
+                }
+        }
+    }
+}
+
+// udt_AVX_pivot! (UDT.jl:216-334) on one n x n block: Householder QR with
+// column pivoting (column norms recomputed every step, as indmaxcolumn does),
+// explicit Q by backward accumulation, D = |diag R| (0 -> 1), T = D^-1 R
+// pivoted (apply = true) or left unpivoted with the reflectors below the
+// diagonal (apply = false, consumed by rdivp).  scr: n*n scratch (apply only);
+// sv: n doubles of shared memory; sx: 2 shared doubles / ints.
+__device__ __noinline__ void udt_pivot(int n, double* __restrict__ U, double* __restrict__ D,
+                          double* __restrict__ In, int* __restrict__ piv, double* __restrict__ tau,
+                          bool apply, double* __restrict__ scr, double* sv, double* sxd, int* sxi) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    for (int i = tid; i < n; i += DQMC_NT) piv[i] = i + 1;
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        for (int col = j + warp; col < n; col += DQMC_NW) {
+            const double* x = In + (size_t)col * n;
+            double s = 0.0;
+            for (int r = j + lane; r < n; r += 32) s = fma(x[r], x[r], s);
+            s = warp_sum(s);
+            if (lane == 0) sv[col] = s;
+        }
+        __syncthreads();
+        if (warp == 0) {
+            double best = -1.0;
+            int bi = n;
+            for (int col = j + lane; col < n; col += 32) {
+                double v = sv[col];
+                if (v > best) { best = v; bi = col; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                double ob = __shfl_down_sync(0xffffffffu, best, o);
+                int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            if (lane == 0) sxi[0] = bi;
+        }
+        __syncthreads();
+        const int jm = sxi[0];
+        const double normu = sv[jm];
+        if (jm != j) {
+            double* a = In + (size_t)jm * n;
+            double* b = In + (size_t)j * n;
+            for (int r = tid; r < n; r += DQMC_NT) {
+                double t = a[r];
+                a[r] = b[r];
+                b[r] = t;
+            }
+            if (tid == 0) {
+                int tp = piv[jm];
+                piv[jm] = piv[j];
+                piv[j] = tp;
+            }
+            __syncthreads();
+        }
+        // reflector! (UDT.jl:157-172)
+        if (warp == 0) {
+            double* x = In + (size_t)j * n;
+            double xi1 = x[j];
+            double t = 0.0;
+            if (normu != 0.0) {
+                double nu = copysign(sqrt(normu), xi1);
+                xi1 += nu;
+                __syncwarp();
+                for (int r = j + 1 + lane; r < n; r += 32) x[r] = x[r] / xi1;
+                if (lane == 0) x[j] = -nu;
+                t = xi1 / nu;
+            }
+            if (lane == 0) { tau[j] = t; sxd[0] = t; }
+        }
+        __syncthreads();
+        // reflectorApply! (UDT.jl:53-70)
+        const double t = sxd[0];
+        const double* x = In + (size_t)j * n;
+        for (int col = j + 1 + warp; col < n; col += DQMC_NW) {
+            double* a = In + (size_t)col * n;
+            double aj = a[j];
+            double s = 0.0;
+            for (int r = j + 1 + lane; r < n; r += 32) s = fma(x[r], a[r], s);
+            s = warp_sum(s);
+            double vAj = t * (aj + s);
+            if (lane == 0) a[j] = aj - vAj;
+            for (int r = j + 1 + lane; r < n; r += 32) a[r] = fma(-x[r], vAj, a[r]);
+        }
+        __syncthreads();
+    }
+    // Calculate Q (UDT.jl:272-289)
+    ident(n, U);
+    __syncthreads();
+    if (tid == 0) U[(size_t)(n - 1) * n + (n - 1)] -= tau[n - 1];
+    __syncthreads();
+    for (int k = n - 2; k >= 0; --k) {
+        const double* v = In + (size_t)k * n;
+        const double t = tau[k];
+        for (int col = k + warp; col < n; col += DQMC_NW) {
+            double* u = U + (size_t)col * n;
+            double uk = u[k];
+            double s = 0.0;
+            for (int r = k + 1 + lane; r < n; r += 32) s = fma(v[r], u[r], s);
+            s = warp_sum(s);
+            double vB = t * (uk + s);
+            if (lane == 0) u[k] = uk - vB;
+            for (int r = k + 1 + lane; r < n; r += 32) u[r] = fma(-v[r], vB, u[r]);
+        }
+        __syncthreads();
+    }
+    // D (UDT.jl:293-301)
+    for (int i = tid; i < n; i += DQMC_NT) {
+        double xx = fabs(In[(size_t)i * n + i]);
+        D[i] = (xx == 0.0) ? 1.0 : xx;
+    }
+    __syncthreads();
+    // _apply_pivot! (UDT.jl:311-334)
+    if (apply) {
+        for (int e = tid; e < n * n; e += DQMC_NT) {
+            int i = e % n, j = e / n;
+            double d = 1.0 / D[i];
+            double val = (j >= i) ? d * In[e] : 0.0;
+            scr[i + (size_t)(piv[j] - 1) * n] = val;
+        }
+        __syncthreads();
+        copy(n * n, In, scr);
+    } else {
+        for (int e = tid; e < n * n; e += DQMC_NT) {
+            int i = e % n, j = e / n;
+            if (j >= i) {
+                double d = 1.0 / D[i];
+                In[e] = d * In[e];
+            }
+        }
+    }
+    __syncthreads();
+}
+
+// rdivp!: A <- A * P * T^-1 with T upper triangular (real.jl:198-226 for the
+// dense form, blockdiagonal.jl:286-324 for the block form, which multiplies
+// by 1/T[j,j] instead of dividing).  Rows of A are independent: one thread per
+// row runs the forward substitution.
+__device__ __noinline__ void rdivp(int n, double* __restrict__ A, const double* __restrict__ T,
+                      double* __restrict__ O, const int* __restrict__ piv, bool block_form) {
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
+        int i = e % n, j = e / n;
+        O[e] = A[i + (size_t)(piv[j] - 1) * n];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += DQMC_NT) {
+        for (int j = 0; j < n; ++j) {
+            const double* tj = T + (size_t)j * n;
+            double x = O[i + (size_t)j * n];
+            for (int k = 0; k < j; ++k) x = fma(-A[i + (size_t)k * n], tj[k], x);
+            double tjj = tj[j];
+            A[i + (size_t)j * n] = block_form ? x * (1.0 / tjj) : x / tjj;
+        }
+    }
+    __syncthreads();
+}
+
+}  // namespace dqmc

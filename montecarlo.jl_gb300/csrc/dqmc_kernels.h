@@ -1,0 +1,10 @@
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+#include "dqmc_chain.h"
+
+size_t dqmc_chain_kernel_smem();
+// One CTA per chain; op is one of DQMC_OP_*.
+cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
+                                     cudaStream_t stream);

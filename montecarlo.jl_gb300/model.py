@@ -1,0 +1,243 @@
+"""Hubbard model, parameters and Hubbard-Stratonovich fields (host side).
+
+Mirrors src/models/HubbardModel.jl, src/flavors/DQMC/parameters.jl and the
+field constructors of src/flavors/DQMC/fields.jl.  Sign convention is the
+reference's: ``U > 0`` is attractive (DensityHirschField), ``U < 0`` is
+repulsive (MagneticHirschField) -- HubbardModel.jl:15-16, 83.
+"""
+from __future__ import annotations
+
+import math
+import warnings
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+
+from .lattices import Lattice, choose_lattice
+
+# field kind numbering shared with include/dqmc_gb300.h
+DENSITY_HIRSCH = 0
+MAGNETIC_HIRSCH = 1
+DENSITY_GHQ = 2
+MAGNETIC_GHQ = 3
+
+
+class HubbardModel:
+    """``HubbardModel(l; U, mu, t)`` / ``HubbardModel(L, dims; ...)``
+    (HubbardModel.jl:23-46)."""
+
+    def __init__(self, l: Optional[Lattice] = None, dims: int = 2, L: int = 2,
+                 U: float = 1.0, mu: float = 0.0, t: float = 1.0, *args):
+        if isinstance(l, int):  # HubbardModel(L, dims; kwargs...)
+            L, dims, l = l, (dims if not args else args[0]), None
+        if l is None:
+            l = choose_lattice(dims, L)
+        if U < 0.0 and mu != 0.0:
+            warnings.warn(
+                f"A repulsive Hubbard model with chemical potential mu = {mu} will have a sign problem!")
+        self.t = float(t)
+        self.mu = float(mu)
+        self.U = float(U)
+        self.l = l
+
+    def __repr__(self):
+        kind = "repulsive" if self.U < 0 else "attractive"
+        return (f"{kind} Hubbard model\n\tParameters t = {self.t}, mu = {self.mu}, U = {self.U}\n"
+                f"\t{self.l.name} with {len(self.l)} sites")
+
+    @property
+    def lattice(self) -> Lattice:
+        return self.l
+
+    def choose_field(self):
+        """HubbardModel.jl:83."""
+        return MagneticHirschField if self.U < 0.0 else DensityHirschField
+
+    def hopping_matrix(self) -> np.ndarray:
+        """T = diag(-mu) - t * sum over directed bonds (HubbardModel.jl:112-124)."""
+        n = len(self.l)
+        T = np.zeros((n, n))
+        T[np.diag_indices(n)] = -self.mu
+        for fr, to in self.l.bonds(True):
+            T[to, fr] += -self.t
+        return T
+
+
+def AttractiveHubbardModel(*args, **kw):
+    return HubbardModel(*args, **kw)
+
+
+def RepulsiveHubbardModel(*args, **kw):
+    """HubbardModel.jl:49-53: flips the sign of U."""
+    kw = dict(kw)
+    kw["U"] = -kw.get("U", 1.0)
+    return HubbardModel(*args, **kw)
+
+
+@dataclass
+class DQMCParameters:
+    """parameters.jl:84-139."""
+
+    thermalization: int = 100
+    sweeps: int = 100
+    silent: bool = False
+    check_sign_problem: bool = True
+    check_propagation_error: bool = True
+    safe_mult: int = 10
+    delta_tau: float = 0.1
+    beta: float = 1.0
+    slices: int = 10
+    measure_rate: int = 10
+    print_rate: int = 10
+    checkerboard: bool = False
+
+    @classmethod
+    def make(cls, thermalization=100, sweeps=100, silent=False, check_sign_problem=True,
+             check_propagation_error=True, safe_mult=10, measure_rate=10, warn_round=True,
+             print_rate=None, checkerboard=False, **kw):
+        if checkerboard:
+            raise NotImplementedError("checkerboard hopping is not part of this library")
+        if print_rate is None:
+            print_rate = max(10, (thermalization + sweeps) // 100)
+        keys = set(kw)
+        if keys == {"beta"}:
+            kw = dict(beta=kw["beta"], delta_tau=0.1)
+            keys = set(kw)
+        if keys == {"delta_tau", "beta", "slices"}:
+            dt, beta = kw["delta_tau"], kw["beta"]
+            slices = _round_half_even(beta / dt)
+            if slices != kw["slices"]:
+                raise ValueError(f"Given slices ({kw['slices']}) does not match calculated slices "
+                                 f"beta/delta_tau ~ {slices}")
+        elif keys == {"beta", "slices"}:
+            beta, slices = kw["beta"], kw["slices"]
+            dt = beta / slices
+        elif keys == {"delta_tau", "slices"}:
+            dt, slices = kw["delta_tau"], kw["slices"]
+            beta = dt * slices
+        elif keys == {"delta_tau", "beta"}:
+            dt, beta = kw["delta_tau"], kw["beta"]
+            slices = _round_half_even(beta / dt)
+            if warn_round and not math.isclose(slices, beta / dt, rel_tol=1.5e-8):
+                warnings.warn(f"beta/delta_tau = {beta / dt} not an integer. Rounded to {slices}")
+        else:
+            raise ValueError(f"Invalid keyword arguments to DQMCParameters {kw}")
+        return cls(thermalization, sweeps, silent, check_sign_problem, check_propagation_error,
+                   safe_mult, float(dt), float(beta), int(slices), measure_rate, print_rate, False)
+
+
+def _round_half_even(x: float) -> int:
+    return int(round(x))  # Python rounds half to even, like Julia's round
+
+
+class _Field:
+    kind = -1
+    unique_flavors = 1
+    ghq = False
+
+    def __init__(self, param: DQMCParameters, model: HubbardModel, U: Optional[float] = None):
+        U = model.U if U is None else U
+        self.alpha = self._alpha(param.delta_tau, U)
+        self.n = len(model.l)
+        self.slices = param.slices
+        self.conf = np.zeros((self.n, self.slices), dtype=np.int8, order="F")
+
+    @staticmethod
+    def _real(x: complex, what: str) -> float:
+        if isinstance(x, complex):
+            if abs(x.imag) < 10 * np.spacing(abs(x.real)):
+                return x.real
+            raise NotImplementedError(
+                f"{what}: complex alpha (field / sign(U) mismatch) is the reference's complex path, "
+                "which this library does not implement")
+        return float(x)
+
+    def energy_boson(self, conf=None):
+        return 0.0
+
+
+class DensityHirschField(_Field):
+    """fields.jl:363-395: alpha = acosh(exp(0.5 dtau U))."""
+
+    kind = DENSITY_HIRSCH
+
+    def _alpha(self, dt, U):
+        x = math.exp(0.5 * dt * U)
+        if x < 1.0:
+            return self._real(complex(0, math.acos(x)), "DensityHirschField")
+        return math.acosh(x)
+
+    def energy_boson(self, conf=None):
+        conf = self.conf if conf is None else conf
+        return self.alpha * float(np.sum(conf))
+
+
+class MagneticHirschField(_Field):
+    """fields.jl:412-451: alpha = acosh(exp(-0.5 dtau U))."""
+
+    kind = MAGNETIC_HIRSCH
+    unique_flavors = 2
+
+    def _alpha(self, dt, U):
+        x = math.exp(-0.5 * dt * U)
+        if x < 1.0:
+            return self._real(complex(0, math.acos(x)), "MagneticHirschField")
+        return math.acosh(x)
+
+
+class DensityGHQField(_Field):
+    """fields.jl:589-637: alpha = sqrt(0.5 dtau U)."""
+
+    kind = DENSITY_GHQ
+    ghq = True
+
+    def _alpha(self, dt, U):
+        x = 0.5 * dt * U
+        if x < 0:
+            return self._real(complex(0, math.sqrt(-x)), "DensityGHQField")
+        return math.sqrt(x)
+
+
+class MagneticGHQField(_Field):
+    """fields.jl:519-573: alpha = sqrt(-0.5 dtau U)."""
+
+    kind = MAGNETIC_GHQ
+    unique_flavors = 2
+    ghq = True
+
+    def _alpha(self, dt, U):
+        x = -0.5 * dt * U
+        if x < 0:
+            return self._real(complex(0, math.sqrt(-x)), "MagneticGHQField")
+        return math.sqrt(x)
+
+
+def hopping_exponentials(T: np.ndarray, delta_tau: float):
+    """The four hopping exponentials of init_hopping_matrices (stack.jl:209-249):
+    exp(-dtau T), exp(+dtau T), exp(-dtau T / 2), exp(+dtau T / 2).
+
+    The reference's ``exp`` of a Hermitian matrix is an eigendecomposition
+    followed by copying the upper triangle into the lower one, so each result
+    is exactly symmetric; this does the same with numpy's ``eigh``.
+    """
+    if not np.array_equal(T, T.T):
+        if not np.allclose(T, T.T, rtol=math.sqrt(np.finfo(float).eps)):
+            raise ValueError("The hopping matrix is not approximately Hermitian.")
+        warnings.warn("The hopping matrix is not exactly Hermitian.")
+    lam, V = np.linalg.eigh(T)
+
+    def ex(c):
+        E = (V * np.exp(c * lam)) @ V.T
+        iu = np.triu_indices(E.shape[0], 1)
+        E[(iu[1], iu[0])] = E[iu]
+        return np.asfortranarray(E)
+
+    return ex(-delta_tau), ex(+delta_tau), ex(-0.5 * delta_tau), ex(+0.5 * delta_tau)
+
+
+def generate_chunks(length: int, max_chunk: int):
+    """stack.jl:154-158 (1-based inclusive (first, last) pairs)."""
+    n = -(-length // max_chunk)
+    step = length / n
+    return [(_round_half_even((i - 1) * step) + 1, _round_half_even(i * step)) for i in range(1, n + 1)]

@@ -1,0 +1,836 @@
+/*
+ * dqmc_oracle.c -- CPU FP64 restatement of the DQMC local-sweep path of
+ * carstenbauer/MonteCarlo.jl (TEST INFRASTRUCTURE ONLY; see dqmc_oracle.h).
+ *
+ * Reference files restated here (paths inside the reference project):
+ *   src/flavors/DQMC/stack.jl, fields.jl, greens.jl,
+ *   src/flavors/DQMC/linalg/{UDT,real,blockdiagonal,updates,fallbacks}.jl,
+ *   src/flavors/DQMC/updates/local_updates.jl.
+ * Loop orders of the matrix products are this file's own (the reference's
+ * @turbo loops have no fixed summation order either); the sequence of
+ * operations, chunking, pivoting and decisions follow the reference.
+ *
+ * The random stream is Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11),
+ * which replaces Julia's global RNG: draw d of a chain with seed s is
+ * philox(ctr = {d_lo, d_hi, 0, 0}, key = {s_lo, s_hi}); the 64-bit word is
+ * (out0 << 32) | out1.  Draws are consumed in the reference's order.
+ */
+#include "dqmc_oracle.h"
+
+#include <math.h>
+#include <pthread.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+/* ------------------------------------------------------------------ RNG */
+
+void oc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+    uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+    uint32_t k0 = key[0], k1 = key[1];
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+        uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+        uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+        uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+        c0 = hi1 ^ c1 ^ k0;
+        c1 = lo1;
+        c2 = hi0 ^ c3 ^ k1;
+        c3 = lo0;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+uint64_t oc_rng_word(uint64_t key, uint64_t ctr) {
+    uint32_t c[4] = {(uint32_t)ctr, (uint32_t)(ctr >> 32), 0u, 0u};
+    uint32_t k[2] = {(uint32_t)key, (uint32_t)(key >> 32)};
+    uint32_t o[4];
+    oc_philox4x32_10(c, k, o);
+    return ((uint64_t)o[0] << 32) | (uint64_t)o[1];
+}
+
+double oc_word_to_uniform(uint64_t w) { return (double)(w >> 11) * 0x1.0p-53; }
+
+/* ------------------------------------------------------------------ chain */
+
+struct OcChain {
+    int n, nf, M, k, kind, nr, check_prop;
+    int *rfirst, *rlast;          /* 1-based inclusive slice ranges (generate_chunks) */
+    double alpha;
+    double gam[4], eta[4];
+    double *eT2, *eT2inv, *eTh, *eThinv;
+    int8_t* conf;                 /* n x M, column-major (site fastest) */
+    uint64_t key, ctr;
+    double *u_stack, *t_stack, *d_stack;
+    double *Ul, *Ur, *Tl, *Tr, *Dl, *Dr, *greens, *greens_temp, *tmp1, *tmp2, *curr_U, *eV;
+    double *tempv, *scratch;
+    int64_t* pivot;
+    int current_slice, current_range, direction;
+    double prop_err_all, prop_err_reported;
+    long n_prop_err, n_neg_p, accepted;
+};
+
+int oc_generate_chunks(int length, int max_chunk, int* first, int* last) {
+    /* N_chunks = cld(length, max_chunk); step = length / N_chunks;
+       [round(Int,(i-1)*step)+1 : round(Int, i*step)]  (round half to even) */
+    int nch = (length + max_chunk - 1) / max_chunk;
+    double step = (double)length / (double)nch;
+    for (int i = 1; i <= nch; ++i) {
+        first[i - 1] = (int)nearbyint((double)(i - 1) * step) + 1;
+        last[i - 1] = (int)nearbyint((double)i * step);
+    }
+    return nch;
+}
+
+#define NN(c) ((size_t)(c)->n * (size_t)(c)->n)
+#define MATSZ(c) ((size_t)(c)->nf * NN(c))
+
+static double* dalloc(size_t cnt) {
+    double* p = (double*)calloc(cnt ? cnt : 1, sizeof(double));
+    return p;
+}
+
+/* ---------------------------------------------------------- block algebra */
+
+/* C = A * B, one n x n block, column-major (register-blocked, no aliasing). */
+static void gemm_nn(int n, double* restrict C, const double* restrict A, const double* restrict B) {
+    int j = 0;
+    for (; j + 4 <= n; j += 4) {
+        int i = 0;
+        for (; i + 8 <= n; i += 8) {
+            double acc[4][8];
+            for (int q = 0; q < 4; ++q)
+                for (int r = 0; r < 8; ++r) acc[q][r] = 0.0;
+            for (int k = 0; k < n; ++k) {
+                const double* a = A + (size_t)k * n + i;
+                for (int q = 0; q < 4; ++q) {
+                    double b = B[(size_t)(j + q) * n + k];
+                    for (int r = 0; r < 8; ++r) acc[q][r] += a[r] * b;
+                }
+            }
+            for (int q = 0; q < 4; ++q)
+                for (int r = 0; r < 8; ++r) C[(size_t)(j + q) * n + i + r] = acc[q][r];
+        }
+        for (; i < n; ++i) {
+            for (int q = 0; q < 4; ++q) {
+                double s = 0.0;
+                for (int k = 0; k < n; ++k) s += A[(size_t)k * n + i] * B[(size_t)(j + q) * n + k];
+                C[(size_t)(j + q) * n + i] = s;
+            }
+        }
+    }
+    for (; j < n; ++j) {
+        for (int i = 0; i < n; ++i) C[(size_t)j * n + i] = 0.0;
+        for (int k = 0; k < n; ++k) {
+            double b = B[(size_t)j * n + k];
+            const double* a = A + (size_t)k * n;
+            double* cc = C + (size_t)j * n;
+            for (int i = 0; i < n; ++i) cc[i] += a[i] * b;
+        }
+    }
+}
+
+static void transpose(int n, double* restrict out, const double* restrict A) {
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) out[(size_t)i * n + j] = A[(size_t)j * n + i];
+}
+
+/* C = A^T * B  (real.jl:82-91, vmul!(C, adjoint(A), B)) */
+static void gemm_tn(int n, double* C, const double* A, const double* B, double* scratch) {
+    transpose(n, scratch, A);
+    gemm_nn(n, C, scratch, B);
+}
+/* C = A * B^T  (real.jl:72-81, vmul!(C, A, adjoint(B))) */
+static void gemm_nt(int n, double* C, const double* A, const double* B, double* scratch) {
+    transpose(n, scratch, B);
+    gemm_nn(n, C, A, scratch);
+}
+/* C = Diagonal(d) * B  (real.jl:27-37) */
+static void diag_left(int n, double* C, const double* d, const double* B) {
+    for (int j = 0; j < n; ++j)
+        for (int i = 0; i < n; ++i) C[(size_t)j * n + i] = d[i] * B[(size_t)j * n + i];
+}
+/* C = A * Diagonal(d)  (real.jl:16-26) */
+static void diag_right(int n, double* C, const double* A, const double* d) {
+    for (int j = 0; j < n; ++j) {
+        double dj = d[j];
+        for (int i = 0; i < n; ++i) C[(size_t)j * n + i] = A[(size_t)j * n + i] * dj;
+    }
+}
+static void set_identity(int n, double* A) {
+    memset(A, 0, sizeof(double) * (size_t)n * n);
+    for (int i = 0; i < n; ++i) A[(size_t)i * n + i] = 1.0;
+}
+
+/* ------------------------------------------------------------------- UDT */
+
+/* indmaxcolumn, UDT.jl:175-192 (0-based j) */
+static int indmaxcolumn(int n, const double* A, int j, double* maxval) {
+    double sq = 0.0;
+    for (int k = j; k < n; ++k) sq += A[(size_t)j * n + k] * A[(size_t)j * n + k];
+    int ii = j;
+    for (int i = j + 1; i < n; ++i) {
+        double mi = 0.0;
+        const double* col = A + (size_t)i * n;
+        for (int k = j; k < n; ++k) mi += col[k] * col[k];
+        if (fabs(mi) > sq) { sq = mi; ii = i; }
+    }
+    *maxval = sq;
+    return ii;
+}
+
+void oc_udt_pivot(int n, double* U, double* D, double* input, int64_t* pivot, double* temp,
+                  int apply_pivot) {
+    for (int i = 0; i < n; ++i) pivot[i] = i + 1;
+    /* QR with column pivoting, UDT.jl:236-268 */
+    for (int j = 0; j < n; ++j) {
+        double normu;
+        int jm = indmaxcolumn(n, input, j, &normu);
+        if (jm != j) {
+            int64_t tp = pivot[jm]; pivot[jm] = pivot[j]; pivot[j] = tp;
+            double* a = input + (size_t)jm * n;
+            double* b = input + (size_t)j * n;
+            for (int i = 0; i < n; ++i) { double t = a[i]; a[i] = b[i]; b[i] = t; }
+        }
+        /* reflector!, UDT.jl:157-172 */
+        double* x = input + (size_t)j * n;
+        double tau;
+        double xi1 = x[j];
+        if (normu == 0.0) {
+            tau = 0.0;
+        } else {
+            double nrm = sqrt(normu);
+            double nu = copysign(nrm, xi1);
+            xi1 += nu;
+            x[j] = -nu;
+            for (int i = j + 1; i < n; ++i) x[i] /= xi1;
+            tau = xi1 / nu;
+        }
+        temp[j] = tau;
+        /* reflectorApply!(M, tau, k, n), UDT.jl:53-70 */
+        for (int jj = j + 1; jj < n; ++jj) {
+            double* col = input + (size_t)jj * n;
+            double vAj = col[j];
+            for (int i = j + 1; i < n; ++i) vAj += x[i] * col[i];
+            vAj = tau * vAj;
+            col[j] -= vAj;
+            for (int i = j + 1; i < n; ++i) col[i] -= x[i] * vAj;
+        }
+    }
+    /* Calculate Q, UDT.jl:272-289 */
+    set_identity(n, U);
+    U[(size_t)(n - 1) * n + (n - 1)] -= temp[n - 1];
+    for (int k = n - 2; k >= 0; --k) {
+        const double* v = input + (size_t)k * n;
+        for (int j = k; j < n; ++j) {
+            double* u = U + (size_t)j * n;
+            double vBj = u[k];
+            for (int i = k + 1; i < n; ++i) vBj += v[i] * u[i];
+            vBj = temp[k] * vBj;
+            u[k] -= vBj;
+            for (int i = k + 1; i < n; ++i) u[i] -= v[i] * vBj;
+        }
+    }
+    /* D, UDT.jl:293-301 */
+    for (int i = 0; i < n; ++i) {
+        double xx = fabs(input[(size_t)i * n + i]);
+        D[i] = (xx == 0.0) ? 1.0 : xx;
+    }
+    /* _apply_pivot!, UDT.jl:311-334 */
+    if (apply_pivot) {
+        for (int i = 0; i < n; ++i) {
+            double d = 1.0 / D[i];
+            for (int j = 0; j < i; ++j) temp[pivot[j] - 1] = 0.0;
+            for (int j = i; j < n; ++j) temp[pivot[j] - 1] = d * input[(size_t)j * n + i];
+            for (int j = 0; j < n; ++j) input[(size_t)j * n + i] = temp[j];
+        }
+    } else {
+        for (int i = 0; i < n; ++i) {
+            double d = 1.0 / D[i];
+            for (int j = i; j < n; ++j) input[(size_t)j * n + i] = d * input[(size_t)j * n + i];
+        }
+    }
+}
+
+/* rdivp!: A <- A * T^{-1} (pivoted), real.jl:198-226 / blockdiagonal.jl:286-324 */
+void oc_rdivp(int n, double* A, const double* T, double* O, const int64_t* pivot, int block_form) {
+    for (int j = 0; j < n; ++j) {
+        const double* src = A + (size_t)(pivot[j] - 1) * n;
+        double* dst = O + (size_t)j * n;
+        for (int i = 0; i < n; ++i) dst[i] = src[i];
+    }
+    for (int j = 0; j < n; ++j) {
+        double tjj = T[(size_t)j * n + j];
+        double inv = 1.0 / tjj;
+        double* aj = A + (size_t)j * n;
+        const double* oj = O + (size_t)j * n;
+        for (int i = 0; i < n; ++i) aj[i] = oj[i];
+        for (int k = 0; k < j; ++k) {
+            double tkj = T[(size_t)j * n + k];
+            const double* ak = A + (size_t)k * n;
+            for (int i = 0; i < n; ++i) aj[i] -= ak[i] * tkj;
+        }
+        if (block_form)
+            for (int i = 0; i < n; ++i) aj[i] = aj[i] * inv;
+        else
+            for (int i = 0; i < n; ++i) aj[i] = aj[i] / tjj;
+    }
+}
+
+/* calculate_greens_AVX!, stack.jl:442-496; all operations act per flavour block */
+static void calc_greens_blocks(int n, int nf, double* Ul, double* Dl, double* Tl, double* Ur,
+                               double* Dr, double* Tr, double* G, int64_t* pivot, double* temp,
+                               double* scratch) {
+    size_t nn = (size_t)n * n;
+    for (int b = 0; b < nf; ++b) {
+        double *ul = Ul + b * nn, *tl = Tl + b * nn, *ur = Ur + b * nn, *tr = Tr + b * nn,
+               *g = G + b * nn;
+        double *dl = Dl + b * n, *dr = Dr + b * n;
+        int64_t* pv = pivot + b * n;
+        double* tv = temp + b * n;
+        gemm_nt(n, g, tl, tr, scratch);          /* G = Tl * Tr'          */
+        diag_right(n, tr, g, dr);                /* Tr = G * Dr           */
+        diag_left(n, g, dl, tr);                 /* G = Dl * Tr           */
+        oc_udt_pivot(n, tr, dr, g, pv, tv, 0);   /* Tr, Dr, G = udt(G)    */
+        gemm_nn(n, tl, ul, tr);                  /* Tl = Ul * Tr          */
+        oc_rdivp(n, ur, g, ul, pv, nf > 1);      /* Ur = Ur * G^-1        */
+        gemm_tn(n, tr, tl, ur, scratch);         /* Tr = Tl' * Ur         */
+        for (int i = 0; i < n; ++i) tr[(size_t)i * n + i] += dr[i]; /* rvadd! */
+        oc_udt_pivot(n, ul, dr, tr, pv, tv, 0);  /* Ul, Dr, Tr = udt(Tr)  */
+        oc_rdivp(n, ur, tr, g, pv, nf > 1);      /* Ur = Ur * Tr^-1       */
+        gemm_nn(n, tr, tl, ul);                  /* Tr = Tl * Ul          */
+        for (int i = 0; i < n; ++i) dl[i] = 1.0 / dr[i]; /* vinv!        */
+        diag_right(n, ul, ur, dl);               /* Ul = Ur * Dl          */
+        gemm_nt(n, g, ul, tr, scratch);          /* G = Ul * Tr'          */
+    }
+}
+
+void oc_calculate_greens_avx(int n, int nf, double* Ul, double* Dl, double* Tl, double* Ur,
+                             double* Dr, double* Tr, double* G) {
+    int64_t* pivot = (int64_t*)calloc((size_t)nf * n, sizeof(int64_t));
+    double* temp = dalloc((size_t)nf * n);
+    double* scratch = dalloc((size_t)n * n);
+    calc_greens_blocks(n, nf, Ul, Dl, Tl, Ur, Dr, Tr, G, pivot, temp, scratch);
+    free(pivot); free(temp); free(scratch);
+}
+
+/* ------------------------------------------------------------ chain setup */
+
+OcChain* oc_create(int n, int nf, int M, int safe_mult, int kind, double alpha,
+                   const double* eT2, const double* eT2inv, const double* eTh,
+                   const double* eThinv, uint64_t seed, int check_propagation_error) {
+    OcChain* c = (OcChain*)calloc(1, sizeof(OcChain));
+    c->n = n; c->nf = nf; c->M = M; c->k = safe_mult; c->kind = kind; c->alpha = alpha;
+    c->check_prop = check_propagation_error;
+    int maxch = (M + safe_mult - 1) / safe_mult;
+    c->rfirst = (int*)calloc((size_t)maxch, sizeof(int));
+    c->rlast = (int*)calloc((size_t)maxch, sizeof(int));
+    c->nr = oc_generate_chunks(M, safe_mult, c->rfirst, c->rlast);
+    /* GHQ tables, fields.jl:531-534 / 601-604 */
+    double s6 = sqrt(6.0);
+    c->gam[0] = 1.0 - s6 / 3.0; c->gam[1] = 1.0 + s6 / 3.0;
+    c->gam[2] = 1.0 + s6 / 3.0; c->gam[3] = 1.0 - s6 / 3.0;
+    c->eta[0] = -sqrt(6.0 + 2.0 * s6); c->eta[1] = -sqrt(6.0 - 2.0 * s6);
+    c->eta[2] = sqrt(6.0 - 2.0 * s6);  c->eta[3] = sqrt(6.0 + 2.0 * s6);
+    size_t nn = (size_t)n * n;
+    c->eT2 = dalloc(nn); c->eT2inv = dalloc(nn); c->eTh = dalloc(nn); c->eThinv = dalloc(nn);
+    memcpy(c->eT2, eT2, nn * sizeof(double));
+    memcpy(c->eT2inv, eT2inv, nn * sizeof(double));
+    memcpy(c->eTh, eTh, nn * sizeof(double));
+    memcpy(c->eThinv, eThinv, nn * sizeof(double));
+    c->conf = (int8_t*)calloc((size_t)n * M, 1);
+    c->key = seed; c->ctr = 0;
+    size_t ms = (size_t)nf * nn;
+    c->u_stack = dalloc(ms * (c->nr + 1));
+    c->t_stack = dalloc(ms * (c->nr + 1));
+    c->d_stack = dalloc((size_t)nf * n * (c->nr + 1));
+    c->Ul = dalloc(ms); c->Ur = dalloc(ms); c->Tl = dalloc(ms); c->Tr = dalloc(ms);
+    c->Dl = dalloc((size_t)nf * n); c->Dr = dalloc((size_t)nf * n);
+    c->greens = dalloc(ms); c->greens_temp = dalloc(ms); c->tmp1 = dalloc(ms); c->tmp2 = dalloc(ms);
+    c->curr_U = dalloc(ms);
+    c->eV = dalloc((size_t)nf * n);
+    c->tempv = dalloc((size_t)nf * n);
+    c->scratch = dalloc(nn);
+    c->pivot = (int64_t*)calloc((size_t)nf * n, sizeof(int64_t));
+    /* initialize_stack, stack.jl:187-192 */
+    for (int b = 0; b < nf; ++b) {
+        set_identity(n, c->Ul + b * nn); set_identity(n, c->Ur + b * nn);
+        set_identity(n, c->Tl + b * nn); set_identity(n, c->Tr + b * nn);
+    }
+    for (int i = 0; i < nf * n; ++i) { c->Dl[i] = 1.0; c->Dr[i] = 1.0; }
+    return c;
+}
+
+void oc_destroy(OcChain* c) {
+    if (!c) return;
+    free(c->rfirst); free(c->rlast);
+    free(c->eT2); free(c->eT2inv); free(c->eTh); free(c->eThinv); free(c->conf);
+    free(c->u_stack); free(c->t_stack); free(c->d_stack);
+    free(c->Ul); free(c->Ur); free(c->Tl); free(c->Tr); free(c->Dl); free(c->Dr);
+    free(c->greens); free(c->greens_temp); free(c->tmp1); free(c->tmp2); free(c->curr_U);
+    free(c->eV); free(c->tempv); free(c->scratch); free(c->pivot);
+    free(c);
+}
+
+static inline uint64_t next_word(OcChain* c) { return oc_rng_word(c->key, c->ctr++); }
+
+void oc_init_random_conf(OcChain* c) {
+    size_t cnt = (size_t)c->n * c->M;
+    int ghq = (c->kind == OC_DENSITY_GHQ || c->kind == OC_MAGNETIC_GHQ);
+    for (size_t i = 0; i < cnt; ++i) {
+        uint64_t w = next_word(c);
+        if (ghq) c->conf[i] = (int8_t)(1 + (int)(w >> 62));
+        else c->conf[i] = (w >> 63) ? (int8_t)1 : (int8_t)-1;
+    }
+}
+void oc_set_conf(OcChain* c, const int8_t* conf) { memcpy(c->conf, conf, (size_t)c->n * c->M); }
+void oc_get_conf(const OcChain* c, int8_t* conf) { memcpy(conf, c->conf, (size_t)c->n * c->M); }
+void oc_set_rng(OcChain* c, uint64_t key, uint64_t counter) { c->key = key; c->ctr = counter; }
+uint64_t oc_get_rng_counter(const OcChain* c) { return c->ctr; }
+
+/* interaction_matrix_exp!, fields.jl:380-386, 429-438, 548-560, 618-624 */
+static void interaction_matrix_exp(OcChain* c, int slice, double power, double* eV) {
+    int n = c->n;
+    const int8_t* s = c->conf + (size_t)(slice - 1) * n;
+    double a = c->alpha;
+    switch (c->kind) {
+    case OC_DENSITY_HIRSCH:
+        for (int i = 0; i < n; ++i) eV[i] = exp(power * a * (double)s[i]);
+        break;
+    case OC_MAGNETIC_HIRSCH:
+        for (int i = 0; i < n; ++i) eV[i] = exp(power * a * (double)s[i]);
+        for (int i = 0; i < n; ++i) eV[i + n] = exp(-power * a * (double)s[i]);
+        break;
+    case OC_DENSITY_GHQ:
+        for (int i = 0; i < n; ++i) eV[i] = exp(+power * a * c->eta[s[i] - 1]);
+        break;
+    default: /* OC_MAGNETIC_GHQ */
+        for (int i = 0; i < n; ++i) eV[i] = exp(+power * a * c->eta[s[i] - 1]);
+        for (int i = 0; i < n; ++i) eV[i + n] = exp(-power * a * c->eta[s[i] - 1]);
+        break;
+    }
+}
+
+/* slice matrices, stack.jl:319-367 (hopping exponentials are Hermitian-wrapped,
+ * so vmul! multiplies with the transposed data: fallbacks.jl:67-68) */
+static void mult_slice_left(OcChain* c, int slice, double* M) {
+    int n = c->n; size_t nn = NN(c);
+    interaction_matrix_exp(c, slice, 1.0, c->eV);
+    for (int b = 0; b < c->nf; ++b) {
+        diag_left(n, c->tmp1 + b * nn, c->eV + b * n, M + b * nn);
+        gemm_tn(n, M + b * nn, c->eT2, c->tmp1 + b * nn, c->scratch);
+    }
+}
+static void mult_slice_right(OcChain* c, int slice, double* M) {
+    int n = c->n; size_t nn = NN(c);
+    interaction_matrix_exp(c, slice, 1.0, c->eV);
+    for (int b = 0; b < c->nf; ++b) {
+        gemm_nt(n, c->tmp1 + b * nn, M + b * nn, c->eT2, c->scratch);
+        diag_right(n, M + b * nn, c->tmp1 + b * nn, c->eV + b * n);
+    }
+}
+static void mult_slice_inv_right(OcChain* c, int slice, double* M) {
+    int n = c->n; size_t nn = NN(c);
+    interaction_matrix_exp(c, slice, -1.0, c->eV);
+    for (int b = 0; b < c->nf; ++b) {
+        diag_right(n, c->tmp1 + b * nn, M + b * nn, c->eV + b * n);
+        gemm_nt(n, M + b * nn, c->tmp1 + b * nn, c->eT2inv, c->scratch);
+    }
+}
+static void mult_slice_inv_left(OcChain* c, int slice, double* M) {
+    int n = c->n; size_t nn = NN(c);
+    interaction_matrix_exp(c, slice, -1.0, c->eV);
+    for (int b = 0; b < c->nf; ++b) {
+        gemm_tn(n, c->tmp1 + b * nn, c->eT2inv, M + b * nn, c->scratch);
+        diag_left(n, M + b * nn, c->eV + b * n, c->tmp1 + b * nn);
+    }
+}
+static void mult_daggered_slice_left(OcChain* c, int slice, double* M) {
+    int n = c->n; size_t nn = NN(c);
+    interaction_matrix_exp(c, slice, 1.0, c->eV);
+    for (int b = 0; b < c->nf; ++b) {
+        gemm_tn(n, c->tmp1 + b * nn, c->eT2, M + b * nn, c->scratch);
+        diag_left(n, M + b * nn, c->eV + b * n, c->tmp1 + b * nn);
+    }
+}
+
+static double* ustk(OcChain* c, int idx) { return c->u_stack + (size_t)(idx - 1) * MATSZ(c); }
+static double* tstk(OcChain* c, int idx) { return c->t_stack + (size_t)(idx - 1) * MATSZ(c); }
+static double* dstk(OcChain* c, int idx) { return c->d_stack + (size_t)(idx - 1) * c->nf * c->n; }
+
+static void mat_identity(OcChain* c, double* A) {
+    for (int b = 0; b < c->nf; ++b) set_identity(c->n, A + b * NN(c));
+}
+static void vec_ones(OcChain* c, double* d) {
+    for (int i = 0; i < c->nf * c->n; ++i) d[i] = 1.0;
+}
+static void mat_copy(OcChain* c, double* dst, const double* src) {
+    memcpy(dst, src, MATSZ(c) * sizeof(double));
+}
+static void vec_copy(OcChain* c, double* dst, const double* src) {
+    memcpy(dst, src, (size_t)c->nf * c->n * sizeof(double));
+}
+
+/* udt_AVX_pivot! on all blocks (blockdiagonal.jl:352-370) */
+static void udt_blocks(OcChain* c, double* U, double* D, double* input, int apply) {
+    for (int b = 0; b < c->nf; ++b)
+        oc_udt_pivot(c->n, U + b * NN(c), D + b * c->n, input + b * NN(c), c->pivot + b * c->n,
+                     c->tempv + b * c->n, apply);
+}
+static void gemm_blocks(OcChain* c, double* C, const double* A, const double* B) {
+    for (int b = 0; b < c->nf; ++b) gemm_nn(c->n, C + b * NN(c), A + b * NN(c), B + b * NN(c));
+}
+static void diag_right_blocks(OcChain* c, double* C, const double* A, const double* d) {
+    for (int b = 0; b < c->nf; ++b) diag_right(c->n, C + b * NN(c), A + b * NN(c), d + b * c->n);
+}
+
+/* add_slice_sequence_left, stack.jl:377-393 */
+static void add_slice_sequence_left(OcChain* c, int idx) {
+    mat_copy(c, c->curr_U, ustk(c, idx));
+    for (int s = c->rfirst[idx - 1]; s <= c->rlast[idx - 1]; ++s) mult_slice_left(c, s, c->curr_U);
+    diag_right_blocks(c, c->tmp1, c->curr_U, dstk(c, idx));
+    udt_blocks(c, ustk(c, idx + 1), dstk(c, idx + 1), c->tmp1, 1);
+    gemm_blocks(c, tstk(c, idx + 1), c->tmp1, tstk(c, idx));
+}
+/* add_slice_sequence_right, stack.jl:402-416 */
+static void add_slice_sequence_right(OcChain* c, int idx) {
+    mat_copy(c, c->curr_U, ustk(c, idx + 1));
+    for (int s = c->rlast[idx - 1]; s >= c->rfirst[idx - 1]; --s)
+        mult_daggered_slice_left(c, s, c->curr_U);
+    diag_right_blocks(c, c->tmp1, c->curr_U, dstk(c, idx + 1));
+    udt_blocks(c, ustk(c, idx), dstk(c, idx), c->tmp1, 1);
+    gemm_blocks(c, tstk(c, idx), c->tmp1, tstk(c, idx + 1));
+}
+
+/* calculate_greens(mc), stack.jl:509-516 */
+static void calculate_greens(OcChain* c, double* out) {
+    calc_greens_blocks(c->n, c->nf, c->Ul, c->Dl, c->Tl, c->Ur, c->Dr, c->Tr, out, c->pivot,
+                       c->tempv, c->scratch);
+}
+
+void oc_build_stack(OcChain* c) {
+    mat_identity(c, ustk(c, 1)); vec_ones(c, dstk(c, 1)); mat_identity(c, tstk(c, 1));
+    for (int i = 1; i <= c->nr; ++i) add_slice_sequence_left(c, i);
+    c->current_slice = c->M + 1;
+    c->current_range = c->nr;
+    c->direction = -1;
+    mat_copy(c, c->Ul, ustk(c, c->nr + 1)); vec_copy(c, c->Dl, dstk(c, c->nr + 1));
+    mat_copy(c, c->Tl, tstk(c, c->nr + 1));
+    mat_identity(c, c->Ur); vec_ones(c, c->Dr); mat_identity(c, c->Tr);
+    calculate_greens(c, c->greens);
+}
+
+void oc_reverse_build_stack(OcChain* c) {
+    mat_identity(c, ustk(c, c->nr + 1)); vec_ones(c, dstk(c, c->nr + 1));
+    mat_identity(c, tstk(c, c->nr + 1));
+    for (int i = c->nr; i >= 1; --i) add_slice_sequence_right(c, i);
+    c->current_slice = 0;
+    c->current_range = 1;
+    c->direction = 1;
+    mat_identity(c, c->Ul); vec_ones(c, c->Dl); mat_identity(c, c->Tl);
+    mat_copy(c, c->Ur, ustk(c, 1)); vec_copy(c, c->Dr, dstk(c, 1)); mat_copy(c, c->Tr, tstk(c, 1));
+    calculate_greens(c, c->greens);
+}
+
+void oc_wrap_greens(OcChain* c, double* gf, int curr_slice, int direction) {
+    if (direction == -1) {
+        mult_slice_inv_left(c, curr_slice - 1, gf);
+        mult_slice_right(c, curr_slice - 1, gf);
+    } else {
+        mult_slice_left(c, curr_slice, gf);
+        mult_slice_inv_right(c, curr_slice, gf);
+    }
+}
+
+static void record_prop_error(OcChain* c) {
+    double mx = 0.0;
+    size_t ms = MATSZ(c);
+    for (size_t i = 0; i < ms; ++i) {
+        double d = fabs(c->greens_temp[i] - c->greens[i]);
+        if (d > mx || d != d) mx = d;
+    }
+    if (mx > c->prop_err_all || mx != mx) c->prop_err_all = mx;
+    if (mx > 1e-7) {
+        c->n_prop_err++;
+        if (mx > c->prop_err_reported) c->prop_err_reported = mx;
+    }
+}
+
+void oc_propagate(OcChain* c) {
+    c->current_slice += c->direction;
+    if (c->direction == 1) {
+        if (c->current_slice == 1) {
+            mat_identity(c, ustk(c, 1)); vec_ones(c, dstk(c, 1)); mat_identity(c, tstk(c, 1));
+        } else if (c->current_slice - 1 == c->rlast[c->current_range - 1]) {
+            int idx = c->current_range;
+            mat_copy(c, c->Ur, ustk(c, idx + 1)); vec_copy(c, c->Dr, dstk(c, idx + 1));
+            mat_copy(c, c->Tr, tstk(c, idx + 1));
+            add_slice_sequence_left(c, idx);
+            mat_copy(c, c->Ul, ustk(c, idx + 1)); vec_copy(c, c->Dl, dstk(c, idx + 1));
+            mat_copy(c, c->Tl, tstk(c, idx + 1));
+            if (c->check_prop) mat_copy(c, c->greens_temp, c->greens);
+            oc_wrap_greens(c, c->greens_temp, c->current_slice - 1, 1);
+            calculate_greens(c, c->greens);
+            if (c->check_prop) record_prop_error(c);
+            if (c->current_range == c->nr) {
+                c->direction = -1;
+                oc_propagate(c);
+            } else {
+                c->current_range += 1;
+            }
+        } else {
+            oc_wrap_greens(c, c->greens, c->current_slice - 1, 1);
+        }
+    } else {
+        if (c->current_slice == c->M) {
+            mat_identity(c, ustk(c, c->nr + 1)); vec_ones(c, dstk(c, c->nr + 1));
+            mat_identity(c, tstk(c, c->nr + 1));
+            oc_wrap_greens(c, c->greens, c->current_slice + 1, -1);
+        } else if (c->current_slice + 1 == c->rfirst[c->current_range - 1]) {
+            int idx = c->current_range;
+            mat_copy(c, c->Ul, ustk(c, idx)); vec_copy(c, c->Dl, dstk(c, idx));
+            mat_copy(c, c->Tl, tstk(c, idx));
+            add_slice_sequence_right(c, idx);
+            mat_copy(c, c->Ur, ustk(c, idx)); vec_copy(c, c->Dr, dstk(c, idx));
+            mat_copy(c, c->Tr, tstk(c, idx));
+            if (c->check_prop) mat_copy(c, c->greens_temp, c->greens);
+            calculate_greens(c, c->greens);
+            if (c->check_prop) record_prop_error(c);
+            if (c->current_range == 1) {
+                c->direction = 1;
+                oc_propagate(c);
+            } else {
+                oc_wrap_greens(c, c->greens, c->current_slice + 1, -1);
+                c->current_range -= 1;
+            }
+        } else {
+            oc_wrap_greens(c, c->greens, c->current_slice + 1, -1);
+        }
+    }
+}
+
+void oc_initialize_run(OcChain* c) {
+    oc_reverse_build_stack(c);
+    oc_propagate(c);
+}
+
+/* update_greens!, fields.jl:271-286 with vldiv22!/vsub!/vmul!/vsubkron!
+ * (fields.jl:176-209, linalg/updates.jl:7-11, 48-54, 92-97) on one block */
+static void update_block(int n, double* G, double R, double delta, int i, double* IG, double* Gr) {
+    double invRD = delta / R;
+    for (int j = 0; j < n; ++j) IG[j] = -G[(size_t)i * n + j];
+    IG[i] += 1.0;
+    for (int j = 0; j < n; ++j) Gr[j] = invRD * G[(size_t)j * n + i];
+    for (int l = 0; l < n; ++l) {
+        double r = Gr[l];
+        double* g = G + (size_t)l * n;
+        for (int k = 0; k < n; ++k) g[k] -= IG[k] * r;
+    }
+}
+
+void oc_update_greens(int n, int nf, double* G, const double* delta, int i) {
+    double* IG = dalloc((size_t)n);
+    double* Gr = dalloc((size_t)n);
+    for (int b = 0; b < nf; ++b) {
+        double* g = G + (size_t)b * n * n;
+        double R = 1.0 + delta[b] * (1.0 - g[(size_t)i * n + i]);
+        update_block(n, g, R, delta[b], i, IG, Gr);
+    }
+    free(IG); free(Gr);
+}
+
+/* sweep_spatial, local_updates.jl:23-60 with propose_local / accept_local!
+ * (fields.jl:340-344, 388-393, 440-449, 497-503, 563-573, 627-637) */
+int oc_sweep_spatial(OcChain* c) {
+    int n = c->n, nf = c->nf;
+    size_t nn = NN(c);
+    int slice = c->current_slice;
+    int8_t* s = c->conf + (size_t)(slice - 1) * n;
+    double* IG = c->tempv;         /* n-vectors: reuse workspace not live here */
+    double* Gr = c->scratch;
+    int accepted = 0;
+    static const int8_t choices[4][3] = {{2, 3, 4}, {1, 3, 4}, {1, 2, 4}, {1, 2, 3}};
+    for (int i = 0; i < n; ++i) {
+        double delta[2], R[2], detratio, dEb, p;
+        int x_new = 0;
+        double* g0 = c->greens;
+        double* g1 = c->greens + nn;
+        switch (c->kind) {
+        case OC_DENSITY_HIRSCH:
+            dEb = -2.0 * c->alpha * (double)s[i];
+            delta[0] = exp(dEb) - 1.0;
+            R[0] = 1.0 + delta[0] * (1.0 - g0[(size_t)i * n + i]);
+            detratio = R[0] * R[0];
+            p = exp(-dEb) * detratio;
+            break;
+        case OC_MAGNETIC_HIRSCH:
+            dEb = -2.0 * c->alpha * (double)s[i];
+            delta[0] = exp(+dEb) - 1.0;
+            delta[1] = exp(-dEb) - 1.0;
+            R[0] = 1.0 + delta[0] * (1.0 - g0[(size_t)i * n + i]);
+            R[1] = 1.0 + delta[1] * (1.0 - g1[(size_t)i * n + i]);
+            detratio = R[0] * R[1];
+            p = exp(-0.0) * detratio;
+            break;
+        case OC_DENSITY_GHQ: {
+            int x_old = s[i];
+            uint64_t w = next_word(c);
+            int r = (int)(((unsigned __int128)w * 3u) >> 64);
+            x_new = choices[x_old - 1][r];
+            dEb = c->alpha * (c->eta[x_new - 1] - c->eta[x_old - 1]);
+            double er = exp(dEb);
+            delta[0] = er - 1.0;
+            R[0] = 1.0 + delta[0] * (1.0 - g0[(size_t)i * n + i]);
+            detratio = R[0] * R[0];
+            detratio = detratio * c->gam[x_new - 1] / c->gam[x_old - 1];
+            p = exp(-dEb) * detratio;
+            break;
+        }
+        default: { /* OC_MAGNETIC_GHQ */
+            int x_old = s[i];
+            uint64_t w = next_word(c);
+            int r = (int)(((unsigned __int128)w * 3u) >> 64);
+            x_new = choices[x_old - 1][r];
+            double er = exp(c->alpha * (c->eta[x_new - 1] - c->eta[x_old - 1]));
+            delta[0] = er - 1.0;
+            delta[1] = 1.0 / er - 1.0;
+            R[0] = 1.0 + delta[0] * (1.0 - g0[(size_t)i * n + i]);
+            R[1] = 1.0 + delta[1] * (1.0 - g1[(size_t)i * n + i]);
+            detratio = R[0] * R[1];
+            detratio = detratio * c->gam[x_new - 1] / c->gam[x_old - 1];
+            p = exp(-0.0) * detratio;
+            break;
+        }
+        }
+        if (p < 0.0) c->n_neg_p++;
+        int acc = 0;
+        if (p > 1.0) acc = 1;
+        else acc = oc_word_to_uniform(next_word(c)) < p;
+        if (acc) {
+            for (int b = 0; b < nf; ++b)
+                update_block(n, c->greens + b * nn, R[b], delta[b], i, IG, Gr);
+            if (c->kind == OC_DENSITY_HIRSCH || c->kind == OC_MAGNETIC_HIRSCH) s[i] = (int8_t)(-s[i]);
+            else s[i] = (int8_t)x_new;
+            accepted++;
+        }
+    }
+    c->accepted += accepted;
+    return accepted;
+}
+
+long oc_local_sweeps(OcChain* c, int nsweeps) {
+    long acc = 0;
+    for (int s = 0; s < nsweeps; ++s)
+        for (int t = 0; t < 2 * c->M; ++t) {
+            acc += oc_sweep_spatial(c);
+            oc_propagate(c);
+        }
+    return acc;
+}
+
+/* calculate_greens(mc, slice, output, field, safe_mult), stack.jl:525-583 */
+void oc_calculate_greens_at(OcChain* c, int slice, double* out, int safe_mult) {
+    if (safe_mult <= 0) safe_mult = c->k;
+    mat_identity(c, c->curr_U); mat_identity(c, c->Ur); vec_ones(c, c->Dr); mat_identity(c, c->Tr);
+    if (slice + 1 <= c->M) {
+        for (int k = c->M; k >= slice + 1; --k) {
+            mult_daggered_slice_left(c, k, c->curr_U);
+            if (k % safe_mult == 0) {
+                diag_right_blocks(c, c->tmp1, c->curr_U, c->Dr);
+                udt_blocks(c, c->curr_U, c->Dr, c->tmp1, 1);
+                mat_copy(c, c->tmp2, c->Tr);
+                gemm_blocks(c, c->Tr, c->tmp1, c->tmp2);
+            }
+        }
+        diag_right_blocks(c, c->tmp1, c->curr_U, c->Dr);
+        udt_blocks(c, c->Ur, c->Dr, c->tmp1, 1);
+        mat_copy(c, c->tmp2, c->Tr);
+        gemm_blocks(c, c->Tr, c->tmp1, c->tmp2);
+    }
+    mat_identity(c, c->curr_U); mat_identity(c, c->Ul); vec_ones(c, c->Dl); mat_identity(c, c->Tl);
+    if (slice >= 1) {
+        for (int k = 1; k <= slice; ++k) {
+            mult_slice_left(c, k, c->curr_U);
+            if (k % safe_mult == 0) {
+                diag_right_blocks(c, c->tmp1, c->curr_U, c->Dl);
+                udt_blocks(c, c->curr_U, c->Dl, c->tmp1, 1);
+                mat_copy(c, c->tmp2, c->Tl);
+                gemm_blocks(c, c->Tl, c->tmp1, c->tmp2);
+            }
+        }
+        diag_right_blocks(c, c->tmp1, c->curr_U, c->Dl);
+        udt_blocks(c, c->Ul, c->Dl, c->tmp1, 1);
+        mat_copy(c, c->tmp2, c->Tl);
+        gemm_blocks(c, c->Tl, c->tmp1, c->tmp2);
+    }
+    calculate_greens(c, out);
+}
+
+/* _greens!, greens.jl:114-125: eThalfplus * (G * eThalfminus) */
+void oc_greens_physical(OcChain* c, const double* src, double* out) {
+    int n = c->n;
+    size_t nn = NN(c);
+    double* tmp = dalloc(nn);
+    for (int b = 0; b < c->nf; ++b) {
+        gemm_nt(n, tmp, src + b * nn, c->eTh, c->scratch);
+        gemm_tn(n, out + b * nn, c->eThinv, tmp, c->scratch);
+    }
+    free(tmp);
+}
+
+void oc_get_greens(const OcChain* c, double* out) { memcpy(out, c->greens, MATSZ(c) * sizeof(double)); }
+void oc_set_greens(OcChain* c, const double* in) { memcpy(c->greens, in, MATSZ(c) * sizeof(double)); }
+
+void oc_get_state(const OcChain* c, int* st) {
+    st[0] = c->current_slice; st[1] = c->current_range; st[2] = c->direction; st[3] = c->nr;
+}
+
+void oc_get_stack(const OcChain* c, int which, int idx, double* out) {
+    OcChain* cc = (OcChain*)c;
+    if (which == 0) memcpy(out, ustk(cc, idx), MATSZ(c) * sizeof(double));
+    else if (which == 1) memcpy(out, tstk(cc, idx), MATSZ(c) * sizeof(double));
+    else memcpy(out, dstk(cc, idx), (size_t)c->nf * c->n * sizeof(double));
+}
+
+void oc_get_analysis(const OcChain* c, double* out) {
+    out[0] = c->prop_err_all;
+    out[1] = (double)c->n_prop_err;
+    out[2] = c->prop_err_reported;
+    out[3] = (double)c->n_neg_p;
+    out[4] = (double)c->accepted;
+}
+
+/* ---------------------------------------------------- threaded baseline */
+
+typedef struct {
+    OcChain** chains;
+    int first, count, nsweeps;
+} OcWork;
+
+static void* oc_worker(void* arg) {
+    OcWork* w = (OcWork*)arg;
+    for (int i = 0; i < w->count; ++i) oc_local_sweeps(w->chains[w->first + i], w->nsweeps);
+    return NULL;
+}
+
+double oc_run_chains_threaded(OcChain** chains, int nchains, int nsweeps, int threads) {
+    if (threads < 1) threads = 1;
+    if (threads > nchains) threads = nchains;
+    pthread_t* th = (pthread_t*)calloc((size_t)threads, sizeof(pthread_t));
+    OcWork* wk = (OcWork*)calloc((size_t)threads, sizeof(OcWork));
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    int base = nchains / threads, rem = nchains % threads, pos = 0;
+    for (int t = 0; t < threads; ++t) {
+        wk[t].chains = chains; wk[t].first = pos; wk[t].count = base + (t < rem ? 1 : 0);
+        wk[t].nsweeps = nsweeps;
+        pos += wk[t].count;
+        pthread_create(&th[t], NULL, oc_worker, &wk[t]);
+    }
+    for (int t = 0; t < threads; ++t) pthread_join(th[t], NULL);
+    clock_gettime(CLOCK_MONOTONIC, &t1);
+    free(th); free(wk);
+    return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
+}
