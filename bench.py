@@ -1,0 +1,385 @@
+#!/usr/bin/env python
+"""DQMC sweep throughput on GB300: sweeps/s of an ensemble of Hubbard-model chains.
+
+Workload (default): the repulsive Hubbard model at half filling on an 8x8
+periodic square lattice (N = 64, two spin flavours), t = 1, U = 4 in the
+physics convention (U = -4 in the reference's convention), mu = 0,
+MagneticHirschField, beta = 8, delta_tau = 0.1 (80 slices), safe_mult = 10,
+FP64, run as an ensemble of independent chains (seeds 2 + j), two per SM.
+One step = one sweep (2M slice visits x N proposals, with wraps and
+stabilisations) of every chain in one launch; ``value`` is aggregate sweeps/s.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                  [--workload c2|c1|c4] [--chains B]
+
+``--impl reference`` times the CPU restatement of the reference's algorithm
+(the oracle; the reference itself is Julia, which this machine cannot run) on
+all host cores with the same workload and prints the same JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "DQMC sweeps/s/GPU (plain FP64 path, batched ensemble)"
+
+WORKLOADS = {
+    # name: (lattice L, U (reference convention), beta, safe_mult, field, description)
+    "c2": (8, -4.0, 8.0, 10, "MagneticHirschField",
+           "8x8 square repulsive Hubbard U=4 (physics), mu=0, MagneticHirschField, beta=8, "
+           "dtau=0.1 (M=80), safe_mult=10, FP64"),
+    "c1": (4, 4.0, 4.0, 10, "DensityHirschField",
+           "4x4 square attractive Hubbard U=-4 (physics), mu=0, DensityHirschField, beta=4, "
+           "dtau=0.1 (M=40), safe_mult=10, FP64"),
+    "c4": (16, -4.0, 10.0, 10, "MagneticHirschField",
+           "16x16 square repulsive Hubbard U=4 (physics), mu=0, MagneticHirschField, beta=10, "
+           "dtau=0.1 (M=100), safe_mult=10, FP64"),
+}
+
+
+def sweep_flops(n, nf, M, nr, acc):
+    """Algorithmic FP64 flops of one sweep of one chain (O(n^3) terms only):
+    nf * n^3 * (12 M + 48 c + 4 a M) -- wraps 8M, slice chains 4M, UDT + T
+    update 2c(10/3 + 2), Green's reconstruction 2c(56/3), rank-1 updates 4aM."""
+    return nf * float(n) ** 3 * (12 * M + 48 * nr + 4 * acc * M)
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            if len(r) < 9:
+                continue
+            for k, nm in enumerate(names):
+                if r[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def setup_workload(pkg, name):
+    L, U, beta, k, field, desc = WORKLOADS[name]
+    model = pkg.HubbardModel(pkg.SquareLattice(L), U=U)
+    param = pkg.DQMCParameters.make(beta=beta, delta_tau=0.1, safe_mult=k)
+    fld = getattr(pkg, field)(param, model)
+    exps = pkg.hopping_exponentials(model.hopping_matrix(), param.delta_tau)
+    return model, param, fld, exps, desc
+
+
+def run_reference(args, pkg, rank):
+    """CPU restatement of the reference's sweep (oracle), all host threads."""
+    import oracle as O
+
+    O.use_fast_build(True)
+    model, param, fld, exps, desc = setup_workload(pkg, args.workload)
+    n = len(model.l)
+    threads = os.cpu_count() or 1
+    chains = []
+    for j in range(threads):
+        c = O.OracleChain(n, fld.unique_flavors, param.slices, param.safe_mult, fld.kind, fld.alpha,
+                          exps, 2 + j)
+        c.init_random_conf()
+        c.initialize_run()
+        chains.append(c)
+    # calibrate: one sweep of one chain
+    t = time.perf_counter()
+    chains[0].sweeps(1)
+    t1 = time.perf_counter() - t
+    per_step = max(1, int(round(args.cpu_budget / max(args.steps, 1) / t1)))
+    for _ in range(min(args.warmup, 1)):
+        O.run_chains_threaded(chains, 1, threads)
+    wall = 0.0
+    for _ in range(args.steps):
+        wall += O.run_chains_threaded(chains, per_step, threads)
+    value = threads * per_step * args.steps / wall
+    cores = threads
+    sample = (f"{threads} chains x {per_step * args.steps} sweeps ({per_step} per step) of the "
+              f"workload, one chain per host thread")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "sweeps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random HS fields)",
+        "config": {"workload": desc, "chains": threads, "ensemble": "independent chains"},
+        "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": cores, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+        "note": "reference is Julia (not installed on this machine); timed its C restatement "
+                "(oracle/dqmc_oracle.c, FMA contraction on)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(pkg, workload, budget_s):
+    """Bounded oracle run on all host threads (rank 0 only)."""
+    import oracle as O
+
+    O.use_fast_build(True)
+    model, param, fld, exps, desc = setup_workload(pkg, workload)
+    n = len(model.l)
+    threads = os.cpu_count() or 1
+    chains = []
+    for j in range(threads):
+        c = O.OracleChain(n, fld.unique_flavors, param.slices, param.safe_mult, fld.kind, fld.alpha,
+                          exps, 2 + j)
+        c.init_random_conf()
+        c.initialize_run()
+        chains.append(c)
+    t = time.perf_counter()
+    chains[0].sweeps(1)
+    t1 = time.perf_counter() - t
+    nsw = max(1, int(round(budget_s / t1)))
+    wall = O.run_chains_threaded(chains, nsw, threads)
+    return {"value": threads * nsw / wall, "unit": "sweeps/s", "cores": threads, "kind": "port",
+            "sample": f"{threads} chains x {nsw} sweeps, one chain per host thread "
+                      f"(C restatement of the reference, FMA contraction on)"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--chains", type=int, default=0, help="ensemble size (default 2 per SM)")
+    ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    import __graft_entry__ as g
+    pkg = g.load_package()
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        run_reference(args, pkg, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
+
+    from montecarlo_gb300 import build as B
+    B.build()
+    from montecarlo_gb300 import _lib
+
+    props = torch.cuda.get_device_properties(local_rank)
+    nsm = props.multi_processor_count
+    model, param, fld, exps, desc = setup_workload(pkg, args.workload)
+    n, nf, M = len(model.l), fld.unique_flavors, param.slices
+    nr = len(pkg.generate_chunks(M, param.safe_mult))
+    B_chains = args.chains or 2 * nsm
+
+    def configs(base_seed):
+        return [_lib.ChainConfig(n, nf, M, param.safe_mult, fld.kind, 1, fld.alpha, base_seed + j)
+                for j in range(B_chains)]
+
+    # ---- peak of the FP64 pipe, measured in this run (cuBLAS DGEMM 4096^3)
+    a = torch.randn(4096, 4096, device="cuda", dtype=torch.float64)
+    bm = torch.randn(4096, 4096, device="cuda", dtype=torch.float64)
+    for _ in range(2):
+        a @ bm
+    torch.cuda.synchronize()
+    best = 1e9
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        a @ bm
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    fp64_peak = 2 * 4096.0 ** 3 / best / 1e12
+    del a, bm
+    torch.cuda.empty_cache()
+
+    # ---- device-resident throughput (value)
+    seed0 = 2 + rank * B_chains
+    h = _lib.Handle(configs(seed0))
+    h.set_hopping(-1, exps)
+    h.init_random_field(-1)
+    # a dedicated stream: the library launches on it and the CUDA events below
+    # are recorded on it (the legacy default stream has handle 0)
+    stream = torch.cuda.Stream()
+    assert stream.cuda_stream != 0
+    h.set_stream(stream.cuda_stream)
+    h.initialize_run()
+    for _ in range(args.warmup):
+        h.sweep_async(1)
+    h.synchronize()
+    st0 = [h.stats(i) for i in range(B_chains)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    evs[0].record(stream)
+    for i in range(args.steps):
+        h.sweep_async(1)
+        evs[i + 1].record(stream)
+    h.synchronize()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    launch_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
+    elapsed = evs[0].elapsed_time(evs[-1]) / 1e3
+    if dist:
+        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    st1 = [h.stats(i) for i in range(B_chains)]
+    acc = sum(s1["accepted"] - s0["accepted"] for s0, s1 in zip(st0, st1)) / max(
+        1, sum(s1["proposals"] - s0["proposals"] for s0, s1 in zip(st0, st1)))
+    max_prop = max(s["max_propagation_error"] for s in st1)
+    value = world * B_chains * args.steps / elapsed
+    flops_launch = B_chains * sweep_flops(n, nf, M, nr, acc)
+    avg_launch = statistics.mean(launch_ms) / 1e3
+    achieved = flops_launch / avg_launch / 1e12
+    h.close()
+
+    # ---- end to end through the C ABI with host buffers
+    h2 = _lib.Handle(configs(seed0 + 10_000))
+    pin = torch.empty(4 * n * n, dtype=torch.float64, pin_memory=True)
+    pin_np = pin.numpy().reshape(4, n, n)
+    for m in range(4):
+        pin_np[m] = np.asarray(exps[m])
+    conf_pin = torch.empty(B_chains * n * M, dtype=torch.int8, pin_memory=True).numpy()
+    rng = np.random.default_rng(seed0)
+    conf_pin[:] = rng.choice(np.array([-1, 1], dtype=np.int8), size=conf_pin.size)
+    g_pin = torch.empty(B_chains * nf * n * n, dtype=torch.float64, pin_memory=True).numpy()
+    f_pin = torch.empty(B_chains * n * M, dtype=torch.int8, pin_memory=True).numpy()
+    h2.set_stream(stream.cuda_stream)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h2.set_hopping(-1, [pin_np[m].T for m in range(4)])  # symmetric: F-order views, no copy
+    for j in range(B_chains):
+        h2.set_field(j, conf_pin[j * n * M:(j + 1) * n * M].reshape(n, M, order="F"))
+    h2.initialize_run()
+    for i in range(args.steps):
+        h2.sweep(1)
+        for j in range(B_chains):
+            h2.greens_into(j, g_pin[j * nf * n * n:(j + 1) * nf * n * n])
+            buf = f_pin[j * n * M:(j + 1) * n * M]
+            _lib.check(_lib.load().dqmc_get_field(h2.h, j, _lib.i8ptr(buf)))
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    h2.close()
+    h2d = (4 * n * n * 8 + B_chains * n * M) / args.steps
+    d2h = B_chains * (nf * n * n * 8 + n * M + 0)
+
+    # DRAM traffic of the chain kernel from the committed ncu capture, scaled
+    # by chains (independent per-chain workspaces)
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "chain_kernel_traffic.json")
+    if os.path.exists(tpath):
+        tr = json.load(open(tpath))
+        if tr.get("workload") == args.workload:
+            traffic = tr["dram_bytes_per_launch"] * B_chains / tr["chains_captured"]
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_sample(pkg, args.workload, args.cpu_budget)
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded random Hubbard-Stratonovich fields)",
+            "config": {"workload": desc, "chains_per_gpu": B_chains, "parallelism": f"replicas{world}",
+                       "l2": "working set larger than L2 (no flush needed)",
+                       "chain_bytes": int(_lib.load().dqmc_chain_bytes(_lib.ChainConfig(
+                           n, nf, M, param.safe_mult, fld.kind, 1, fld.alpha, 0), 0))},
+            "e2e": {"value": world * B_chains * args.steps / e2e_s, "unit": "sweeps/s",
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "includes": "hopping + field upload, stack build, sweeps, per-sweep download "
+                                "of every chain's G and field"},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak,
+                         "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": traffic,
+                         "traffic_unit": "bytes per launch (ncu dram read+write)",
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run (FP64 pipe; "
+                                        "MEASURED_PEAKS.json has no FP64 figure)",
+                         "kernel": "dqmc::chain_kernel",
+                         "flops_per_launch": flops_launch,
+                         "avg_launch_ms": 1e3 * avg_launch},
+            "gpu_launches": args.steps,
+            "acceptance": acc, "max_propagation_error": max_prop,
+            "clocks": clk,
+        }
+        if cpu is not None:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -93,6 +93,10 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
 int dqmc_destroy(dqmc_handle* h);
 const char* dqmc_last_error(void);
 int dqmc_abi_version(void);
+/* Run the handle's work on a caller-owned cudaStream_t (passed as void*);
+ * NULL restores the handle's own stream.  Lets a host time or order the
+ * library's launches with its own CUDA events and streams. */
+int dqmc_set_stream(dqmc_handle* h, void* cuda_stream);
 /* Device bytes one chain needs (stack + Green's function workspace). */
 int64_t dqmc_chain_bytes(const dqmc_chain_config* cfg, int precision);
 
@@ -143,6 +147,7 @@ int dqmc_set_greens(dqmc_handle* h, int chain, const double* in);
 int dqmc_calculate_greens(dqmc_handle* h, int chain, int slice, int safe_mult, double* out);
 /* which: 0 u_stack, 1 t_stack (nf*n*n), 2 d_stack (nf*n); idx 1-based (stack.jl:13-15) */
 int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out);
+
 
 #ifdef __cplusplus
 }

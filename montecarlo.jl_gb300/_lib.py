@@ -51,7 +51,7 @@ EXPORTS = [
     "dqmc_set_rng", "dqmc_get_rng", "dqmc_initialize_run", "dqmc_build_stack", "dqmc_propagate",
     "dqmc_sweep_spatial", "dqmc_sweep", "dqmc_sweep_async", "dqmc_query", "dqmc_synchronize",
     "dqmc_get_stats", "dqmc_get_greens", "dqmc_set_greens", "dqmc_calculate_greens",
-    "dqmc_get_stack",
+    "dqmc_get_stack", "dqmc_set_stream",
 ]
 
 _lib = None
@@ -91,6 +91,7 @@ def load(path: str = LIB_PATH):
     L.dqmc_set_greens.argtypes = [P, C.c_int, dp]
     L.dqmc_calculate_greens.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
     L.dqmc_get_stack.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
+    L.dqmc_set_stream.argtypes = [P, C.c_void_p]
     _lib = L
     return L
 
@@ -145,6 +146,11 @@ class Handle:
 
     def cfg(self, chain):
         return self._cfg[chain]
+
+    def set_stream(self, stream_ptr):
+        """Run on a caller-owned cudaStream_t (an int handle, e.g. torch's
+        ``torch.cuda.current_stream().cuda_stream``); 0 restores the own stream."""
+        check(load().dqmc_set_stream(self.h, C.c_void_p(stream_ptr or None)))
 
     def set_hopping(self, chain, exps):
         e = [np.asfortranarray(x, dtype=np.float64) for x in exps]

@@ -10,8 +10,12 @@
 
 #include "../../include/dqmc_gb300.h"
 #include "dqmc_chain.h"
+#include "dqmc_host_tables.h"
 #include "dqmc_kernels.h"
 #include "philox.h"
+
+using dqmc_host::fill_tables;
+using dqmc_host::generate_chunks;
 
 namespace {
 
@@ -32,17 +36,6 @@ int cuda_fail(cudaError_t e, const char* what) {
         cudaError_t _e = (expr);                   \
         if (_e != cudaSuccess) return cuda_fail(_e, what); \
     } while (0)
-
-// generate_chunks (stack.jl:154-158)
-int generate_chunks(int length, int max_chunk, int* first, int* last) {
-    int nch = (length + max_chunk - 1) / max_chunk;
-    double step = (double)length / (double)nch;
-    for (int i = 1; i <= nch; ++i) {
-        first[i - 1] = (int)nearbyint((double)(i - 1) * step) + 1;
-        last[i - 1] = (int)nearbyint((double)i * step);
-    }
-    return nch;
-}
 
 size_t mat_elems(const dqmc_chain_config& c) { return (size_t)c.n_flavors * c.n_sites * c.n_sites; }
 
@@ -78,81 +71,13 @@ Layout layout_of(const dqmc_chain_config& c, int prec) {
     return L;
 }
 
-// Tables of the proposal / interaction exponentials, computed with the
-// reference's expressions in the reference's operation order.
-void fill_tables(DqmcChain& d, int kind, double alpha) {
-    const double s6 = sqrt(6.0);
-    const double gam[4] = {1.0 - s6 / 3.0, 1.0 + s6 / 3.0, 1.0 + s6 / 3.0, 1.0 - s6 / 3.0};
-    const double eta[4] = {-sqrt(6.0 + 2.0 * s6), -sqrt(6.0 - 2.0 * s6), sqrt(6.0 - 2.0 * s6),
-                           sqrt(6.0 + 2.0 * s6)};
-    for (int i = 0; i < 4; ++i) d.gam[i] = gam[i];
-    for (int i = 0; i < 16; ++i) { d.delta0[i] = 0.0; d.delta1[i] = 0.0; d.wboson[i] = 0.0; }
-    for (int f = 0; f < 2; ++f)
-        for (int v = 0; v < 4; ++v) { d.ev[f][v] = 0.0; d.evinv[f][v] = 0.0; }
-    const double a = alpha;
-    switch (kind) {
-    case DQMC_FIELD_DENSITY_HIRSCH:
-        for (int v = 0; v < 2; ++v) {
-            double s = v ? 1.0 : -1.0;
-            d.ev[0][v] = exp(1.0 * a * s);      // fields.jl:383
-            d.evinv[0][v] = exp(-1.0 * a * s);
-            double dE = -2.0 * a * s;           // fields.jl:389-390
-            d.delta0[v] = exp(dE) - 1;
-            d.wboson[v] = exp(-dE);             // local_updates.jl:31
-        }
-        break;
-    case DQMC_FIELD_MAGNETIC_HIRSCH:
-        for (int v = 0; v < 2; ++v) {
-            double s = v ? 1.0 : -1.0;
-            d.ev[0][v] = exp(1.0 * a * s);      // fields.jl:432
-            d.ev[1][v] = exp(-1.0 * a * s);     // fields.jl:435
-            d.evinv[0][v] = exp(-1.0 * a * s);
-            d.evinv[1][v] = exp(-(-1.0) * a * s);
-            double dE = -2.0 * a * s;           // fields.jl:441-443
-            d.delta0[v] = exp(+dE) - 1.0;
-            d.delta1[v] = exp(-dE) - 1.0;
-            d.wboson[v] = exp(-0.0);
-        }
-        break;
-    case DQMC_FIELD_DENSITY_GHQ:
-        for (int v = 0; v < 4; ++v) {
-            d.ev[0][v] = exp(+1.0 * a * eta[v]); // fields.jl:621
-            d.evinv[0][v] = exp(+(-1.0) * a * eta[v]);
-        }
-        for (int xo = 0; xo < 4; ++xo)
-            for (int xn = 0; xn < 4; ++xn) {
-                if (xo == xn) continue;
-                double dE = a * (eta[xn] - eta[xo]); // fields.jl:631-633
-                double er = exp(dE);
-                d.delta0[xo * 4 + xn] = er - 1.0;
-                d.wboson[xo * 4 + xn] = exp(-dE);
-            }
-        break;
-    default: /* DQMC_FIELD_MAGNETIC_GHQ */
-        for (int v = 0; v < 4; ++v) {
-            d.ev[0][v] = exp(+1.0 * a * eta[v]);    // fields.jl:553
-            d.ev[1][v] = exp(-1.0 * a * eta[v]);    // fields.jl:556
-            d.evinv[0][v] = exp(+(-1.0) * a * eta[v]);
-            d.evinv[1][v] = exp(-(-1.0) * a * eta[v]);
-        }
-        for (int xo = 0; xo < 4; ++xo)
-            for (int xn = 0; xn < 4; ++xn) {
-                if (xo == xn) continue;
-                double er = exp(a * (eta[xn] - eta[xo])); // fields.jl:567-569
-                d.delta0[xo * 4 + xn] = er - 1.0;
-                d.delta1[xo * 4 + xn] = 1 / er - 1.0;
-                d.wboson[xo * 4 + xn] = exp(-0.0);
-            }
-        break;
-    }
-}
-
 }  // namespace
 
 struct dqmc_handle {
     int device = 0;
     int precision = DQMC_PREC_FP64;
-    cudaStream_t stream = nullptr;
+    cudaStream_t stream = nullptr;      // stream in use (own or caller's)
+    cudaStream_t own_stream = nullptr;
     std::vector<dqmc_chain_config> cfg;
     std::vector<Layout> lay;
     std::vector<DqmcChain> host;  // descriptors (pointers into `arena`)
@@ -189,7 +114,9 @@ int push_descriptors(dqmc_handle* h) {
 }
 
 int launch(dqmc_handle* h, int op, int arg0, int arg1, bool sync) {
-    if (h->busy) {
+    // launches are stream-ordered, so queued asynchronous sweeps need no host
+    // synchronisation here; host-side descriptor edits synchronise first
+    if (h->busy && (sync || h->host_dirty)) {
         int st = dqmc_synchronize(h);
         if (st != DQMC_OK) return st;
     }
@@ -263,11 +190,12 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
         base[i] = total;
         total += h->lay.back().bytes;
     }
-    e = cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking);
+    e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreate"); }
+    h->stream = h->own_stream;
     e = cudaMalloc((void**)&h->arena, total);
     if (e != cudaSuccess) {
-        cudaStreamDestroy(h->stream);
+        cudaStreamDestroy(h->own_stream);
         delete h;
         return cuda_fail(e, "cudaMalloc chain workspace");
     }
@@ -275,7 +203,7 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_chains, sizeof(DqmcChain) * n_chains);
     if (e != cudaSuccess) {
         cudaFree(h->arena);
-        cudaStreamDestroy(h->stream);
+        cudaStreamDestroy(h->own_stream);
         delete h;
         return cuda_fail(e, "cudaMalloc chain descriptors");
     }
@@ -321,8 +249,16 @@ int dqmc_destroy(dqmc_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->arena) cudaFree(h->arena);
     if (h->d_chains) cudaFree(h->d_chains);
-    if (h->stream) cudaStreamDestroy(h->stream);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
+    return DQMC_OK;
+}
+
+int dqmc_set_stream(dqmc_handle* h, void* cuda_stream) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    h->stream = cuda_stream ? (cudaStream_t)cuda_stream : h->own_stream;
     return DQMC_OK;
 }
 
@@ -569,3 +505,5 @@ int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out) {
 }
 
 }  // extern "C"
+
+int dqmc_report_error(int code, const std::string& msg) { return fail(code, msg); }

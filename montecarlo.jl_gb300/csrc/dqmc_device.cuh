@@ -17,6 +17,7 @@
 #define DQMC_NMAX 512
 
 namespace dqmc {
+namespace {  // internal linkage: each translation unit gets its own copy
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -267,4 +268,5 @@ __device__ __noinline__ void rdivp(int n, double* __restrict__ A, const double* 
     __syncthreads();
 }
 
+}  // namespace
 }  // namespace dqmc

@@ -8,3 +8,7 @@ size_t dqmc_chain_kernel_smem();
 // One CTA per chain; op is one of DQMC_OP_*.
 cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
                                      cudaStream_t stream);
+
+#include <string>
+// Records `msg` as the calling thread's dqmc_last_error() text; returns `code`.
+int dqmc_report_error(int code, const std::string& msg);

@@ -20,27 +20,47 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libdqmc_oracle.so")
+# Same source built with floating-point contraction allowed (fused multiply-add
+# where the target has it): the timed CPU baseline, as the reference's
+# LoopVectorization loops also emit FMAs.  The parity build keeps every
+# product and sum separately rounded so it gives the same bits on x86_64 and
+# aarch64.
+FAST_LIB_PATH = os.path.join(HERE, "libdqmc_oracle_fast.so")
 
 
 def build(force: bool = False) -> str:
-    """Compile the oracle with gcc (portable flags: runs on x86_64 and aarch64)."""
+    """Compile both oracle builds with gcc (portable flags: x86_64 and aarch64)."""
     src = os.path.join(HERE, "dqmc_oracle.c")
-    if force or not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(src):
-        tmp = LIB_PATH + f".{os.getpid()}.tmp"
-        cmd = ["gcc", "-O3", "-std=gnu11", "-fPIC", "-shared", "-o", tmp, src, "-lm", "-lpthread"]
-        subprocess.run(cmd, check=True)
-        os.replace(tmp, LIB_PATH)
+    hdr = os.path.join(HERE, "dqmc_oracle.h")
+    for path, contract in ((LIB_PATH, "off"), (FAST_LIB_PATH, "fast")):
+        newest = max(os.path.getmtime(src), os.path.getmtime(hdr))
+        if force or not os.path.exists(path) or os.path.getmtime(path) < newest:
+            tmp = path + f".{os.getpid()}.tmp"
+            cmd = ["gcc", "-O3", "-std=gnu11", f"-ffp-contract={contract}", "-fPIC", "-shared",
+                   "-o", tmp, src, "-lm", "-lpthread"]
+            subprocess.run(cmd, check=True)
+            os.replace(tmp, path)
     return LIB_PATH
 
 
 _lib = None
+_fast = False
+
+
+def use_fast_build(flag: bool = True):
+    """Select the contraction-enabled build (CPU-baseline timing only); must be
+    called before the first oracle call."""
+    global _fast
+    if _lib is not None and flag != _fast:
+        raise RuntimeError("oracle library already loaded")
+    _fast = flag
 
 
 def lib():
     global _lib
     if _lib is None:
         build()
-        L = C.CDLL(LIB_PATH)
+        L = C.CDLL(FAST_LIB_PATH if _fast else LIB_PATH)
         P = C.c_void_p
         dp = C.POINTER(C.c_double)
         L.oc_create.restype = P
@@ -243,7 +263,7 @@ def run_chains_threaded(chains, nsweeps, threads):
 def udt_pivot(A, apply_pivot=True):
     """udt_AVX_pivot! on a dense n x n numpy array; returns U, D, T, pivot."""
     n = A.shape[0]
-    inp = np.asfortranarray(A, dtype=np.float64).copy()
+    inp = np.array(A, dtype=np.float64, order="F")
     U = np.zeros((n, n), order="F")
     D = np.zeros(n)
     piv = np.zeros(n, dtype=np.int64)
@@ -255,7 +275,7 @@ def udt_pivot(A, apply_pivot=True):
 
 def rdivp(A, T, pivot, block_form=False):
     n = A.shape[0]
-    a = np.asfortranarray(A, dtype=np.float64).copy()
+    a = np.array(A, dtype=np.float64, order="F")
     t = np.asfortranarray(T, dtype=np.float64)
     o = np.zeros((n, n), order="F")
     p = np.ascontiguousarray(pivot, dtype=np.int64)
