@@ -148,6 +148,25 @@ int dqmc_calculate_greens(dqmc_handle* h, int chain, int slice, int safe_mult, d
 /* which: 0 u_stack, 1 t_stack (nf*n*n), 2 d_stack (nf*n); idx 1-based (stack.jl:13-15) */
 int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out);
 
+/* ---- allocation-free Green's function ---------------------------------------
+ * No counterpart in the reference: an addition for callers that cannot
+ * allocate device memory when they need G -- hosts whose device memory budget
+ * is owned by their own pool allocator, or latency-critical loops where
+ * cudaMalloc / cudaFree would synchronise the device.  Computes the same
+ * calculate_greens(mc, slice) as dqmc_calculate_greens, without a handle and
+ * without allocating: all work matrices live in one fixed device array of the
+ * library (about 0.53 MB per GPU, held until the process exits).
+ *   d_hopping: device, 4 n x n FP64 blocks (the order of dqmc_set_hopping)
+ *   d_conf:    device, n x M int8 field configuration
+ *   d_out:     device, n_flavors*n*n FP64 result
+ * Limit: n_flavors * n_sites^2 <= 8192; larger chains return DQMC_ERR_INVALID.
+ * The work is queued on cuda_stream (NULL = legacy default stream); the result
+ * is ready when that stream reaches it.  The first call on a device looks up
+ * the array's address (make it before any stream capture).  All calls share
+ * the array: calls that overlap on the GPU race and must be serialised. */
+int dqmc_calculate_greens_noalloc(const dqmc_chain_config* cfg, const double* d_hopping,
+                                  const int8_t* d_conf, int slice, int safe_mult, double* d_out,
+                                  void* cuda_stream);
 
 #ifdef __cplusplus
 }
