@@ -136,6 +136,11 @@ int dqmc_sweep_async(dqmc_handle* h, int n_sweeps);
 int dqmc_query(dqmc_handle* h);       /* DQMC_OK when idle, DQMC_ERR_NOT_READY when busy */
 int dqmc_synchronize(dqmc_handle* h);
 int dqmc_get_stats(dqmc_handle* h, int chain, dqmc_stats* out);
+/* Replaces: the @bm / TimerOutputs sections (src/helpers.jl:83-131).  out[8]:
+ * SM cycles since creation spent in sweep_spatial, ordinary wraps, slice chains,
+ * UDT decompositions, Green's reconstruction, propagation checks, T updates,
+ * other. */
+int dqmc_get_timers(dqmc_handle* h, int chain, uint64_t* out);
 
 /* ---- outputs --------------------------------------------------------------
  * Replaces: mc.stack.greens (physical = 0) and greens!/_greens!

@@ -51,8 +51,11 @@ EXPORTS = [
     "dqmc_set_rng", "dqmc_get_rng", "dqmc_initialize_run", "dqmc_build_stack", "dqmc_propagate",
     "dqmc_sweep_spatial", "dqmc_sweep", "dqmc_sweep_async", "dqmc_query", "dqmc_synchronize",
     "dqmc_get_stats", "dqmc_get_greens", "dqmc_set_greens", "dqmc_calculate_greens",
-    "dqmc_get_stack", "dqmc_set_stream",
+    "dqmc_get_stack", "dqmc_set_stream", "dqmc_get_timers", "dqmc_calculate_greens_noalloc",
 ]
+
+PHASES = ["sweep_spatial", "wrap", "slice_chain", "udt", "greens", "prop_check", "t_update",
+          "other"]
 
 _lib = None
 
@@ -92,6 +95,7 @@ def load(path: str = LIB_PATH):
     L.dqmc_calculate_greens.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
     L.dqmc_get_stack.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
     L.dqmc_set_stream.argtypes = [P, C.c_void_p]
+    L.dqmc_get_timers.argtypes = [P, C.c_int, C.POINTER(C.c_uint64)]
     _lib = L
     return L
 
@@ -211,6 +215,12 @@ class Handle:
         s = Stats()
         check(load().dqmc_get_stats(self.h, chain, C.byref(s)))
         return s.as_dict()
+
+    def timers(self, chain):
+        """SM cycles per phase since creation (dict keyed by PHASES)."""
+        out = (C.c_uint64 * 8)()
+        check(load().dqmc_get_timers(self.h, chain, out))
+        return dict(zip(PHASES, list(out)))
 
     def _mat_buf(self, chain):
         cfg = self._cfg[chain]

@@ -43,7 +43,7 @@ struct Layout {
     size_t bytes;
     size_t off_conf, off_hop, off_G, off_Gtmp, off_Ul, off_Ur, off_Tl, off_Tr, off_tmp1, off_tmp2,
         off_currU, off_out, off_ustack, off_tstack, off_dstack, off_Dl, off_Dr, off_tempv,
-        off_pivot, off_mix;
+        off_pivot;
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -65,8 +65,6 @@ Layout layout_of(const dqmc_chain_config& c, int prec) {
     L.off_Dr = o; o = align256(o + nf * n * sizeof(double));
     L.off_tempv = o; o = align256(o + nf * n * sizeof(double));
     L.off_pivot = o; o = align256(o + nf * n * sizeof(int));
-    L.off_mix = o;
-    if (prec == DQMC_PREC_MIXED) o = align256(o + 4 * n * n * sizeof(float) + 2 * mat_elems(c) * sizeof(float));
     L.bytes = o;
     return L;
 }
@@ -233,7 +231,6 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
         d.Dl = (double*)(b + L.off_Dl); d.Dr = (double*)(b + L.off_Dr);
         d.tempv = (double*)(b + L.off_tempv);
         d.pivot = (int*)(b + L.off_pivot);
-        d.mixG = precision == DQMC_PREC_MIXED ? (float*)(b + L.off_mix) : nullptr;
         d.key = c.seed; d.ctr = 0;
         d.current_slice = 0; d.current_range = 1; d.direction = 1;
     }
@@ -430,6 +427,14 @@ int dqmc_get_stats(dqmc_handle* h, int chain, dqmc_stats* out) {
     if (!out) return fail(DQMC_ERR_INVALID, "dqmc_get_stats: null out");
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     fill_stats(h->host[chain], out);
+    return DQMC_OK;
+}
+
+int dqmc_get_timers(dqmc_handle* h, int chain, uint64_t* out) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!out) return fail(DQMC_ERR_INVALID, "dqmc_get_timers: null out");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    for (int p = 0; p < 8; ++p) out[p] = h->host[chain].timers[p];
     return DQMC_OK;
 }
 

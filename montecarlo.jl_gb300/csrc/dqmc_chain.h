@@ -36,7 +36,6 @@ struct DqmcChain {
     double *G, *Gtmp, *ustack, *tstack, *dstack, *Ul, *Ur, *Tl, *Tr, *Dl, *Dr, *tmp1, *tmp2,
         *currU, *tempv, *out;
     int* pivot;
-    float* mixG;  // FP32 scratch of the mixed-precision wrap (nf*n*n*2), or null
     // RNG
     uint64_t key, ctr;
     // stack state (stack.jl:34-41)
@@ -45,7 +44,19 @@ struct DqmcChain {
     double prop_err_max, prop_err_reported;
     long long n_prop_err, n_neg_p, accepted, proposals;
     int status, pad1;
+    // SM cycles spent per phase (thread 0's clock64 around each phase), the
+    // device counterpart of the reference's @bm / TimerOutputs sections
+    // (helpers.jl:83-131): see DQMC_PHASE_*
+    unsigned long long timers[8];
 };
+
+enum { DQMC_PHASE_SWEEP_SPATIAL = 0, DQMC_PHASE_WRAP = 1, DQMC_PHASE_SLICE_CHAIN = 2,
+       DQMC_PHASE_UDT = 3, DQMC_PHASE_GREENS = 4, DQMC_PHASE_PROP_CHECK = 5,
+       DQMC_PHASE_T_UPDATE = 6, DQMC_PHASE_OTHER = 7 };
 
 enum { DQMC_OP_SWEEP = 0, DQMC_OP_BUILD = 1, DQMC_OP_GREENS_AT = 2, DQMC_OP_PHYSICAL = 3,
        DQMC_OP_BUILD_FWD = 4, DQMC_OP_PROPAGATE = 5, DQMC_OP_SWEEP_SPATIAL = 6 };
+
+// DqmcChain::prec values (same numbers as DQMC_PREC_* of the C ABI)
+#define DQMC_PREC_FP64_ID 0
+#define DQMC_PREC_MIXED_ID 1

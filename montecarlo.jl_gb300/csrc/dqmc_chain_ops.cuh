@@ -12,15 +12,23 @@ namespace dqmc {
 namespace {  // internal linkage: each translation unit gets its own copy
 
 struct Smem {
-    double tiles[2 * 16 * 64];   // mm() staging
+    union {                      // never live at the same time
+        double tiles[2 * 16 * 64];  // mm() / mm_df() staging
+        struct {
+            double col[2][DQMC_NMAX];  // rank-1: (I - G)[:, i] per block
+            double row[2][DQMC_NMAX];  // rank-1: (Delta/R) G[i, :] per block
+        } r1;
+    };
     double sv[DQMC_NMAX];        // column norms / small vectors
     double ev[2 * DQMC_NMAX];    // interaction exponential of the current slice
-    double col[2][DQMC_NMAX];    // rank-1: (I - G)[:, i] per block
-    double row[2][DQMC_NMAX];    // rank-1: (Delta/R) G[i, :] per block
     double sxd[4];
     double red[DQMC_NW];
     int sxi[4];
     DqmcChain c;                 // this CTA's chain (state mutated here, written back at exit)
+    double arena[2 * 64 * 65];   // shared-memory QR of one block when n <= 64; between
+                                 // stabilisations of a sweep it holds G (G-resident mode)
+    double* Gglob;               // the chain's G in global memory
+    int gres;                    // G currently lives in `arena`
 };
 
 struct Ctx {
@@ -31,6 +39,59 @@ struct Ctx {
 };
 
 __device__ __forceinline__ double* blk(double* p, const Ctx& x, int b) { return p + (size_t)b * x.nn; }
+
+// G-resident mode (n <= 64): during sweeps G stays in shared memory for the
+// rank-1 updates and wraps, and moves to global memory while a stabilisation
+// needs the arena for its QR factorisations.
+__device__ __forceinline__ bool g_resident_possible(const Ctx& x) {
+    return x.n <= 64 && (size_t)x.nf * x.nn <= sizeof(x.s->arena) / sizeof(double);
+}
+__device__ void g_to_arena(const Ctx& x) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) x.s->arena[e] = x.s->Gglob[e];
+    __syncthreads();
+    if (threadIdx.x == 0) { x.c->G = x.s->arena; x.s->gres = 1; }
+    __syncthreads();
+}
+__device__ void g_to_global(const Ctx& x) {
+    __syncthreads();
+    for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) x.s->Gglob[e] = x.s->arena[e];
+    __syncthreads();
+    if (threadIdx.x == 0) { x.c->G = x.s->Gglob; x.s->gres = 0; }
+    __syncthreads();
+}
+
+// UDT of one flavour block: in shared memory for n <= 64, else from global memory
+__device__ __forceinline__ void udt_one(const Ctx& x, double* U, double* D, double* In, int b,
+                                        bool apply) {
+    if (x.n <= 64)
+        udt_pivot_sm(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
+                     x.s->arena, x.s->arena + x.n * (x.n + 1), x.s->sv, x.s->sxd);
+    else
+        udt_pivot(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
+                  blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->sxi);
+}
+
+
+// phase timers: thread 0 accumulates SM cycles per DQMC_PHASE_*
+__device__ __forceinline__ long long phase_start() { return threadIdx.x == 0 ? clock64() : 0; }
+__device__ __forceinline__ void phase_stop(const Ctx& x, int phase, long long t0) {
+    if (threadIdx.x == 0) x.c->timers[phase] += (unsigned long long)(clock64() - t0);
+}
+
+// Slice-matrix products (wraps and slice chains): FP64, or on a
+// mixed-precision chain the double-float product on the FP32 pipe.  The UDT,
+// the Green's reconstruction, the T updates, the determinant ratios and the
+// rank-1 updates stay FP64 on every chain.
+template <bool TA, bool TB>
+__device__ __forceinline__ void smm(const Ctx& x, bool wrap, double* C, const double* A,
+                                    const double* B) {
+    (void)wrap;
+    if (x.c->prec == DQMC_PREC_MIXED_ID)
+        mm_df<TA, TB>(x.n, C, A, B, x.s->tiles);
+    else
+        mm<TA, TB>(x.n, C, A, B, x.s->tiles);
+}
 
 // interaction_matrix_exp! (fields.jl:380-386, 429-438, 548-560, 618-624)
 // into shared memory: ev[b*n + i]
@@ -47,40 +108,40 @@ __device__ __noinline__ void interaction_exp(const Ctx& x, int slice, bool inver
 }
 
 // multiply_slice_matrix_left!: M <- eT2 * eV * M  (stack.jl:319-327)
-__device__ __noinline__ void slice_left(const Ctx& x, int slice, double* M) {
+__device__ __noinline__ void slice_left(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, false);
     for (int b = 0; b < x.nf; ++b) {
         dleft(x.n, blk(x.c->tmp1, x, b), x.s->ev + b * x.n, blk(M, x, b));
         __syncthreads();
-        mm<true, false>(x.n, blk(M, x, b), x.c->eT2, blk(x.c->tmp1, x, b), x.s->tiles);
+        smm<true, false>(x, wrap, blk(M, x, b), x.c->eT2, blk(x.c->tmp1, x, b));
         __syncthreads();
     }
 }
 // multiply_slice_matrix_right!: M <- M * eT2 * eV  (stack.jl:329-337)
-__device__ __noinline__ void slice_right(const Ctx& x, int slice, double* M) {
+__device__ __noinline__ void slice_right(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, false);
     for (int b = 0; b < x.nf; ++b) {
-        mm<false, true>(x.n, blk(x.c->tmp1, x, b), blk(M, x, b), x.c->eT2, x.s->tiles);
+        smm<false, true>(x, wrap, blk(x.c->tmp1, x, b), blk(M, x, b), x.c->eT2);
         __syncthreads();
         dright(x.n, blk(M, x, b), blk(x.c->tmp1, x, b), x.s->ev + b * x.n);
         __syncthreads();
     }
 }
 // multiply_slice_matrix_inv_right!: M <- M * eV^-1 * eT2^-1  (stack.jl:339-347)
-__device__ __noinline__ void slice_inv_right(const Ctx& x, int slice, double* M) {
+__device__ __noinline__ void slice_inv_right(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, true);
     for (int b = 0; b < x.nf; ++b) {
         dright(x.n, blk(x.c->tmp1, x, b), blk(M, x, b), x.s->ev + b * x.n);
         __syncthreads();
-        mm<false, true>(x.n, blk(M, x, b), blk(x.c->tmp1, x, b), x.c->eT2inv, x.s->tiles);
+        smm<false, true>(x, wrap, blk(M, x, b), blk(x.c->tmp1, x, b), x.c->eT2inv);
         __syncthreads();
     }
 }
 // multiply_slice_matrix_inv_left!: M <- eV^-1 * eT2^-1 * M  (stack.jl:349-357)
-__device__ __noinline__ void slice_inv_left(const Ctx& x, int slice, double* M) {
+__device__ __noinline__ void slice_inv_left(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, true);
     for (int b = 0; b < x.nf; ++b) {
-        mm<true, false>(x.n, blk(x.c->tmp1, x, b), x.c->eT2inv, blk(M, x, b), x.s->tiles);
+        smm<true, false>(x, wrap, blk(x.c->tmp1, x, b), x.c->eT2inv, blk(M, x, b));
         __syncthreads();
         dleft(x.n, blk(M, x, b), x.s->ev + b * x.n, blk(x.c->tmp1, x, b));
         __syncthreads();
@@ -90,7 +151,7 @@ __device__ __noinline__ void slice_inv_left(const Ctx& x, int slice, double* M) 
 __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* M) {
     interaction_exp(x, slice, false);
     for (int b = 0; b < x.nf; ++b) {
-        mm<true, false>(x.n, blk(x.c->tmp1, x, b), x.c->eT2, blk(M, x, b), x.s->tiles);
+        smm<true, false>(x, false, blk(x.c->tmp1, x, b), x.c->eT2, blk(M, x, b));
         __syncthreads();
         dleft(x.n, blk(M, x, b), x.s->ev + b * x.n, blk(x.c->tmp1, x, b));
         __syncthreads();
@@ -100,11 +161,11 @@ __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* 
 // wrap_greens! (stack.jl:594-603)
 __device__ void wrap_greens(const Ctx& x, double* gf, int curr_slice, int direction) {
     if (direction == -1) {
-        slice_inv_left(x, curr_slice - 1, gf);
-        slice_right(x, curr_slice - 1, gf);
+        slice_inv_left(x, curr_slice - 1, gf, true);
+        slice_right(x, curr_slice - 1, gf, true);
     } else {
-        slice_left(x, curr_slice, gf);
-        slice_inv_right(x, curr_slice, gf);
+        slice_left(x, curr_slice, gf, true);
+        slice_inv_right(x, curr_slice, gf, true);
     }
 }
 
@@ -123,9 +184,7 @@ __device__ void mat_ident(const Ctx& x, double* A) {
 }
 
 __device__ __noinline__ void udt_blocks(const Ctx& x, double* U, double* D, double* In, bool apply) {
-    for (int b = 0; b < x.nf; ++b)
-        udt_pivot(x.n, blk(U, x, b), D + b * x.n, blk(In, x, b), x.c->pivot + b * x.n,
-                  x.c->tempv + b * x.n, apply, blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->sxi);
+    for (int b = 0; b < x.nf; ++b) udt_one(x, blk(U, x, b), D + b * x.n, blk(In, x, b), b, apply);
 }
 __device__ __noinline__ void mm_blocks(const Ctx& x, double* C, double* A, double* B) {
     for (int b = 0; b < x.nf; ++b) {
@@ -143,20 +202,32 @@ __device__ __noinline__ void add_slice_sequence_left(const Ctx& x, int idx) {
     DqmcChain& c = *x.c;
     copy(x.nf * (int)x.nn, c.currU, ustk(x, idx));
     __syncthreads();
+    long long t0 = phase_start();
     for (int s = c.rfirst[idx - 1]; s <= c.rlast[idx - 1]; ++s) slice_left(x, s, c.currU);
     dright_blocks(x, c.tmp1, c.currU, dstk(x, idx));
+    phase_stop(x, DQMC_PHASE_SLICE_CHAIN, t0);
+    t0 = phase_start();
     udt_blocks(x, ustk(x, idx + 1), dstk(x, idx + 1), c.tmp1, true);
+    phase_stop(x, DQMC_PHASE_UDT, t0);
+    t0 = phase_start();
     mm_blocks(x, tstk(x, idx + 1), c.tmp1, tstk(x, idx));
+    phase_stop(x, DQMC_PHASE_T_UPDATE, t0);
 }
 // add_slice_sequence_right (stack.jl:402-416)
 __device__ __noinline__ void add_slice_sequence_right(const Ctx& x, int idx) {
     DqmcChain& c = *x.c;
     copy(x.nf * (int)x.nn, c.currU, ustk(x, idx + 1));
     __syncthreads();
+    long long t0 = phase_start();
     for (int s = c.rlast[idx - 1]; s >= c.rfirst[idx - 1]; --s) slice_dagger_left(x, s, c.currU);
     dright_blocks(x, c.tmp1, c.currU, dstk(x, idx + 1));
+    phase_stop(x, DQMC_PHASE_SLICE_CHAIN, t0);
+    t0 = phase_start();
     udt_blocks(x, ustk(x, idx), dstk(x, idx), c.tmp1, true);
+    phase_stop(x, DQMC_PHASE_UDT, t0);
+    t0 = phase_start();
     mm_blocks(x, tstk(x, idx), c.tmp1, tstk(x, idx + 1));
+    phase_stop(x, DQMC_PHASE_T_UPDATE, t0);
 }
 
 // calculate_greens_AVX! (stack.jl:442-496), per flavour block
@@ -176,7 +247,7 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout) {
         __syncthreads();
         dleft(n, g, dl, tr);
         __syncthreads();
-        udt_pivot(n, tr, dr, g, pv, tv, false, nullptr, x.s->sv, x.s->sxd, x.s->sxi);
+        udt_one(x, tr, dr, g, b, false);
         mm<false, false>(n, tl, ul, tr, x.s->tiles);
         __syncthreads();
         rdivp(n, ur, g, ul, pv, bf);
@@ -184,7 +255,7 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout) {
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += DQMC_NT) tr[(size_t)i * n + i] += dr[i];
         __syncthreads();
-        udt_pivot(n, ul, dr, tr, pv, tv, false, nullptr, x.s->sv, x.s->sxd, x.s->sxi);
+        udt_one(x, ul, dr, tr, b, false);
         rdivp(n, ur, tr, g, pv, bf);
         mm<false, false>(n, tr, tl, ul, x.s->tiles);
         for (int i = threadIdx.x; i < n; i += DQMC_NT) dl[i] = 1.0 / dr[i];
@@ -301,6 +372,8 @@ __device__ __noinline__ void propagate(const Ctx& x) {
                 __syncthreads();
             } else if (cs - 1 == c.rlast[cr - 1]) {
                 const int idx = cr;
+                const bool was_res = x.s->gres;
+                if (was_res) g_to_global(x);
                 copy(x.nf * (int)x.nn, c.Ur, ustk(x, idx + 1));
                 copy(x.nf * x.n, c.Dr, dstk(x, idx + 1));
                 copy(x.nf * (int)x.nn, c.Tr, tstk(x, idx + 1));
@@ -309,19 +382,30 @@ __device__ __noinline__ void propagate(const Ctx& x) {
                 copy(x.nf * (int)x.nn, c.Ul, ustk(x, idx + 1));
                 copy(x.nf * x.n, c.Dl, dstk(x, idx + 1));
                 copy(x.nf * (int)x.nn, c.Tl, tstk(x, idx + 1));
+                long long t0 = phase_start();
                 if (c.check_prop) copy(x.nf * (int)x.nn, c.Gtmp, c.G);
                 __syncthreads();
                 wrap_greens(x, c.Gtmp, cs - 1, 1);
+                phase_stop(x, DQMC_PHASE_PROP_CHECK, t0);
+                t0 = phase_start();
                 calculate_greens(x, c.G);
+                phase_stop(x, DQMC_PHASE_GREENS, t0);
+                t0 = phase_start();
                 if (c.check_prop) record_prop_error(x);
+                phase_stop(x, DQMC_PHASE_PROP_CHECK, t0);
                 if (cr == c.nr) {
                     if (threadIdx.x == 0) c.direction = -1;
                     recurse = true;
                 } else {
                     if (threadIdx.x == 0) c.current_range = cr + 1;
                 }
+                if (was_res) g_to_arena(x);
             } else {
-                wrap_greens(x, c.G, cs - 1, 1);
+                {
+                    long long tw = phase_start();
+                    wrap_greens(x, c.G, cs - 1, 1);
+                    phase_stop(x, DQMC_PHASE_WRAP, tw);
+                }
             }
         } else {
             if (cs == c.M) {
@@ -329,9 +413,15 @@ __device__ __noinline__ void propagate(const Ctx& x) {
                 set_ones(x, dstk(x, c.nr + 1));
                 mat_ident(x, tstk(x, c.nr + 1));
                 __syncthreads();
-                wrap_greens(x, c.G, cs + 1, -1);
+                {
+                    long long tw = phase_start();
+                    wrap_greens(x, c.G, cs + 1, -1);
+                    phase_stop(x, DQMC_PHASE_WRAP, tw);
+                }
             } else if (cs + 1 == c.rfirst[cr - 1]) {
                 const int idx = cr;
+                const bool was_res = x.s->gres;
+                if (was_res) g_to_global(x);
                 copy(x.nf * (int)x.nn, c.Ul, ustk(x, idx));
                 copy(x.nf * x.n, c.Dl, dstk(x, idx));
                 copy(x.nf * (int)x.nn, c.Tl, tstk(x, idx));
@@ -340,19 +430,34 @@ __device__ __noinline__ void propagate(const Ctx& x) {
                 copy(x.nf * (int)x.nn, c.Ur, ustk(x, idx));
                 copy(x.nf * x.n, c.Dr, dstk(x, idx));
                 copy(x.nf * (int)x.nn, c.Tr, tstk(x, idx));
+                long long t0 = phase_start();
                 if (c.check_prop) copy(x.nf * (int)x.nn, c.Gtmp, c.G);
                 __syncthreads();
+                phase_stop(x, DQMC_PHASE_PROP_CHECK, t0);
+                t0 = phase_start();
                 calculate_greens(x, c.G);
+                phase_stop(x, DQMC_PHASE_GREENS, t0);
+                t0 = phase_start();
                 if (c.check_prop) record_prop_error(x);
+                phase_stop(x, DQMC_PHASE_PROP_CHECK, t0);
                 if (cr == 1) {
                     if (threadIdx.x == 0) c.direction = 1;
                     recurse = true;
                 } else {
-                    wrap_greens(x, c.G, cs + 1, -1);
+                    {
+                        long long tw = phase_start();
+                        wrap_greens(x, c.G, cs + 1, -1);
+                        phase_stop(x, DQMC_PHASE_WRAP, tw);
+                    }
                     if (threadIdx.x == 0) c.current_range = cr - 1;
                 }
+                if (was_res) g_to_arena(x);
             } else {
-                wrap_greens(x, c.G, cs + 1, -1);
+                {
+                    long long tw = phase_start();
+                    wrap_greens(x, c.G, cs + 1, -1);
+                    phase_stop(x, DQMC_PHASE_WRAP, tw);
+                }
             }
         }
         __syncthreads();
@@ -433,17 +538,18 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 const double* g = c.G + (size_t)b * x.nn;
                 double ig = -g[(size_t)i * n + j];
                 if (j == i) ig += 1.0;
-                x.s->col[b][j] = ig;
-                x.s->row[b][j] = x.s->sxd[b] * g[(size_t)j * n + i];
+                x.s->r1.col[b][j] = ig;
+                x.s->r1.row[b][j] = x.s->sxd[b] * g[(size_t)j * n + i];
             }
             __syncthreads();
             for (int b = 0; b < nf; ++b) {
                 double* g = c.G + (size_t)b * x.nn;
-                const double* cl = x.s->col[b];
-                const double* rw = x.s->row[b];
-                for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
-                    const int k = e % n, l = e / n;
-                    g[e] = fma(-cl[k], rw[l], g[e]);
+                const double* cl = x.s->r1.col[b];
+                const double* rw = x.s->r1.row[b];
+                for (int k = threadIdx.x & 63; k < n; k += 64) {
+                    const double ck = -cl[k];
+                    for (int l = threadIdx.x >> 6; l < n; l += DQMC_NT / 64)
+                        g[k + (size_t)l * n] = fma(ck, rw[l], g[k + (size_t)l * n]);
                 }
             }
             __syncthreads();

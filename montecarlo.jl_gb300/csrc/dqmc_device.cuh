@@ -48,7 +48,9 @@ __device__ __forceinline__ void dright(int n, double* __restrict__ C, const doub
     for (int e = threadIdx.x; e < n * n; e += DQMC_NT) C[e] = A[e] * d[e / n];
 }
 
-// C = op(A) * op(B), op = transpose when TA / TB.  64 x 64 output tiles,
+// C = op(A) * op(B), op = transpose when TA / TB, on the FP64 FMA pipe (on
+// GB300 measured at 1.16 TFLOP/s for 64 x 64 blocks, above the DMMA tensor
+// path at 1.04).  64 x 64 output tiles,
 // 4 x 4 outputs per thread, k staged 16 at a time through shared memory
 // (sm: 2 * 16 * 64 doubles).  C must not alias A or B.  Summation over k is
 // in ascending order with fused multiply-adds.
@@ -107,6 +109,101 @@ __device__ __noinline__ void mm(int n, double* __restrict__ C, const double* __r
                 for (int q = 0; q < 4; ++q) {
                     int gm = m0 + tx + 16 * r, gj = n0 + ty + 16 * q;
                     if (gm < n && gj < n) C[gm + (size_t)gj * n] = acc[r][q];
+                }
+        }
+    }
+}
+
+// Double-float product for the mixed path: C = op(A) * op(B) with FP64
+// inputs and output, computed on the FP32 pipe.  Each operand is split
+// X = Xh + Xl (Xh = fp32(X), Xl = fp32(X - Xh), on the fly while staging).
+// The main term sum_k Ah Bh is accumulated exactly-rounded in a pair of floats:
+// the product is split exactly with one fmaf (TwoProd) and added with TwoSum
+// (Knuth); the cross terms Ah Bl + Al Bh are accumulated in plain FP32 and
+// Al Bl is dropped.  Relative error ~1e-14 per product (FP32 alone: ~1e-7,
+// which the wraps' error amplification over ten slices turns into O(1)).
+// About 12 FP32 instructions per multiply-add, against one FP64 instruction
+// on a pipe ~57x narrower on GB300.  64 x 64 tiles, 4 x 4 per thread, k staged
+// 16 at a time (sm: 4 * 16 * 64 floats).  C must not alias A or B.
+template <bool TA, bool TB>
+__device__ __noinline__ void mm_df(int n, double* __restrict__ C, const double* __restrict__ A,
+                                   const double* __restrict__ B, double* smd) {
+    float* sAh = reinterpret_cast<float*>(smd);  // [16][64]: sAh[kk*64 + m]
+    float* sAl = sAh + 16 * 64;
+    float* sBh = sAl + 16 * 64;                   // [16][64]: sBh[kk*64 + j]
+    float* sBl = sBh + 16 * 64;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    for (int n0 = 0; n0 < n; n0 += 64) {
+        for (int m0 = 0; m0 < n; m0 += 64) {
+            float sh[4][4], sl[4][4], xx[4][4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sh[r][q] = sl[r][q] = xx[r][q] = 0.f;
+            for (int k0 = 0; k0 < n; k0 += 16) {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    int e = tid + t * DQMC_NT;
+                    int mm_, kk;
+                    if (!TA) { mm_ = e & 63; kk = e >> 6; } else { kk = e & 15; mm_ = e >> 4; }
+                    int gm = m0 + mm_, gk = k0 + kk;
+                    double v = 0.0;
+                    if (gm < n && gk < n) v = TA ? A[gk + (size_t)gm * n] : A[gm + (size_t)gk * n];
+                    float h = __double2float_rn(v);
+                    sAh[kk * 64 + mm_] = h;
+                    sAl[kk * 64 + mm_] = __double2float_rn(v - (double)h);
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    int e = tid + t * DQMC_NT;
+                    int kk, jj;
+                    if (!TB) { kk = e & 15; jj = e >> 4; } else { jj = e & 63; kk = e >> 6; }
+                    int gk = k0 + kk, gj = n0 + jj;
+                    double v = 0.0;
+                    if (gk < n && gj < n) v = TB ? B[gj + (size_t)gk * n] : B[gk + (size_t)gj * n];
+                    float h = __double2float_rn(v);
+                    sBh[kk * 64 + jj] = h;
+                    sBl[kk * 64 + jj] = __double2float_rn(v - (double)h);
+                }
+                __syncthreads();
+#pragma unroll 4
+                for (int kk = 0; kk < 16; ++kk) {
+                    float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        ah[r] = sAh[kk * 64 + tx + 16 * r];
+                        al[r] = sAl[kk * 64 + tx + 16 * r];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        bh[q] = sBh[kk * 64 + ty + 16 * q];
+                        bl[q] = sBl[kk * 64 + ty + 16 * q];
+                    }
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const float p = __fmul_rn(ah[r], bh[q]);
+                            const float pe = __fmaf_rn(ah[r], bh[q], -p);  // exact: ah*bh = p + pe
+                            const float t = __fadd_rn(sh[r][q], p);       // TwoSum(sh, p)
+                            const float z = __fsub_rn(t, sh[r][q]);
+                            const float er = __fadd_rn(__fsub_rn(sh[r][q], __fsub_rn(t, z)),
+                                                       __fsub_rn(p, z));
+                            sh[r][q] = t;
+                            sl[r][q] = __fadd_rn(sl[r][q], __fadd_rn(er, pe));
+                            xx[r][q] = __fmaf_rn(ah[r], bl[q], __fmaf_rn(al[r], bh[q], xx[r][q]));
+                        }
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    int gm = m0 + tx + 16 * r, gj = n0 + ty + 16 * q;
+                    if (gm < n && gj < n)
+                        C[gm + (size_t)gj * n] =
+                            (double)sh[r][q] + ((double)sl[r][q] + (double)xx[r][q]);
                 }
         }
     }
@@ -240,6 +337,168 @@ __device__ __noinline__ void udt_pivot(int n, double* __restrict__ U, double* __
                 double d = 1.0 / D[i];
                 In[e] = d * In[e];
             }
+        }
+    }
+    __syncthreads();
+}
+
+// udt_AVX_pivot! for n <= 64 with the factorisation held in shared memory
+// (sIn, sU: n*(n+1) doubles each, leading dimension n+1).  Same algorithm and
+// outputs as udt_pivot, organised for GB300's narrow FP64 pipe, where every
+// FP64 warp instruction costs the same pipe time however few lanes do useful
+// work: two threads per column run the dot products and updates down the
+// column (one shuffle to combine), instead of a warp per column with a
+// five-level reduction.  The column norms that the reference recomputes each
+// step (indmaxcolumn) come out of the reflector-application pass, which
+// already holds the updated columns; the pivot search compares the norms'
+// bit patterns on the integer pipe (non-negative doubles order like their
+// bits); the reflector scales by the reciprocal of xi1 (rounding-level
+// difference from the division).  Two barriers per column.
+__device__ __noinline__ void udt_pivot_sm(int n, double* __restrict__ U, double* __restrict__ D,
+                                          double* __restrict__ In, int* __restrict__ piv,
+                                          double* __restrict__ tau, bool apply, double* sIn,
+                                          double* sU, double* sv, double* sxd) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int ld = n + 1;
+    for (int e = tid; e < n * n; e += DQMC_NT) sIn[(e % n) + (e / n) * ld] = In[e];
+    for (int i = tid; i < n; i += DQMC_NT) piv[i] = i + 1;
+    __syncthreads();
+    // initial squared column norms: two threads per column (the guard is
+    // warp-uniform so every lane of a participating warp reaches the shuffle)
+    if (warp * 32 < 2 * n) {
+        const bool act = tid < 2 * n;
+        const int col = act ? (tid >> 1) : 0, h = tid & 1;
+        const double* a = sIn + col * ld;
+        double q = 0.0;
+        if (act)
+            for (int r = h; r < n; r += 2) q = fma(a[r], a[r], q);
+        q += __shfl_xor_sync(0xffffffffu, q, 1);
+        if (act && h == 0) sv[col] = q;
+    }
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        if (warp == 0) {
+            // indmaxcolumn: first column of maximal norm among j..n-1
+            long long best = -1;
+            int bi = n;
+            for (int col = j + lane; col < n; col += 32) {
+                long long v = __double_as_longlong(sv[col]);
+                if (v > best) { best = v; bi = col; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            const int jm = bi;
+            const double normu = __longlong_as_double(best);
+            if (jm != j) {
+                double* a = sIn + jm * ld;
+                double* b = sIn + j * ld;
+                for (int r = lane; r < n; r += 32) {
+                    double t = a[r];
+                    a[r] = b[r];
+                    b[r] = t;
+                }
+                if (lane == 0) {
+                    int tp = piv[jm];
+                    piv[jm] = piv[j];
+                    piv[j] = tp;
+                    sv[jm] = sv[j];
+                }
+            }
+            __syncwarp();
+            // reflector! (UDT.jl:157-172)
+            double* x = sIn + j * ld;
+            double xi1 = x[j];
+            double t = 0.0;
+            if (normu != 0.0) {
+                double nu = copysign(sqrt(normu), xi1);
+                xi1 += nu;
+                const double inv = 1.0 / xi1;
+                __syncwarp();
+                for (int r = j + 1 + lane; r < n; r += 32) x[r] = x[r] * inv;
+                if (lane == 0) x[j] = -nu;
+                t = xi1 / nu;
+            }
+            if (lane == 0) { tau[j] = t; sxd[0] = t; }
+        }
+        __syncthreads();
+        // reflectorApply! (UDT.jl:53-70) fused with the next step's column norms
+        const int ncols = n - j - 1;
+        if (warp * 32 < 2 * ncols) {
+            const double t = sxd[0];
+            const double* x = sIn + j * ld;
+            const bool act = tid < 2 * ncols;
+            const int col = j + 1 + (tid >> 1), h = tid & 1;
+            double* a = sIn + (act ? col : j) * ld;
+            const double aj = act ? a[j] : 0.0;
+            double s = 0.0;
+            if (act)
+                for (int r = j + 1 + h; r < n; r += 2) s = fma(x[r], a[r], s);
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            const double vAj = t * (aj + s);
+            double q = 0.0;
+            if (act) {
+                if (h == 0) a[j] = aj - vAj;
+                for (int r = j + 1 + h; r < n; r += 2) {
+                    double v = fma(-x[r], vAj, a[r]);
+                    a[r] = v;
+                    q = fma(v, v, q);
+                }
+            }
+            q += __shfl_xor_sync(0xffffffffu, q, 1);
+            if (act && h == 0) sv[col] = q;
+        }
+        __syncthreads();
+    }
+    // Calculate Q (UDT.jl:272-289)
+    for (int e = tid; e < n * n; e += DQMC_NT) {
+        int i = e % n, c = e / n;
+        sU[i + c * ld] = (i == c) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    if (tid == 0) sU[(n - 1) * ld + (n - 1)] -= tau[n - 1];
+    __syncthreads();
+    for (int k = n - 2; k >= 0; --k) {
+        const int ncols = n - k;
+        if (warp * 32 < 2 * ncols) {
+            const double* v = sIn + k * ld;
+            const double t = tau[k];
+            const bool act = tid < 2 * ncols;
+            const int col = k + (tid >> 1), h = tid & 1;
+            double* u = sU + (act ? col : k) * ld;
+            const double uk = act ? u[k] : 0.0;
+            double s = 0.0;
+            if (act)
+                for (int r = k + 1 + h; r < n; r += 2) s = fma(v[r], u[r], s);
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            const double vB = t * (uk + s);
+            if (act) {
+                if (h == 0) u[k] = uk - vB;
+                for (int r = k + 1 + h; r < n; r += 2) u[r] = fma(-v[r], vB, u[r]);
+            }
+        }
+        __syncthreads();
+    }
+    // D (UDT.jl:293-301); 1/D per row as the reference's _apply_pivot!
+    for (int i = tid; i < n; i += DQMC_NT) {
+        double xx = fabs(sIn[i * ld + i]);
+        double d = (xx == 0.0) ? 1.0 : xx;
+        D[i] = d;
+        sv[i] = 1.0 / d;
+    }
+    for (int e = tid; e < n * n; e += DQMC_NT) U[e] = sU[(e % n) + (e / n) * ld];
+    __syncthreads();
+    // _apply_pivot! (UDT.jl:311-334), straight from shared memory
+    for (int e = tid; e < n * n; e += DQMC_NT) {
+        int i = e % n, j = e / n;
+        const double v = sIn[i + j * ld];
+        if (apply) {
+            In[i + (size_t)(piv[j] - 1) * n] = (j >= i) ? sv[i] * v : 0.0;
+        } else {
+            In[e] = (j >= i) ? sv[i] * v : v;
         }
     }
     __syncthreads();

@@ -30,19 +30,30 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
     x.n = s->c.n;
     x.nf = s->c.nf;
     x.nn = (size_t)x.n * x.n;
+    if (threadIdx.x == 0) {
+        s->Gglob = s->c.G;
+        s->gres = 0;
+    }
+    __syncthreads();
     if (x.n > DQMC_NMAX || x.nf < 1 || x.nf > 2) {
         if (threadIdx.x == 0) chains[blockIdx.x].status = 1;
         return;
     }
     switch (op) {
-    case DQMC_OP_SWEEP:
+    case DQMC_OP_SWEEP: {
+        const bool res = g_resident_possible(x);
+        if (res) g_to_arena(x);
         for (int sw = 0; sw < arg0; ++sw) {
             for (int t = 0; t < 2 * s->c.M; ++t) {
+                long long t0 = phase_start();
                 sweep_spatial(x);
+                phase_stop(x, DQMC_PHASE_SWEEP_SPATIAL, t0);
                 propagate(x);
             }
         }
+        if (res) g_to_global(x);
         break;
+    }
     case DQMC_OP_BUILD:
         reverse_build_stack(x);
         propagate(x);
@@ -79,6 +90,7 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
         g.n_neg_p = s->c.n_neg_p;
         g.accepted = s->c.accepted;
         g.proposals = s->c.proposals;
+        for (int p = 0; p < 8; ++p) g.timers[p] = s->c.timers[p];
     }
 }
 
