@@ -13,3 +13,13 @@ from .model import (DENSITY_GHQ, DENSITY_HIRSCH, MAGNETIC_GHQ, MAGNETIC_HIRSCH, 
                     AttractiveHubbardModel, DensityGHQField, DensityHirschField, DQMCParameters,
                     HubbardModel, MagneticGHQField, MagneticHirschField, RepulsiveHubbardModel,
                     generate_chunks, hopping_exponentials)
+from .measurements import (LogBinner, double_occupancy as double_occupancy_kernel,  # noqa: F401
+                           interaction_energy, occupation_kernel, spin_density_correlation_z,
+                           structure_factor)
+from .dqmc import (DQMC, ExitCode, Measurement, double_occupancy, greens_measurement,  # noqa: F401
+                   occupation, spin_density_correlation)
+
+
+def run(mc, **kwargs):
+    """``run!(mc)`` of the reference (DQMC.jl:252)."""
+    return mc.run(**kwargs)

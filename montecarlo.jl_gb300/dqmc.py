@@ -1,0 +1,180 @@
+"""``DQMC`` simulation object and ``run`` (the reference's ``run!``) on the GPU.
+
+Mirrors src/flavors/DQMC/DQMC.jl:32-394: construction from a model and
+keyword parameters, random field initialisation from the seed, the stack
+build of ``initialize_run`` and the sweep loop of ``run!`` with measurements
+every ``measure_rate`` sweeps after thermalisation.  The sweeps, wraps,
+stabilisations and Green's functions run in libdqmc_gb300.so; measurements
+are evaluated on the downloaded physical Green's function.
+"""
+from __future__ import annotations
+
+import enum
+import time
+
+import numpy as np
+
+from . import _lib
+from .measurements import LogBinner, MEASUREMENTS
+from .model import DQMCParameters, hopping_exponentials
+
+
+class ExitCode(enum.IntEnum):
+    """src/helpers.jl:17-22."""
+
+    SUCCESS = 0
+    GENERIC_FAILURE = 1
+    CANCELLED_TIME_LIMIT = 2
+    CANCELLED_LOW_ACCEPTANCE = 3
+
+
+class DQMC:
+    """``DQMC(model; seed, field, measurements, thermalization, sweeps,
+    measure_rate, beta, delta_tau | slices, safe_mult, ...)``.
+
+    Extra keywords of this implementation: ``precision`` ("fp64" or "mixed")
+    and ``device``.
+    """
+
+    def __init__(self, model, *, seed: int = -1, field=None, measurements=None,
+                 thermalization_measurements=None, last_sweep: int = 0, measure_rate: int = 10,
+                 precision: str = "fp64", device: int = 0, **kwargs):
+        self.model = model
+        self.parameters = DQMCParameters.make(measure_rate=measure_rate, **kwargs)
+        fcls = field if field is not None else model.choose_field()
+        self.field = fcls(self.parameters, model)
+        if seed == -1:
+            seed = int(np.random.SeedSequence().generate_state(1, dtype=np.uint64)[0])
+        self.seed = int(seed) & (2**64 - 1)
+        self.last_sweep = last_sweep
+        self.measurements = dict(measurements or {})
+        self.thermalization_measurements = dict(thermalization_measurements or {})
+        self.precision = precision
+        p = self.parameters
+        self.n = len(model.l)
+        self.config = _lib.ChainConfig(self.n, self.field.unique_flavors, p.slices, p.safe_mult,
+                                       self.field.kind, int(p.check_propagation_error),
+                                       self.field.alpha, self.seed)
+        prec = _lib.PREC_MIXED if precision == "mixed" else _lib.PREC_FP64
+        self.handle = _lib.Handle([self.config], precision=prec, device=device)
+        self.exps = hopping_exponentials(model.hopping_matrix(), p.delta_tau)
+        self.handle.set_hopping(0, self.exps)
+        self.handle.init_random_field(0)  # rand!(field_data), DQMC.jl:50
+        self.field.conf[:] = self.handle.get_field(0)
+        self.initialized = False
+        self.analysis = {}
+        self.max_sweeps_per_launch = 50
+
+    # -- stack --------------------------------------------------------------
+    def init(self):
+        """init! + the stack part of initialize_run (DQMC.jl:144-179)."""
+        self.handle.set_field(0, np.asfortranarray(self.field.conf))
+        self.handle.initialize_run()
+        self.initialized = True
+
+    @property
+    def current_slice(self):
+        return self.handle.stats(0)["current_slice"]
+
+    def greens(self, physical=True):
+        """greens(mc) (greens.jl:87): the physical equal-time G by default."""
+        return self.handle.greens(0, physical=physical)
+
+    def calculate_greens(self, slice_, safe_mult=0):
+        """calculate_greens(mc, slice) (stack.jl:525-583), effective G."""
+        return self.handle.calculate_greens(0, slice_, safe_mult)
+
+    def __getitem__(self, key):
+        return self.measurements[key]
+
+    def __setitem__(self, key, value):
+        self.measurements[key] = value
+
+    # -- run! -----------------------------------------------------------------
+    def run(self, *, verbose: bool = False, thermalization: int = None, sweeps: int = None,
+            safe_before: float = None, min_acceptance: float = None) -> ExitCode:
+        """run! (DQMC.jl:252-394): thermalisation + measurement sweeps."""
+        p = self.parameters
+        th = p.thermalization if thermalization is None else thermalization
+        sw = p.sweeps if sweeps is None else sweeps
+        if not self.initialized:
+            self.init()
+        t0 = time.time()
+        total = th + sw
+        st = self.handle.stats(0)
+        acc0, prop0 = st["accepted"], st["proposals"]
+        while self.last_sweep < total:
+            # advance in device launches up to the next measurement point
+            # (measurements read G after every measure_rate-th sweep)
+            if self.last_sweep < th:
+                k = th - self.last_sweep
+            elif self.measurements:
+                k = p.measure_rate - (self.last_sweep % p.measure_rate)
+            else:
+                k = total - self.last_sweep
+            k = max(1, min(k, total - self.last_sweep, self.max_sweeps_per_launch))
+            self.handle.sweep(k)
+            self.last_sweep += k
+            if self.last_sweep > th and self.last_sweep % p.measure_rate == 0:
+                self._measure()
+            if safe_before is not None and time.time() > safe_before:
+                return ExitCode.CANCELLED_TIME_LIMIT
+        st = self.handle.stats(0)
+        self.analysis = dict(
+            acceptance=(st["accepted"] - acc0) / max(1, st["proposals"] - prop0),
+            propagation_errors=st["propagation_errors"],
+            max_propagation_error=st["max_propagation_error"],
+            negative_probability=st["negative_probability"],
+            runtime=time.time() - t0)
+        self.field.conf[:] = self.handle.get_field(0)
+        if min_acceptance is not None and self.analysis["acceptance"] < min_acceptance:
+            return ExitCode.CANCELLED_LOW_ACCEPTANCE
+        if verbose:
+            print(f"DQMC run: {total} sweeps, acceptance {self.analysis['acceptance']:.3f}, "
+                  f"max propagation error {self.analysis['max_propagation_error']:.2e}")
+        return ExitCode.SUCCESS
+
+    def _measure(self):
+        G = self.greens(physical=True)
+        for name, obs in self.measurements.items():
+            obs.measure(G, self)
+
+
+class Measurement:
+    """A DQMC measurement: a kernel over the physical G pushed into a LogBinner
+    (DQMCMeasurement, measurements/generic.jl:6-13)."""
+
+    def __init__(self, kernel, post=None):
+        self.kernel = MEASUREMENTS.get(kernel, kernel) if isinstance(kernel, str) else kernel
+        self.post = post
+        self.observable = LogBinner()
+
+    def measure(self, G, mc):
+        v = self.kernel(G)
+        if self.post is not None:
+            v = self.post(v, mc)
+        self.observable.push(v)
+
+    def mean(self):
+        return self.observable.mean()
+
+    def std_error(self):
+        return self.observable.std_error()
+
+
+def greens_measurement(mc=None, model=None):
+    return Measurement("greens")
+
+
+def occupation(mc=None, model=None):
+    return Measurement("occupation")
+
+
+def double_occupancy(mc=None, model=None):
+    return Measurement("double_occupancy", post=lambda v, mc: float(np.mean(v)))
+
+
+def spin_density_correlation(mc=None, model=None, component="z"):
+    if component != "z":
+        raise NotImplementedError("only the z component is part of this library")
+    return Measurement("spin_density_correlation_z")

@@ -1,0 +1,76 @@
+"""Exact diagonalisation of the Hubbard model on small lattices (numpy).
+
+TEST INFRASTRUCTURE ONLY: the known-answer check the reference's ED tests
+make (test/ED/ED.jl, HamiltonMatrix :68-121, calculate_Greens_matrix :515,
+energy :539) restated: the grand-canonical Hamiltonian
+    H = -t sum_{directed bonds, sigma} c^dag_{to,sigma} c_{from,sigma}
+        + U_phys sum_i (n_{i,up} - 1/2)(n_{i,down} - 1/2) - mu sum_{i,sigma} n_{i,sigma}
+with U_phys = -U (the reference's sign convention, ED.jl:71), Jordan-Wigner
+fermions, and thermal expectation values at inverse temperature beta.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _ops(nmodes):
+    """Annihilation operators of nmodes fermionic modes (Jordan-Wigner)."""
+    a = np.array([[0.0, 1.0], [0.0, 0.0]])  # |0><1| acting on a mode
+    z = np.diag([1.0, -1.0])
+    eye = np.eye(2)
+    ops = []
+    for m in range(nmodes):
+        mats = [z] * m + [a] + [eye] * (nmodes - m - 1)
+        o = mats[0]
+        for x in mats[1:]:
+            o = np.kron(o, x)
+        ops.append(o)
+    return ops
+
+
+class HubbardED:
+    def __init__(self, n_sites, bonds, t, U_ref, mu, beta):
+        self.n = n_sites
+        self.beta = beta
+        modes = 2 * n_sites  # mode 2*i + s
+        self.c = _ops(modes)
+        c = self.c
+        dim = 2 ** modes
+        H = np.zeros((dim, dim))
+        Uph = -U_ref
+        for s in range(2):
+            for fr, to in bonds:
+                H += -t * c[2 * to + s].T @ c[2 * fr + s]
+        self.nop = [[c[2 * i + s].T @ c[2 * i + s] for s in range(2)] for i in range(n_sites)]
+        for i in range(n_sites):
+            nu, nd = self.nop[i]
+            H += Uph * (nu - 0.5 * np.eye(dim)) @ (nd - 0.5 * np.eye(dim))
+            H += -mu * (nu + nd)
+        self.H = H
+        self.E, self.V = np.linalg.eigh(H)
+        w = np.exp(-beta * (self.E - self.E.min()))
+        self.rho_diag = w / w.sum()
+
+    def expect(self, op):
+        """<op> = Tr(rho op)."""
+        M = self.V.T @ op @ self.V
+        return float(np.sum(self.rho_diag * np.diag(M)))
+
+    def greens(self):
+        """G[s][i, j] = <c_{i,s} c^dag_{j,s}>."""
+        out = np.zeros((2, self.n, self.n))
+        for s in range(2):
+            for i in range(self.n):
+                for j in range(self.n):
+                    out[s, i, j] = self.expect(self.c[2 * i + s] @ self.c[2 * j + s].T)
+        return out
+
+    def double_occupancy(self):
+        return np.array([self.expect(self.nop[i][0] @ self.nop[i][1]) for i in range(self.n)])
+
+    def sdc_z(self):
+        m = [self.nop[i][0] - self.nop[i][1] for i in range(self.n)]
+        return np.array([[self.expect(m[i] @ m[j]) for j in range(self.n)] for i in range(self.n)])
+
+    def energy(self):
+        return self.expect(self.H)
