@@ -187,6 +187,64 @@ def cpu_baseline_sample(pkg, workload, budget_s):
                       f"(C restatement of the reference, FMA contraction on)"}
 
 
+def ensemble_c3(pkg, _lib, n_chains, seconds, seed=3):
+    """Batched ensemble of uneven attractive chains: L in {6,8,10,12}, U_phys in
+    [-8,-2] (U_ref = -U_phys), beta in {4,8,12}, dtau = 0.1; safe_mult
+    autotuned per chain for a propagation error <= 1e-6; plain FP64 and mixed."""
+    from montecarlo_gb300 import autotune
+
+    rng = np.random.default_rng(seed)
+    specs = []
+    for j in range(n_chains):
+        L = int(rng.choice([6, 8, 10, 12]))
+        U = float(rng.uniform(-8.0, -2.0))
+        beta = float(rng.choice([4.0, 8.0, 12.0]))
+        model = pkg.HubbardModel(pkg.SquareLattice(L), U=-U)
+        specs.append((model, model.choose_field(), beta, 0.1, 1000 + j))
+    out = {"workload": f"{n_chains} attractive chains, L in {{6,8,10,12}} square, U in [-8,-2] "
+                       "(physics), beta in {4,8,12}, dtau=0.1, safe_mult autotuned per chain "
+                       "(propagation error <= 1e-6)"}
+    t = time.perf_counter()
+    confs = autotune.thermalize(specs)
+    therm_s = time.perf_counter() - t
+    out["thermalize_s"] = therm_s
+    for name, prec in (("plain_fp64", _lib.PREC_FP64), ("mixed", _lib.PREC_MIXED)):
+        t = time.perf_counter()
+        ks, errs = autotune.tune_safe_mult(specs, tol=1e-6, precision=prec, confs=confs)
+        tune_s = time.perf_counter() - t
+        ce = []
+        for (model, fcls, beta, dt, s), k in zip(specs, ks):
+            param = pkg.DQMCParameters.make(beta=beta, delta_tau=dt, safe_mult=k)
+            fld = fcls(param, model)
+            ce.append((_lib.ChainConfig(len(model.l), 1, param.slices, k, fld.kind, 1, fld.alpha, s),
+                       pkg.hopping_exponentials(model.hopping_matrix(), dt)))
+        r = pkg.run_ensemble(ce, seconds=seconds, quantum_us=100000, precision=prec)
+        out[name] = {"sweeps_per_s": r["sweeps_per_s"], "max_propagation_error": r["max_propagation_error"],
+                     "safe_mult_histogram": {str(k): ks.count(k) for k in sorted(set(ks))},
+                     "autotune_s": tune_s, "timed_s": r["wall"], "launches": r["launches"]}
+    out["mixed_vs_plain"] = out["mixed"]["sweeps_per_s"] / out["plain_fp64"]["sweeps_per_s"]
+    return out
+
+
+def served_c5(pkg, _lib, n_requests, wall_s, seed=5):
+    """Served request stream: Poisson arrivals, square or honeycomb, HBM-budget
+    admission, device-resident chains, time-sliced launches.  Bounded sample
+    of the stream's distribution: L in {4,6,8}, beta in {2,4,8}, 20-200 sweeps."""
+    reqs = pkg.poisson_stream(n_requests, rate=20.0, seed=seed, Ls=(4, 6, 8),
+                              betas=(2.0, 4.0, 8.0), sweeps=(20, 200))
+    out = {"workload": f"{n_requests} Poisson requests at 20/s, square|honeycomb, L in {{4,6,8}}, "
+                       "U in [-8,8] (physics), beta in {2,4,8}, 20-200 sweeps, mixed precision, "
+                       "16 GiB HBM budget, 20 ms time slices"}
+    srv = pkg.Server(max_slots=304, budget_bytes=16 << 30, precision=_lib.PREC_MIXED,
+                     quantum_us=20000)
+    r = srv.serve(reqs, realtime=True, max_wall=wall_s)
+    srv.close()
+    out.update({"sweeps_per_s": r["sweeps_per_s"], "p50_block_s": r["p50_block_s"],
+                "p99_block_s": r["p99_block_s"], "finished": len(r["results"]),
+                "unfinished": r["unfinished"], "launches": r["launches"], "wall_s": r["wall"]})
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -197,6 +255,9 @@ def main():
     ap.add_argument("--chains", type=int, default=0, help="ensemble size (default 2 per SM)")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the mixed / batched-ensemble / served measurements")
+    ap.add_argument("--extra-seconds", type=float, default=6.0)
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -335,6 +396,41 @@ def main():
     h2d = (4 * n * n * 8 + B_chains * n * M) / args.steps
     d2h = B_chains * (nf * n * n * 8 + n * M + 0)
 
+    # ---- mixed precision on the same ensemble (double-float slice products)
+    extras = {}
+    if world == 1 and not args.no_extras:
+        from montecarlo_gb300 import autotune
+
+        specs2 = [(model, type(fld), param.beta, param.delta_tau, seed0 + j) for j in range(8)]
+        kk, _ = autotune.tune_safe_mult(specs2, tol=1e-6, precision=_lib.PREC_MIXED)
+        k_mixed = min(kk)
+        cfgs_m = [_lib.ChainConfig(n, nf, M, k_mixed, fld.kind, 1, fld.alpha, seed0 + j)
+                  for j in range(B_chains)]
+        hm = _lib.Handle(cfgs_m, precision=_lib.PREC_MIXED)
+        hm.set_hopping(-1, exps)
+        hm.init_random_field(-1)
+        hm.set_stream(stream.cuda_stream)
+        hm.initialize_run()
+        for _ in range(args.warmup):
+            hm.sweep_async(1)
+        hm.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(args.steps):
+            hm.sweep_async(1)
+        e1.record(stream)
+        hm.synchronize()
+        torch.cuda.synchronize()
+        mixed_v = B_chains * args.steps / (e0.elapsed_time(e1) / 1e3)
+        mp = max(hm.stats(i)["max_propagation_error"] for i in range(B_chains))
+        hm.close()
+        extras["mixed"] = {"value": mixed_v, "unit": "sweeps/s", "vs_plain_fp64": mixed_v / value,
+                           "max_propagation_error": mp, "safe_mult": k_mixed,
+                           "note": "wraps and slice chains as double-float products on the FP32 "
+                                   "pipe; UDT, reconstruction, ratios, rank-1 updates FP64"}
+        extras["batched"] = ensemble_c3(pkg, _lib, 256, args.extra_seconds)
+        extras["served"] = served_c5(pkg, _lib, 48, 5 * args.extra_seconds)
+
     # DRAM traffic of the chain kernel from the committed ncu capture, scaled
     # by chains (independent per-chain workspaces)
     traffic = None
@@ -374,6 +470,7 @@ def main():
             "acceptance": acc, "max_propagation_error": max_prop,
             "clocks": clk,
         }
+        line.update(extras)
         if cpu is not None:
             line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)

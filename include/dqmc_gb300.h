@@ -153,6 +153,33 @@ int dqmc_calculate_greens(dqmc_handle* h, int chain, int slice, int safe_mult, d
 /* which: 0 u_stack, 1 t_stack (nf*n*n), 2 d_stack (nf*n); idx 1-based (stack.jl:13-15) */
 int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out);
 
+/* ---- pools: batched and served chains -------------------------------------
+ * Replaces: a set of independent simulations driven one after another
+ * (the reference's mpi_queue / pmap task farms, src/mpi.jl:26-168).  A pool
+ * holds up to max_slots chains in one device arena of budget_bytes; chains
+ * are admitted and released between launches while the others keep their
+ * device-resident state (G, UDT stack, field), and one launch advances all of
+ * them.  Per-chain calls (dqmc_set_hopping, dqmc_set_field,
+ * dqmc_init_random_field, dqmc_get_greens, dqmc_get_stats, ...) take the slot
+ * index as the chain index. */
+int dqmc_pool_create(int device, int max_slots, int64_t budget_bytes, int precision,
+                     dqmc_handle** out);
+/* Admit a chain: DQMC_ERR_OOM when its workspace (dqmc_chain_bytes) does not
+ * fit the free budget, DQMC_ERR_NOT_READY when no slot is free (retry after
+ * a release).  The stack is built on the chain's first run. */
+int dqmc_pool_admit(dqmc_handle* h, const dqmc_chain_config* cfg, int* slot);
+int dqmc_pool_release(dqmc_handle* h, int slot);
+/* Sweeps the slot may still run (one sweep = 2M slice visits). */
+int dqmc_pool_set_quota(dqmc_handle* h, int slot, int64_t n_sweeps);
+/* One time slice of every admitted chain: each runs slice visits until its
+ * quota is used up or budget_us microseconds have passed (a chain finishes the
+ * visit it is in).  use_graph = 1 replays the step (descriptor upload, launch,
+ * download) as one captured CUDA graph. */
+int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph);
+int dqmc_pool_slot(dqmc_handle* h, int slot, int64_t* sweeps_done, int64_t* sweeps_left,
+                   int32_t* active);
+int64_t dqmc_pool_free_bytes(dqmc_handle* h);
+
 /* ---- allocation-free Green's function ---------------------------------------
  * No counterpart in the reference: an addition for callers that cannot
  * allocate device memory when they need G -- hosts whose device memory budget

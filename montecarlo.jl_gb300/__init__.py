@@ -23,3 +23,4 @@ from .dqmc import (DQMC, ExitCode, Measurement, double_occupancy, greens_measure
 def run(mc, **kwargs):
     """``run!(mc)`` of the reference (DQMC.jl:252)."""
     return mc.run(**kwargs)
+from .serving import Request, Server, poisson_stream, request_config, run_ensemble  # noqa: F401

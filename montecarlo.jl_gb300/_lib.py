@@ -52,6 +52,8 @@ EXPORTS = [
     "dqmc_sweep_spatial", "dqmc_sweep", "dqmc_sweep_async", "dqmc_query", "dqmc_synchronize",
     "dqmc_get_stats", "dqmc_get_greens", "dqmc_set_greens", "dqmc_calculate_greens",
     "dqmc_get_stack", "dqmc_set_stream", "dqmc_get_timers", "dqmc_calculate_greens_noalloc",
+    "dqmc_pool_create", "dqmc_pool_admit", "dqmc_pool_release", "dqmc_pool_set_quota",
+    "dqmc_pool_run", "dqmc_pool_slot", "dqmc_pool_free_bytes",
 ]
 
 PHASES = ["sweep_spatial", "wrap", "slice_chain", "udt", "greens", "prop_check", "t_update",
@@ -96,6 +98,15 @@ def load(path: str = LIB_PATH):
     L.dqmc_get_stack.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
     L.dqmc_set_stream.argtypes = [P, C.c_void_p]
     L.dqmc_get_timers.argtypes = [P, C.c_int, C.POINTER(C.c_uint64)]
+    L.dqmc_pool_create.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int, C.POINTER(P)]
+    L.dqmc_pool_admit.argtypes = [P, C.POINTER(ChainConfig), C.POINTER(C.c_int)]
+    L.dqmc_pool_release.argtypes = [P, C.c_int]
+    L.dqmc_pool_set_quota.argtypes = [P, C.c_int, C.c_int64]
+    L.dqmc_pool_run.argtypes = [P, C.c_int, C.c_int]
+    L.dqmc_pool_slot.argtypes = [P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                 C.POINTER(C.c_int32)]
+    L.dqmc_pool_free_bytes.argtypes = [P]
+    L.dqmc_pool_free_bytes.restype = C.c_int64
     _lib = L
     return L
 
@@ -149,6 +160,8 @@ class Handle:
             pass
 
     def cfg(self, chain):
+        if not (0 <= chain < len(self._cfg)) or self._cfg[chain] is None:
+            raise DQMCError(1, f"chain index {chain} out of range or slot empty")
         return self._cfg[chain]
 
     def set_stream(self, stream_ptr):
@@ -165,7 +178,7 @@ class Handle:
         check(load().dqmc_set_field(self.h, chain, i8ptr(c)))
 
     def get_field(self, chain):
-        cfg = self._cfg[chain]
+        cfg = self.cfg(chain)
         c = np.zeros((cfg.n_sites, cfg.slices), dtype=np.int8, order="F")
         check(load().dqmc_get_field(self.h, chain, i8ptr(c)))
         return c
@@ -223,11 +236,11 @@ class Handle:
         return dict(zip(PHASES, list(out)))
 
     def _mat_buf(self, chain):
-        cfg = self._cfg[chain]
+        cfg = self.cfg(chain)
         return np.zeros(cfg.n_flavors * cfg.n_sites * cfg.n_sites)
 
     def greens(self, chain, physical=False):
-        cfg = self._cfg[chain]
+        cfg = self.cfg(chain)
         buf = self._mat_buf(chain)
         check(load().dqmc_get_greens(self.h, chain, int(bool(physical)), dptr(buf)))
         return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
@@ -241,13 +254,13 @@ class Handle:
         check(load().dqmc_set_greens(self.h, chain, dptr(buf)))
 
     def calculate_greens(self, chain, slice_, safe_mult=0):
-        cfg = self._cfg[chain]
+        cfg = self.cfg(chain)
         buf = self._mat_buf(chain)
         check(load().dqmc_calculate_greens(self.h, chain, int(slice_), int(safe_mult), dptr(buf)))
         return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
 
     def stack(self, chain, which, idx):
-        cfg = self._cfg[chain]
+        cfg = self.cfg(chain)
         if which == 2:
             out = np.zeros(cfg.n_flavors * cfg.n_sites)
             check(load().dqmc_get_stack(self.h, chain, 2, idx, dptr(out)))
@@ -255,3 +268,50 @@ class Handle:
         buf = self._mat_buf(chain)
         check(load().dqmc_get_stack(self.h, chain, which, idx, dptr(buf)))
         return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
+
+
+DQMC_ERR_OOM = 3
+
+
+class Pool(Handle):
+    """A dqmc pool: slots admitted / released between time-sliced launches."""
+
+    def __init__(self, max_slots, budget_bytes, precision=PREC_FP64, device=0):
+        L = load()
+        h = C.c_void_p()
+        check(L.dqmc_pool_create(device, int(max_slots), int(budget_bytes), precision, C.byref(h)))
+        self.h = h
+        self.n_chains = int(max_slots)
+        self._cfg = [None] * int(max_slots)
+
+    def admit(self, cfg):
+        """Slot index, or None when the budget or the slots are exhausted."""
+        slot = C.c_int(-1)
+        code = load().dqmc_pool_admit(self.h, C.byref(cfg), C.byref(slot))
+        if code in (DQMC_ERR_OOM, DQMC_ERR_NOT_READY):
+            return None
+        check(code)
+        self._cfg[slot.value] = cfg
+        return slot.value
+
+    def release(self, slot):
+        check(load().dqmc_pool_release(self.h, int(slot)))
+        self._cfg[slot] = None
+
+    def set_quota(self, slot, n_sweeps):
+        check(load().dqmc_pool_set_quota(self.h, int(slot), int(n_sweeps)))
+
+    def run(self, budget_us, use_graph=True):
+        check(load().dqmc_pool_run(self.h, int(budget_us), int(bool(use_graph))))
+
+    def slot(self, slot):
+        d, l, a = C.c_int64(), C.c_int64(), C.c_int32()
+        check(load().dqmc_pool_slot(self.h, int(slot), C.byref(d), C.byref(l), C.byref(a)))
+        return d.value, l.value, bool(a.value)
+
+    def free_bytes(self):
+        return int(load().dqmc_pool_free_bytes(self.h))
+
+
+def chain_bytes(cfg, precision=PREC_FP64):
+    return int(load().dqmc_chain_bytes(C.byref(cfg), precision))

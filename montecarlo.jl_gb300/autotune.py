@@ -1,0 +1,82 @@
+"""Autotuner of safe_mult (the stabilisation interval) per chain.
+
+The reference takes safe_mult from the user (parameters.jl:90) and reports a
+propagation error above 1e-7 as an instability (stack.jl:644-653).  For an
+ensemble of uneven chains (different L, U, beta) one safe_mult is either
+wasteful (weak coupling, short beta) or unstable (strong coupling, long
+beta).  The tuner picks per chain the largest safe_mult whose propagation
+error stays below ``safety * tol`` on *thermalised* configurations (random
+initial fields are far better conditioned than equilibrium ones, so probes
+from them overestimate the stable interval):
+
+1. thermalise every chain for a few sweeps at a conservative interval (FP64);
+2. restart probe chains from those configurations at every candidate interval
+   -- all chains x candidates in one batched launch -- and measure the largest
+   propagation error over a few sweeps;
+3. keep the largest candidate under the bound (the smallest one if none is).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _lib
+from .model import DQMCParameters, hopping_exponentials
+
+CANDIDATES = (2, 3, 4, 5, 6, 8, 10, 12, 15)
+
+
+def _cfg(model, field_cls, beta, delta_tau, k, seed):
+    param = DQMCParameters.make(beta=beta, delta_tau=delta_tau, safe_mult=k)
+    fld = field_cls(param, model)
+    k = min(k, param.slices)
+    return _lib.ChainConfig(len(model.l), fld.unique_flavors, param.slices, k, fld.kind, 1,
+                            fld.alpha, seed)
+
+
+def thermalize(specs, sweeps=6, safe_mult=4, device=0):
+    """Field configurations of `specs` ((model, field_cls, beta, delta_tau,
+    seed) tuples) after `sweeps` FP64 sweeps at `safe_mult`."""
+    cfgs = [_cfg(m, f, b, dt, safe_mult, s) for m, f, b, dt, s in specs]
+    h = _lib.Handle(cfgs, precision=_lib.PREC_FP64, device=device)
+    for j, (m, f, b, dt, s) in enumerate(specs):
+        h.set_hopping(j, hopping_exponentials(m.hopping_matrix(), dt))
+    h.init_random_field(-1)
+    h.initialize_run()
+    h.sweep(sweeps)
+    confs = [h.get_field(j) for j in range(len(specs))]
+    h.close()
+    return confs
+
+
+def tune_safe_mult(specs, tol=1e-6, precision=_lib.PREC_FP64, candidates=CANDIDATES,
+                   confs=None, therm_sweeps=6, probe_sweeps=2, safety=0.5, device=0):
+    """Chosen safe_mult per spec and the propagation error measured with it."""
+    if confs is None:
+        confs = thermalize(specs, sweeps=therm_sweeps, device=device)
+    cfgs, owner, ks = [], [], []
+    for j, (m, f, b, dt, s) in enumerate(specs):
+        M = DQMCParameters.make(beta=b, delta_tau=dt).slices
+        for k in sorted({min(k, M) for k in candidates}):
+            cfgs.append(_cfg(m, f, b, dt, k, s))
+            owner.append(j)
+            ks.append(k)
+    h = _lib.Handle(cfgs, precision=precision, device=device)
+    for r, j in enumerate(owner):
+        m, f, b, dt, s = specs[j]
+        h.set_hopping(r, hopping_exponentials(m.hopping_matrix(), dt))
+        h.init_random_field(r)  # seeds the stream; the field is replaced next
+        h.set_field(r, confs[j])
+    h.initialize_run()
+    st = h.sweep(probe_sweeps)
+    h.close()
+    errs = [dict() for _ in specs]
+    for r, j in enumerate(owner):
+        errs[j][ks[r]] = st[r]["max_propagation_error"]
+    chosen, err_at = [], []
+    bound = safety * tol
+    for e in errs:
+        ok = [k for k, v in e.items() if v <= bound]
+        k = max(ok) if ok else min(e)
+        chosen.append(k)
+        err_at.append(e[k])
+    return chosen, err_at

@@ -6,6 +6,7 @@
 #include <string.h>
 
 #include <string>
+#include <map>
 #include <vector>
 
 #include "../../include/dqmc_gb300.h"
@@ -83,6 +84,15 @@ struct dqmc_handle {
     DqmcChain* d_chains = nullptr;
     bool host_dirty = false;      // host descriptors changed (must upload before launch)
     bool busy = false;
+    // pool: slots admitted and released while others run, sub-allocated from
+    // one device arena of `budget` bytes (first fit, 256-byte granules)
+    bool pool = false;
+    size_t budget = 0;
+    std::map<size_t, size_t> free_blocks;  // offset -> bytes
+    std::vector<size_t> slot_off, slot_bytes;
+    DqmcChain* pinned = nullptr;           // pinned mirror for graph replays
+    cudaGraphExec_t graph = nullptr;
+    int graph_budget_us = -1;
 };
 
 namespace {
@@ -91,6 +101,8 @@ int check_chain(dqmc_handle* h, int chain) {
     if (!h) return fail(DQMC_ERR_INVALID, "null handle");
     if (chain < 0 || chain >= (int)h->cfg.size())
         return fail(DQMC_ERR_INVALID, "chain index " + std::to_string(chain) + " out of range");
+    if (!h->host[chain].active)
+        return fail(DQMC_ERR_INVALID, "slot " + std::to_string(chain) + " holds no chain");
     return DQMC_OK;
 }
 
@@ -139,6 +151,80 @@ int launch(dqmc_handle* h, int op, int arg0, int arg1, bool sync) {
     return DQMC_OK;
 }
 
+int validate_config(const dqmc_chain_config& c, int i) {
+    if (c.n_sites < 1 || c.n_sites > 512 || c.slices < 1 || c.safe_mult < 1 ||
+        (c.n_flavors != 1 && c.n_flavors != 2) || c.field < 0 || c.field > 3)
+        return fail(DQMC_ERR_INVALID, "invalid config for chain " + std::to_string(i) +
+                                          " (need 1 <= n_sites <= 512, slices >= 1, safe_mult >= 1, "
+                                          "n_flavors in {1,2}, field in 0..3)");
+    int want_nf = (c.field == DQMC_FIELD_MAGNETIC_HIRSCH || c.field == DQMC_FIELD_MAGNETIC_GHQ) ? 2 : 1;
+    if (c.n_flavors != want_nf)
+        return fail(DQMC_ERR_INVALID, "n_flavors does not match the field kind");
+    if ((c.slices + c.safe_mult - 1) / c.safe_mult > DQMC_MAX_CHUNKS)
+        return fail(DQMC_ERR_INVALID, "too many stabilisation chunks (max 256)");
+    if (!(c.alpha == c.alpha)) return fail(DQMC_ERR_INVALID, "alpha is NaN");
+    return DQMC_OK;
+}
+
+// Fill the descriptor of a chain whose workspace starts at `b` (layout L).
+void fill_descriptor(DqmcChain& d, const dqmc_chain_config& c, char* b, const Layout& L,
+                     int precision) {
+    memset(&d, 0, sizeof(d));
+    d.n = c.n_sites; d.nf = c.n_flavors; d.M = c.slices; d.k = c.safe_mult; d.kind = c.field;
+    d.check_prop = c.check_propagation_error ? 1 : 0;
+    d.prec = precision;
+    d.nr = generate_chunks(c.slices, c.safe_mult, d.rfirst, d.rlast);
+    fill_tables(d, c.field, c.alpha);
+    const size_t nn = (size_t)c.n_sites * c.n_sites;
+    double* hop = (double*)(b + L.off_hop);
+    d.conf = (int8_t*)(b + L.off_conf);
+    d.eT2 = hop; d.eT2inv = hop + nn; d.eTh = hop + 2 * nn; d.eThinv = hop + 3 * nn;
+    d.G = (double*)(b + L.off_G); d.Gtmp = (double*)(b + L.off_Gtmp);
+    d.Ul = (double*)(b + L.off_Ul); d.Ur = (double*)(b + L.off_Ur);
+    d.Tl = (double*)(b + L.off_Tl); d.Tr = (double*)(b + L.off_Tr);
+    d.tmp1 = (double*)(b + L.off_tmp1); d.tmp2 = (double*)(b + L.off_tmp2);
+    d.currU = (double*)(b + L.off_currU); d.out = (double*)(b + L.off_out);
+    d.ustack = (double*)(b + L.off_ustack); d.tstack = (double*)(b + L.off_tstack);
+    d.dstack = (double*)(b + L.off_dstack);
+    d.Dl = (double*)(b + L.off_Dl); d.Dr = (double*)(b + L.off_Dr);
+    d.tempv = (double*)(b + L.off_tempv);
+    d.pivot = (int*)(b + L.off_pivot);
+    d.key = c.seed; d.ctr = 0;
+    d.current_slice = 0; d.current_range = 1; d.direction = 1;
+    d.active = 1;
+}
+
+// first-fit sub-allocation from a pool's arena
+bool pool_alloc(dqmc_handle* h, size_t bytes, size_t* off) {
+    bytes = align256(bytes);
+    for (auto it = h->free_blocks.begin(); it != h->free_blocks.end(); ++it) {
+        if (it->second >= bytes) {
+            *off = it->first;
+            const size_t rest = it->second - bytes, at = it->first + bytes;
+            h->free_blocks.erase(it);
+            if (rest) h->free_blocks[at] = rest;
+            return true;
+        }
+    }
+    return false;
+}
+void pool_free(dqmc_handle* h, size_t off, size_t bytes) {
+    bytes = align256(bytes);
+    auto it = h->free_blocks.emplace(off, bytes).first;
+    auto nx = std::next(it);
+    if (nx != h->free_blocks.end() && it->first + it->second == nx->first) {
+        it->second += nx->second;
+        h->free_blocks.erase(nx);
+    }
+    if (it != h->free_blocks.begin()) {
+        auto pv = std::prev(it);
+        if (pv->first + pv->second == it->first) {
+            pv->second += it->second;
+            h->free_blocks.erase(it);
+        }
+    }
+}
+
 }  // namespace
 
 extern "C" {
@@ -157,20 +243,8 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
     *out = nullptr;
     if (precision != DQMC_PREC_FP64 && precision != DQMC_PREC_MIXED)
         return fail(DQMC_ERR_INVALID, "dqmc_create: unknown precision");
-    for (int i = 0; i < n_chains; ++i) {
-        const dqmc_chain_config& c = chains[i];
-        if (c.n_sites < 1 || c.n_sites > 512 || c.slices < 1 || c.safe_mult < 1 ||
-            (c.n_flavors != 1 && c.n_flavors != 2) || c.field < 0 || c.field > 3)
-            return fail(DQMC_ERR_INVALID, "dqmc_create: invalid config for chain " + std::to_string(i) +
-                                              " (need 1 <= n_sites <= 512, slices >= 1, safe_mult >= 1, "
-                                              "n_flavors in {1,2}, field in 0..3)");
-        int want_nf = (c.field == DQMC_FIELD_MAGNETIC_HIRSCH || c.field == DQMC_FIELD_MAGNETIC_GHQ) ? 2 : 1;
-        if (c.n_flavors != want_nf)
-            return fail(DQMC_ERR_INVALID, "dqmc_create: n_flavors does not match the field kind");
-        if ((c.slices + c.safe_mult - 1) / c.safe_mult > DQMC_MAX_CHUNKS)
-            return fail(DQMC_ERR_INVALID, "dqmc_create: too many stabilisation chunks (max 256)");
-        if (!(c.alpha == c.alpha)) return fail(DQMC_ERR_INVALID, "dqmc_create: alpha is NaN");
-    }
+    for (int i = 0; i < n_chains; ++i)
+        if (int st = validate_config(chains[i], i)) return st;
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0)
@@ -206,34 +280,8 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
         return cuda_fail(e, "cudaMalloc chain descriptors");
     }
     h->host.resize(n_chains);
-    for (int i = 0; i < n_chains; ++i) {
-        const dqmc_chain_config& c = chains[i];
-        const Layout& L = h->lay[i];
-        char* b = h->arena + base[i];
-        DqmcChain& d = h->host[i];
-        memset(&d, 0, sizeof(d));
-        d.n = c.n_sites; d.nf = c.n_flavors; d.M = c.slices; d.k = c.safe_mult; d.kind = c.field;
-        d.check_prop = c.check_propagation_error ? 1 : 0;
-        d.prec = precision;
-        d.nr = generate_chunks(c.slices, c.safe_mult, d.rfirst, d.rlast);
-        fill_tables(d, c.field, c.alpha);
-        const size_t nn = (size_t)c.n_sites * c.n_sites;
-        double* hop = (double*)(b + L.off_hop);
-        d.conf = (int8_t*)(b + L.off_conf);
-        d.eT2 = hop; d.eT2inv = hop + nn; d.eTh = hop + 2 * nn; d.eThinv = hop + 3 * nn;
-        d.G = (double*)(b + L.off_G); d.Gtmp = (double*)(b + L.off_Gtmp);
-        d.Ul = (double*)(b + L.off_Ul); d.Ur = (double*)(b + L.off_Ur);
-        d.Tl = (double*)(b + L.off_Tl); d.Tr = (double*)(b + L.off_Tr);
-        d.tmp1 = (double*)(b + L.off_tmp1); d.tmp2 = (double*)(b + L.off_tmp2);
-        d.currU = (double*)(b + L.off_currU); d.out = (double*)(b + L.off_out);
-        d.ustack = (double*)(b + L.off_ustack); d.tstack = (double*)(b + L.off_tstack);
-        d.dstack = (double*)(b + L.off_dstack);
-        d.Dl = (double*)(b + L.off_Dl); d.Dr = (double*)(b + L.off_Dr);
-        d.tempv = (double*)(b + L.off_tempv);
-        d.pivot = (int*)(b + L.off_pivot);
-        d.key = c.seed; d.ctr = 0;
-        d.current_slice = 0; d.current_range = 1; d.direction = 1;
-    }
+    for (int i = 0; i < n_chains; ++i)
+        fill_descriptor(h->host[i], chains[i], h->arena + base[i], h->lay[i], precision);
     int st = push_descriptors(h);
     if (st != DQMC_OK) { dqmc_destroy(h); return st; }
     *out = h;
@@ -246,6 +294,8 @@ int dqmc_destroy(dqmc_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->arena) cudaFree(h->arena);
     if (h->d_chains) cudaFree(h->d_chains);
+    if (h->graph) cudaGraphExecDestroy(h->graph);
+    if (h->pinned) cudaFreeHost(h->pinned);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return DQMC_OK;
@@ -267,6 +317,7 @@ int dqmc_set_hopping(dqmc_handle* h, int chain, const double* a, const double* b
     else if (int st = check_chain(h, chain)) return st;
     CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
     for (int i = lo; i < hi; ++i) {
+        if (!h->host[i].active) continue;  // free pool slot
         const size_t nn = (size_t)h->cfg[i].n_sites * h->cfg[i].n_sites;
         if (chain == -1 && h->cfg[i].n_sites != h->cfg[lo].n_sites)
             return fail(DQMC_ERR_INVALID, "dqmc_set_hopping(-1): chains have different n_sites");
@@ -320,6 +371,7 @@ int dqmc_init_random_field(dqmc_handle* h, int chain) {
     else if (int st = check_chain(h, chain)) return st;
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     for (int i = lo; i < hi; ++i) {
+        if (!h->host[i].active) continue;  // free pool slot
         const dqmc_chain_config& c = h->cfg[i];
         const size_t cnt = (size_t)c.n_sites * c.slices;
         std::vector<int8_t> conf(cnt);
@@ -507,6 +559,156 @@ int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out) {
     }
     const double* base = which == 0 ? d.ustack : d.tstack;
     return download_mat(h, chain, base + (idx - 1) * ms, out);
+}
+
+/* ---- pools ------------------------------------------------------------------ */
+
+int dqmc_pool_create(int device, int max_slots, int64_t budget_bytes, int precision,
+                     dqmc_handle** out) {
+    if (!out || max_slots <= 0 || budget_bytes <= 0)
+        return fail(DQMC_ERR_INVALID, "dqmc_pool_create: bad arguments");
+    *out = nullptr;
+    if (precision != DQMC_PREC_FP64 && precision != DQMC_PREC_MIXED)
+        return fail(DQMC_ERR_INVALID, "dqmc_pool_create: unknown precision");
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0)
+        return fail(DQMC_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
+    if (device < 0 || device >= ndev) return fail(DQMC_ERR_INVALID, "dqmc_pool_create: bad device");
+    CUDA_TRY(cudaSetDevice(device), "cudaSetDevice");
+    CUDA_TRY(dqmc_prepare_chain_kernel(), "kernel attributes");
+    dqmc_handle* h = new dqmc_handle();
+    h->device = device;
+    h->precision = precision;
+    h->pool = true;
+    h->budget = align256((size_t)budget_bytes);
+    h->cfg.assign(max_slots, dqmc_chain_config{});
+    h->lay.assign(max_slots, Layout{});
+    h->host.assign(max_slots, DqmcChain{});
+    h->slot_off.assign(max_slots, 0);
+    h->slot_bytes.assign(max_slots, 0);
+    e = cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete h; return cuda_fail(e, "cudaStreamCreate"); }
+    h->stream = h->own_stream;
+    e = cudaMalloc((void**)&h->arena, h->budget);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_chains, sizeof(DqmcChain) * max_slots);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&h->pinned, sizeof(DqmcChain) * max_slots, 0);
+    if (e != cudaSuccess) {
+        int st = cuda_fail(e, "dqmc_pool_create: allocation of the pool");
+        dqmc_destroy(h);
+        return st;
+    }
+    h->free_blocks[0] = h->budget;
+    int st = push_descriptors(h);
+    if (st != DQMC_OK) { dqmc_destroy(h); return st; }
+    *out = h;
+    return DQMC_OK;
+}
+
+int dqmc_pool_admit(dqmc_handle* h, const dqmc_chain_config* cfg, int* slot) {
+    if (!h || !h->pool || !cfg || !slot) return fail(DQMC_ERR_INVALID, "dqmc_pool_admit: bad arguments");
+    if (int st = validate_config(*cfg, -1)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    int free_slot = -1;
+    for (size_t i = 0; i < h->host.size(); ++i)
+        if (!h->host[i].active) { free_slot = (int)i; break; }
+    if (free_slot < 0) return fail(DQMC_ERR_NOT_READY, "dqmc_pool_admit: no free slot");
+    const Layout L = layout_of(*cfg, h->precision);
+    size_t off = 0;
+    if (!pool_alloc(h, L.bytes, &off))
+        return fail(DQMC_ERR_OOM, "dqmc_pool_admit: chain needs " + std::to_string(L.bytes) +
+                                      " bytes, more than the pool's free budget allows");
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    CUDA_TRY(cudaMemsetAsync(h->arena + off, 0, L.bytes, h->stream), "clear chain workspace");
+    fill_descriptor(h->host[free_slot], *cfg, h->arena + off, L, h->precision);
+    h->host[free_slot].needs_build = 1;
+    h->cfg[free_slot] = *cfg;
+    h->lay[free_slot] = L;
+    h->slot_off[free_slot] = off;
+    h->slot_bytes[free_slot] = L.bytes;
+    h->host_dirty = true;
+    *slot = free_slot;
+    return DQMC_OK;
+}
+
+int dqmc_pool_release(dqmc_handle* h, int slot) {
+    if (int st = check_chain(h, slot)) return st;
+    if (!h->pool) return fail(DQMC_ERR_INVALID, "dqmc_pool_release: not a pool");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    pool_free(h, h->slot_off[slot], h->slot_bytes[slot]);
+    memset(&h->host[slot], 0, sizeof(DqmcChain));
+    h->cfg[slot] = dqmc_chain_config{};
+    h->slot_bytes[slot] = 0;
+    h->host_dirty = true;
+    return DQMC_OK;
+}
+
+int dqmc_pool_set_quota(dqmc_handle* h, int slot, int64_t n_sweeps) {
+    if (int st = check_chain(h, slot)) return st;
+    if (n_sweeps < 0) return fail(DQMC_ERR_INVALID, "dqmc_pool_set_quota: n_sweeps < 0");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    h->host[slot].visits_quota = n_sweeps * 2 * (int64_t)h->host[slot].M;
+    h->host_dirty = true;
+    return DQMC_OK;
+}
+
+int dqmc_pool_slot(dqmc_handle* h, int slot, int64_t* sweeps_done, int64_t* sweeps_left,
+                   int32_t* active) {
+    if (!h || slot < 0 || slot >= (int)h->host.size())
+        return fail(DQMC_ERR_INVALID, "dqmc_pool_slot: slot out of range");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    const DqmcChain& d = h->host[slot];
+    const int64_t per = d.active ? 2 * (int64_t)d.M : 1;
+    if (sweeps_done) *sweeps_done = d.active ? d.visits_done / per : 0;
+    if (sweeps_left) *sweeps_left = d.active ? (d.visits_quota + per - 1) / per : 0;
+    if (active) *active = d.active;
+    return DQMC_OK;
+}
+
+int64_t dqmc_pool_free_bytes(dqmc_handle* h) {
+    if (!h || !h->pool) return -1;
+    int64_t s = 0;
+    for (auto& kv : h->free_blocks) s += (int64_t)kv.second;
+    return s;
+}
+
+int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph) {
+    if (!h || !h->pool) return fail(DQMC_ERR_INVALID, "dqmc_pool_run: not a pool");
+    if (budget_us <= 0) return fail(DQMC_ERR_INVALID, "dqmc_pool_run: budget_us <= 0");
+    if (!use_graph) return launch(h, DQMC_OP_RUN, budget_us, 0, true);
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    const size_t bytes = sizeof(DqmcChain) * h->host.size();
+    if (!h->graph || h->graph_budget_us != budget_us) {
+        if (h->graph) { cudaGraphExecDestroy(h->graph); h->graph = nullptr; }
+        // one replayable step: upload descriptors, time-sliced launch, download
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        cudaError_t e1 = cudaMemcpyAsync(h->d_chains, h->pinned, bytes, cudaMemcpyHostToDevice, h->stream);
+        cudaError_t e2 = dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), DQMC_OP_RUN,
+                                                  budget_us, 0, h->stream);
+        cudaError_t e3 = cudaMemcpyAsync(h->pinned, h->d_chains, bytes, cudaMemcpyDeviceToHost, h->stream);
+        cudaError_t e4 = cudaStreamEndCapture(h->stream, &g);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return cuda_fail(e4 != cudaSuccess ? e4 : (e1 != cudaSuccess ? e1 : (e2 != cudaSuccess ? e2 : e3)),
+                             "graph capture of the pool step");
+        }
+        cudaError_t e5 = cudaGraphInstantiate(&h->graph, g, 0);
+        cudaGraphDestroy(g);
+        if (e5 != cudaSuccess) { h->graph = nullptr; return cuda_fail(e5, "graph instantiate"); }
+        h->graph_budget_us = budget_us;
+    }
+    memcpy(h->pinned, h->host.data(), bytes);
+    CUDA_TRY(cudaGraphLaunch(h->graph, h->stream), "graph launch");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "pool step");
+    memcpy(h->host.data(), h->pinned, bytes);
+    h->host_dirty = false;
+    for (size_t i = 0; i < h->host.size(); ++i)
+        if (h->host[i].active && h->host[i].status != 0)
+            return fail(DQMC_ERR_NUMERICAL, "slot " + std::to_string(i) + " reported status " +
+                                                 std::to_string(h->host[i].status));
+    return DQMC_OK;
 }
 
 }  // extern "C"

@@ -48,6 +48,10 @@ struct DqmcChain {
     // device counterpart of the reference's @bm / TimerOutputs sections
     // (helpers.jl:83-131): see DQMC_PHASE_*
     unsigned long long timers[8];
+    // pool / time-sliced runs: slot in use, stack still to build, remaining
+    // slice visits the chain may run, slice visits run so far
+    int active, needs_build;
+    long long visits_quota, visits_done;
 };
 
 enum { DQMC_PHASE_SWEEP_SPATIAL = 0, DQMC_PHASE_WRAP = 1, DQMC_PHASE_SLICE_CHAIN = 2,
@@ -55,7 +59,8 @@ enum { DQMC_PHASE_SWEEP_SPATIAL = 0, DQMC_PHASE_WRAP = 1, DQMC_PHASE_SLICE_CHAIN
        DQMC_PHASE_T_UPDATE = 6, DQMC_PHASE_OTHER = 7 };
 
 enum { DQMC_OP_SWEEP = 0, DQMC_OP_BUILD = 1, DQMC_OP_GREENS_AT = 2, DQMC_OP_PHYSICAL = 3,
-       DQMC_OP_BUILD_FWD = 4, DQMC_OP_PROPAGATE = 5, DQMC_OP_SWEEP_SPATIAL = 6 };
+       DQMC_OP_BUILD_FWD = 4, DQMC_OP_PROPAGATE = 5, DQMC_OP_SWEEP_SPATIAL = 6,
+       DQMC_OP_RUN = 7 /* time-sliced: arg0 = budget in microseconds */ };
 
 // DqmcChain::prec values (same numbers as DQMC_PREC_* of the C ABI)
 #define DQMC_PREC_FP64_ID 0

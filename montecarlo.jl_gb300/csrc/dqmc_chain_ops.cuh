@@ -73,6 +73,13 @@ __device__ __forceinline__ void udt_one(const Ctx& x, double* U, double* D, doub
 }
 
 
+// nanoseconds of the GPU-wide timer (comparable across SMs)
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // phase timers: thread 0 accumulates SM cycles per DQMC_PHASE_*
 __device__ __forceinline__ long long phase_start() { return threadIdx.x == 0 ? clock64() : 0; }
 __device__ __forceinline__ void phase_stop(const Ctx& x, int phase, long long t0) {
@@ -344,6 +351,9 @@ __device__ __noinline__ void record_prop_error(const Ctx& x) {
             if (v > mx || v != v) mx = v;
         }
         if (mx > c.prop_err_max || mx != mx) c.prop_err_max = mx;
+        // a non-finite Green's function is reported to the host as a
+        // numerical error (status 2) instead of propagating silently
+        if (mx != mx || mx > 1e300) c.status = 2;
         if (mx > 1e-7) {
             c.n_prop_err += 1;
             if (mx > c.prop_err_reported) c.prop_err_reported = mx;

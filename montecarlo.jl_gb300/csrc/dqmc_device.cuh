@@ -232,7 +232,7 @@ __device__ __noinline__ void udt_pivot(int n, double* __restrict__ U, double* __
         __syncthreads();
         if (warp == 0) {
             double best = -1.0;
-            int bi = n;
+            int bi = j;  // never out of range, also when every norm is NaN
             for (int col = j + lane; col < n; col += 32) {
                 double v = sv[col];
                 if (v > best) { best = v; bi = col; }
@@ -380,7 +380,7 @@ __device__ __noinline__ void udt_pivot_sm(int n, double* __restrict__ U, double*
         if (warp == 0) {
             // indmaxcolumn: first column of maximal norm among j..n-1
             long long best = -1;
-            int bi = n;
+            int bi = j;  // never out of range, also when every norm is NaN
             for (int col = j + lane; col < n; col += 32) {
                 long long v = __double_as_longlong(sv[col]);
                 if (v > best) { best = v; bi = col; }

@@ -35,11 +35,44 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
         s->gres = 0;
     }
     __syncthreads();
+    if (!s->c.active) return;  // free pool slot
     if (x.n > DQMC_NMAX || x.nf < 1 || x.nf > 2) {
         if (threadIdx.x == 0) chains[blockIdx.x].status = 1;
         return;
     }
     switch (op) {
+    case DQMC_OP_RUN: {
+        // time slice of a pool: build the stack of a newly admitted chain,
+        // then run slice visits (sweep_spatial + propagate) until the chain's
+        // quota is used up or the budget (arg0 microseconds) has elapsed; the
+        // chain's state carries over to the next slice
+        const unsigned long long t_start = global_ns();
+        const unsigned long long budget = 1000ull * (unsigned long long)arg0;
+        if (s->c.needs_build) {
+            reverse_build_stack(x);
+            propagate(x);
+            if (threadIdx.x == 0) s->c.needs_build = 0;
+            __syncthreads();
+        }
+        const bool res = g_resident_possible(x);
+        if (res && s->c.visits_quota > 0) g_to_arena(x);
+        bool in_arena = res && s->c.visits_quota > 0;
+        while (s->c.visits_quota > 0) {
+            long long t0 = phase_start();
+            sweep_spatial(x);
+            phase_stop(x, DQMC_PHASE_SWEEP_SPATIAL, t0);
+            propagate(x);
+            if (threadIdx.x == 0) {
+                s->c.visits_quota -= 1;
+                s->c.visits_done += 1;
+                s->sxi[1] = (global_ns() - t_start) >= budget;
+            }
+            __syncthreads();
+            if (s->sxi[1]) break;
+        }
+        if (in_arena) g_to_global(x);
+        break;
+    }
     case DQMC_OP_SWEEP: {
         const bool res = g_resident_possible(x);
         if (res) g_to_arena(x);
@@ -91,6 +124,10 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
         g.accepted = s->c.accepted;
         g.proposals = s->c.proposals;
         for (int p = 0; p < 8; ++p) g.timers[p] = s->c.timers[p];
+        g.needs_build = s->c.needs_build;
+        g.visits_quota = s->c.visits_quota;
+        g.visits_done = s->c.visits_done;
+        if (s->c.status) g.status = s->c.status;
     }
 }
 
@@ -98,16 +135,27 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
 
 size_t dqmc_chain_kernel_smem() { return sizeof(dqmc::Smem); }
 
+static bool g_attr_set[64] = {};
+
+cudaError_t dqmc_prepare_chain_kernel() {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (!g_attr_set[dev]) {
+        e = cudaFuncSetAttribute(dqmc::chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)sizeof(dqmc::Smem));
+        if (e != cudaSuccess) return e;
+        g_attr_set[dev] = true;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
                                      cudaStream_t stream) {
-    static bool attr_set = false;
-    const size_t smem = sizeof(dqmc::Smem);
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(dqmc::chain_kernel,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr_set = true;
-    }
-    dqmc::chain_kernel<<<nchains, DQMC_NT, smem, stream>>>(d_chains, nchains, op, arg0, arg1);
+    cudaError_t e = dqmc_prepare_chain_kernel();
+    if (e != cudaSuccess) return e;
+    dqmc::chain_kernel<<<nchains, DQMC_NT, sizeof(dqmc::Smem), stream>>>(d_chains, nchains, op,
+                                                                          arg0, arg1);
     return cudaGetLastError();
 }

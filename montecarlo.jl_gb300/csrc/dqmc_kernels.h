@@ -5,6 +5,9 @@
 #include "dqmc_chain.h"
 
 size_t dqmc_chain_kernel_smem();
+// Sets the kernel's shared-memory attribute once per device (call before any
+// stream capture of a launch).
+cudaError_t dqmc_prepare_chain_kernel();
 // One CTA per chain; op is one of DQMC_OP_*.
 cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
                                      cudaStream_t stream);

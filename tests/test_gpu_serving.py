@@ -1,0 +1,92 @@
+"""Pools: HBM-budget admission, time-sliced launches, continuous batching.
+
+A chain advanced in a pool over many time slices must be bit-identical to the
+same chain swept by a plain handle, and a request must give the same result
+served alone and in a mix of other requests."""
+import numpy as np
+import pytest
+
+from _util import FIELD_U, chain_config, make_setup, maxdiff, oracle_chain
+
+pytestmark = pytest.mark.gpu
+
+
+def test_pool_budget_admission(pkg, lib):
+    model, param, fld, exps = make_setup(pkg, L=4, U=4.0, beta=1.0, safe_mult=5)
+    cfg = chain_config(lib, model, param, fld, 1)
+    need = lib.chain_bytes(cfg)
+    pool = lib.Pool(4, int(2.5 * need) + 512)
+    a = pool.admit(cfg)
+    b = pool.admit(cfg)
+    assert a is not None and b is not None and a != b
+    assert pool.admit(cfg) is None  # over budget
+    free_before = pool.free_bytes()
+    pool.release(a)
+    assert pool.free_bytes() > free_before
+    c = pool.admit(cfg)
+    assert c is not None
+    pool.close()
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_pool_time_slices_equal_plain_sweeps(pkg, lib, oracle, use_graph):
+    model, param, fld, exps = make_setup(pkg, L=6, U=-4.0, beta=2.0, safe_mult=5)
+    cfg = chain_config(lib, model, param, fld, 42)
+    h = lib.Handle([cfg])
+    h.set_hopping(0, exps)
+    h.init_random_field(0)
+    h.initialize_run()
+    h.sweep(3)
+    pool = lib.Pool(3, 3 * lib.chain_bytes(cfg) + 4096)
+    slot = pool.admit(cfg)
+    pool.set_hopping(slot, exps)
+    pool.init_random_field(slot)
+    pool.set_quota(slot, 3)
+    runs = 0
+    while pool.slot(slot)[1] > 0:
+        pool.run(200, use_graph)  # 0.2 ms slices: many launches per sweep
+        runs += 1
+    assert runs > 3
+    assert pool.slot(slot)[0] == 3
+    assert np.array_equal(pool.get_field(slot), h.get_field(0))
+    assert np.array_equal(pool.greens(slot), h.greens(0))
+    assert pool.get_rng(slot) == h.get_rng(0)
+    oc = oracle_chain(oracle, model, param, fld, exps, 42)
+    oc.init_random_conf()
+    oc.initialize_run()
+    oc.sweeps(3)
+    assert np.array_equal(pool.get_field(slot), oc.get_conf())
+    assert maxdiff(pool.greens(slot), oc.greens()) < 1e-10
+    pool.close()
+
+
+def test_request_alone_equals_request_in_mix(pkg, lib):
+    reqs = [pkg.Request(0, "square", 4, 4.0, 2.0, 30, 11),
+            pkg.Request(1, "honeycomb", 2, -3.0, 4.0, 20, 12),
+            pkg.Request(2, "square", 6, 2.0, 2.0, 25, 13, arrival=0.0),
+            pkg.Request(3, "square", 4, -6.0, 1.0, 40, 14)]
+    alone = pkg.Server(max_slots=2, budget_bytes=64 << 20, quantum_us=500)
+    r_alone = alone.serve([reqs[0]], realtime=False)["results"][0]
+    alone.close()
+    mix = pkg.Server(max_slots=3, budget_bytes=64 << 20, quantum_us=300)
+    out = mix.serve(reqs, realtime=False)
+    mix.close()
+    assert out["unfinished"] == 0 and len(out["results"]) == 4
+    r_mix = out["results"][0]
+    assert np.array_equal(r_alone.conf, r_mix.conf)
+    assert np.array_equal(r_alone.greens, r_mix.greens)
+    assert r_alone.stats["accepted"] == r_mix.stats["accepted"]
+    assert out["p50_block_s"] is not None and out["p99_block_s"] >= out["p50_block_s"]
+
+
+def test_uneven_ensemble_time_sliced(pkg, lib):
+    specs = [(4, 4.0, 2.0), (6, 3.0, 4.0), (8, 6.0, 1.0), (3, 2.0, 2.0)]
+    ce = []
+    for i, (L, U, beta) in enumerate(specs):
+        model, param, fld, exps = make_setup(pkg, L=L, U=U, beta=beta, safe_mult=10)
+        ce.append((chain_config(lib, model, param, fld, 500 + i), exps))
+    out = pkg.run_ensemble(ce, seconds=0.5, quantum_us=20000)
+    assert out["sweeps"] > 0 and all(s > 0 for s in out["per_chain"])
+    # smaller chains do more sweeps in the same slices
+    assert out["per_chain"][3] > out["per_chain"][2]
+    assert out["max_propagation_error"] < 1e-6
