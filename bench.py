@@ -219,7 +219,10 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, seed=3):
             ce.append((_lib.ChainConfig(len(model.l), 1, param.slices, k, fld.kind, 1, fld.alpha, s),
                        pkg.hopping_exponentials(model.hopping_matrix(), dt)))
         r = pkg.run_ensemble(ce, seconds=seconds, quantum_us=100000, precision=prec)
+        pe = np.array(r["per_chain_propagation_error"])
         out[name] = {"sweeps_per_s": r["sweeps_per_s"], "max_propagation_error": r["max_propagation_error"],
+                     "median_chain_propagation_error": float(np.median(pe)),
+                     "chains_over_1e-6": int(np.sum(pe > 1e-6)),
                      "safe_mult_histogram": {str(k): ks.count(k) for k in sorted(set(ks))},
                      "autotune_s": tune_s, "timed_s": r["wall"], "launches": r["launches"]}
     out["mixed_vs_plain"] = out["mixed"]["sweeps_per_s"] / out["plain_fp64"]["sweeps_per_s"]
@@ -315,7 +318,9 @@ def main():
     torch.cuda.empty_cache()
 
     # ---- device-resident throughput (value)
-    seed0 = 2 + rank * B_chains
+    from montecarlo_gb300 import replicas
+
+    seed0 = replicas.chain_seeds(rank, B_chains)[0]  # disjoint seeds per rank
     h = _lib.Handle(configs(seed0))
     h.set_hopping(-1, exps)
     h.init_random_field(-1)
@@ -347,14 +352,12 @@ def main():
     launch_ms = [evs[i].elapsed_time(evs[i + 1]) for i in range(args.steps)]
     elapsed = evs[0].elapsed_time(evs[-1]) / 1e3
     if dist:
-        t = torch.tensor([elapsed], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+        elapsed = replicas.max_over_ranks(elapsed, dist, device="cuda")
     st1 = [h.stats(i) for i in range(B_chains)]
     acc = sum(s1["accepted"] - s0["accepted"] for s0, s1 in zip(st0, st1)) / max(
         1, sum(s1["proposals"] - s0["proposals"] for s0, s1 in zip(st0, st1)))
     max_prop = max(s["max_propagation_error"] for s in st1)
-    value = world * B_chains * args.steps / elapsed
+    value = replicas.aggregate_rate(B_chains * args.steps, world, elapsed)
     flops_launch = B_chains * sweep_flops(n, nf, M, nr, acc)
     avg_launch = statistics.mean(launch_ms) / 1e3
     achieved = flops_launch / avg_launch / 1e12
@@ -389,9 +392,7 @@ def main():
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if dist:
-        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+        e2e_s = replicas.max_over_ranks(e2e_s, dist, device="cuda")
     h2.close()
     h2d = (4 * n * n * 8 + B_chains * n * M) / args.steps
     d2h = B_chains * (nf * n * n * 8 + n * M + 0)
@@ -424,7 +425,24 @@ def main():
         mixed_v = B_chains * args.steps / (e0.elapsed_time(e1) / 1e3)
         mp = max(hm.stats(i)["max_propagation_error"] for i in range(B_chains))
         hm.close()
+        # |dG| of the mixed path against FP64 for the same field configurations:
+        # thermalised configurations of 4 chains, G from scratch at every
+        # stabilisation slice, mixed (double-float slice chains) vs FP64
+        confs = autotune.thermalize(specs2[:4])
+        hcmp = [_lib.Handle([_lib.ChainConfig(n, nf, M, k_mixed, fld.kind, 1, fld.alpha, seed0 + j)
+                             for j in range(4)], precision=pr)
+                for pr in (_lib.PREC_FP64, _lib.PREC_MIXED)]
+        for hc in hcmp:
+            hc.set_hopping(-1, exps)
+            for j in range(4):
+                hc.set_field(j, confs[j])
+        bounds = sorted({0, M} | {b for _, b in pkg.generate_chunks(M, k_mixed)})
+        dG = max(float(np.max(np.abs(hcmp[0].calculate_greens(j, s) - hcmp[1].calculate_greens(j, s))))
+                 for j in range(4) for s in bounds)
+        for hc in hcmp:
+            hc.close()
         extras["mixed"] = {"value": mixed_v, "unit": "sweeps/s", "vs_plain_fp64": mixed_v / value,
+                           "max_dG_vs_fp64_at_stabilisations": dG,
                            "max_propagation_error": mp, "safe_mult": k_mixed,
                            "note": "wraps and slice chains as double-float products on the FP32 "
                                    "pipe; UDT, reconstruction, ratios, rank-1 updates FP64"}

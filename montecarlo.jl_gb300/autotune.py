@@ -49,7 +49,7 @@ def thermalize(specs, sweeps=6, safe_mult=4, device=0):
 
 
 def tune_safe_mult(specs, tol=1e-6, precision=_lib.PREC_FP64, candidates=CANDIDATES,
-                   confs=None, therm_sweeps=6, probe_sweeps=2, safety=0.5, device=0):
+                   confs=None, therm_sweeps=6, probe_sweeps=3, safety=0.1, device=0):
     """Chosen safe_mult per spec and the propagation error measured with it."""
     if confs is None:
         confs = thermalize(specs, sweeps=therm_sweeps, device=device)

@@ -140,6 +140,101 @@ class DQMC:
             obs.measure(G, self)
 
 
+class ConfigRecorder:
+    """Field configurations recorded every `rate` sweeps, compressed
+    (ConfigRecorder, src/configurations.jl:24-66; compress / decompress,
+    fields.jl:331-334 and 472-491): Hirsch fields as one bit per entry
+    (x == 1), Gauss-Hermite fields as two bits (x - 1)."""
+
+    def __init__(self, rate: int = 10):
+        self.rate = rate
+        self.configs = []
+        self.shape = None
+        self.ghq = False
+
+    def push(self, conf, sweep, ghq=False):
+        if sweep % self.rate != 0:
+            return
+        self.shape, self.ghq = conf.shape, ghq
+        c = np.asarray(conf, dtype=np.int8).ravel(order="F")
+        if ghq:
+            v = (c - 1).astype(np.uint8)
+            bits = np.stack([(v >> 1) & 1, v & 1], axis=1).ravel()
+        else:
+            bits = (c == 1).astype(np.uint8)
+        self.configs.append(np.packbits(bits))
+
+    def __len__(self):
+        return len(self.configs)
+
+    def __getitem__(self, i):
+        n = int(np.prod(self.shape))
+        if self.ghq:
+            bits = np.unpackbits(self.configs[i])[: 2 * n].reshape(n, 2)
+            c = (1 + 2 * bits[:, 0] + bits[:, 1]).astype(np.int8)
+        else:
+            bits = np.unpackbits(self.configs[i])[:n]
+            c = (2 * bits.astype(np.int8) - 1).astype(np.int8)
+        return c.reshape(self.shape, order="F")
+
+
+def replay(mc, configurations, measure_rate: int = 1):
+    """replay! (DQMC.jl:418-505): for every recorded configuration recompute G
+    from scratch (calculate_greens(mc, 0), the equal-time G at slice 1) and run
+    the measurements on its physical form."""
+    for i in range(0, len(configurations), measure_rate):
+        conf = configurations[i]
+        mc.handle.set_field(0, np.asfortranarray(conf))
+        G_eff = mc.handle.calculate_greens(0, 0)
+        mc.handle.set_greens(0, G_eff)
+        G = mc.handle.greens(0, physical=True)
+        for obs in mc.measurements.values():
+            obs.measure(G, mc)
+        mc.last_sweep = i + 1
+
+
+def save(mc, path):
+    """Checkpoint of a simulation (FileIO.jl:10-57; flavors/DQMC/FileIO.jl:10-22):
+    parameters, model, field, RNG state, last sweep and recorded
+    configurations.  The stack is not saved: resume rebuilds it from the field,
+    as the reference does (DQMC.jl:178-179)."""
+    key, ctr = mc.handle.get_rng(0)
+    conf = mc.handle.get_field(0)
+    p = mc.parameters
+    lat = mc.model.l
+    np.savez(path, conf=conf, rng=np.array([key, ctr], dtype=np.uint64),
+             last_sweep=mc.last_sweep, seed=mc.seed,
+             params=np.array([p.beta, p.delta_tau, p.slices, p.safe_mult, p.thermalization,
+                              p.sweeps, p.measure_rate], dtype=np.float64),
+             model=np.array([mc.model.t, mc.model.mu, mc.model.U]),
+             lattice=np.array([lat.name] + [str(x) for x in lat.Ls]),
+             field=np.array([type(mc.field).__name__]), precision=np.array([mc.precision]))
+
+
+def resume(path, **kwargs):
+    """Rebuild a simulation from a checkpoint; the next run continues the
+    chain where it stopped (resume!, FileIO.jl:155-171)."""
+    from . import lattices, model as _model
+
+    d = np.load(path, allow_pickle=False)
+    name, *Ls = [str(x) for x in d["lattice"]]
+    ctor = {"Square": lattices.SquareLattice, "Honeycomb": lattices.Honeycomb,
+            "Chain": lattices.Chain, "Cubic": lattices.CubicLattice,
+            "Triangular": lattices.TriangularLattice}[name]
+    t, mu, U = [float(x) for x in d["model"]]
+    m = _model.HubbardModel(ctor(*[int(x) for x in Ls]), U=U, mu=mu, t=t)
+    beta, dt, slices, k, th, sw, mr = d["params"]
+    mc = DQMC(m, seed=int(d["seed"]), field=getattr(_model, str(d["field"][0])),
+              beta=float(beta), delta_tau=float(dt), safe_mult=int(k), thermalization=int(th),
+              sweeps=int(sw), measure_rate=int(mr), precision=str(d["precision"][0]), **kwargs)
+    mc.field.conf[:] = d["conf"]
+    mc.handle.set_field(0, np.asfortranarray(d["conf"]))
+    key, ctr = [int(x) for x in d["rng"]]
+    mc.handle.set_rng(0, key, ctr)
+    mc.last_sweep = int(d["last_sweep"])
+    return mc
+
+
 class Measurement:
     """A DQMC measurement: a kernel over the physical G pushed into a LogBinner
     (DQMCMeasurement, measurements/generic.jl:6-13)."""

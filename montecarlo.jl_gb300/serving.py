@@ -194,8 +194,9 @@ def run_ensemble(configs_and_exps, seconds: float, quantum_us=50000, precision=_
         st1 = pool.stats(s)
         props = st1["proposals"] - st0["proposals"]
         sweeps.append(props / (2.0 * cfg.slices * cfg.n_sites))
-    maxprop = max(pool.stats(s)["max_propagation_error"] for s in slots)
+    per_err = [pool.stats(s)["max_propagation_error"] for s in slots]
+    maxprop = max(per_err)
     pool.close()
     return dict(wall=wall, launches=launches, sweeps=float(sum(sweeps)),
                 sweeps_per_s=float(sum(sweeps)) / wall, per_chain=sweeps,
-                max_propagation_error=maxprop)
+                max_propagation_error=maxprop, per_chain_propagation_error=per_err)

@@ -88,3 +88,18 @@ def test_field_alpha_and_flavours(pkg):
     assert pkg.MagneticHirschField(p, rep).unique_flavors == 2
     with pytest.raises(NotImplementedError):
         pkg.DensityHirschField(p, rep)  # field/U mismatch: complex path
+
+
+def test_config_recorder_roundtrip(pkg):
+    """compress / decompress (fields.jl:331-334, 472-484) for both field families."""
+    from montecarlo_gb300.dqmc import ConfigRecorder
+    rng = np.random.default_rng(1)
+    for ghq, values in ((False, np.array([-1, 1], dtype=np.int8)),
+                        (True, np.array([1, 2, 3, 4], dtype=np.int8))):
+        rec = ConfigRecorder(rate=2)
+        confs = [np.asfortranarray(rng.choice(values, size=(7, 5))) for _ in range(6)]
+        for s, c in enumerate(confs, start=1):
+            rec.push(c, s, ghq=ghq)
+        assert len(rec) == 3
+        for i, c in enumerate(confs[1::2]):
+            assert np.array_equal(rec[i], c)
