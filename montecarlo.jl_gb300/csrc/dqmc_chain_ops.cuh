@@ -257,13 +257,13 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout) {
         udt_one(x, tr, dr, g, b, false);
         mm<false, false>(n, tl, ul, tr, x.s->tiles);
         __syncthreads();
-        rdivp(n, ur, g, ul, pv, bf);
+        rdivp(n, ur, g, ul, pv, bf, x.s->sv);
         mm<true, false>(n, tr, tl, ur, x.s->tiles);
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += DQMC_NT) tr[(size_t)i * n + i] += dr[i];
         __syncthreads();
         udt_one(x, ul, dr, tr, b, false);
-        rdivp(n, ur, tr, g, pv, bf);
+        rdivp(n, ur, tr, g, pv, bf, x.s->sv);
         mm<false, false>(n, tr, tl, ul, x.s->tiles);
         for (int i = threadIdx.x; i < n; i += DQMC_NT) dl[i] = 1.0 / dr[i];
         __syncthreads();
@@ -478,8 +478,12 @@ __device__ __noinline__ void propagate(const Ctx& x) {
 // sweep_spatial (local_updates.jl:23-60) with propose_local / accept_local!
 // (fields.jl:58-84, 176-209, 271-286, 340-344, 388-393, 440-449, 497-503,
 // 563-573, 627-637).  Thread 0 makes the sequential decisions with the
-// reference's operation order (no contraction); all threads apply the rank-1
-// update G -= (I - G)[:, i] (Delta/R) G[i, :] per flavour block.
+// reference's operation order (no contraction), scanning on through rejected
+// proposals without a barrier; at an accepted one, warps 1.. apply the rank-1
+// update G -= (I - G)[:, i] (Delta/R) G[i, :] per flavour block while warp 0
+// applies the same fused multiply-add to a shared-memory copy of G's diagonal
+// and thread 0 goes on deciding from it: the next decisions overlap the update
+// and read bit-identical diagonal values.
 __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     DqmcChain& c = *x.c;
     const int n = x.n, nf = x.nf;
@@ -487,83 +491,104 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     int8_t* s = c.conf + (size_t)(slice - 1) * n;
     const bool ghq = (c.kind >= 2);
     const bool twoflv = (nf == 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    double* diag = x.s->ev;  // [nf * n] mirror of the diagonals (ev is free here)
+    for (int e = tid; e < nf * n; e += DQMC_NT) {
+        const int b = e / n, k = e % n;
+        diag[e] = c.G[(size_t)b * x.nn + (size_t)k * n + k];
+    }
+    __syncthreads();
     long long acc_count = 0;
-    // broadcast slots: sxd[0..1] = invRDelta per block, sxi[0] = accept, sxi[1] = new value
-    for (int i = 0; i < n; ++i) {
-        if (threadIdx.x == 0) {
-            const double g0 = c.G[(size_t)i * n + i];
-            const double g1 = twoflv ? c.G[x.nn + (size_t)i * n + i] : 0.0;
-            int t;
-            int xnew = 0;
-            double gr = 1.0, gq = 1.0;
-            if (ghq) {
-                const int xold = s[i];
-                const uint64_t w = dqmc_philox_word(c.key, c.ctr);
-                c.ctr += 1;
-                const int r = dqmc_word_to_choice3(w);
-                xnew = r + (r + 1 >= xold ? 2 : 1);  // choices[x_old, r+1] (fields.jl:534)
-                t = (xold - 1) * 4 + (xnew - 1);
-                gr = c.gam[xnew - 1];
-                gq = c.gam[xold - 1];
-            } else {
-                t = s[i] > 0 ? 1 : 0;
+    int i = 0, round = 0;
+    while (true) {
+        if (tid == 0) {
+            int j = i;
+            for (; j < n; ++j) {
+                const double g0 = diag[j];
+                const double g1 = twoflv ? diag[n + j] : 0.0;
+                int t;
+                int xnew = 0;
+                double gr = 1.0, gq = 1.0;
+                if (ghq) {
+                    const int xold = s[j];
+                    const uint64_t w = dqmc_philox_word(c.key, c.ctr);
+                    c.ctr += 1;
+                    const int r = dqmc_word_to_choice3(w);
+                    xnew = r + (r + 1 >= xold ? 2 : 1);  // choices[x_old, r+1] (fields.jl:534)
+                    t = (xold - 1) * 4 + (xnew - 1);
+                    gr = c.gam[xnew - 1];
+                    gq = c.gam[xold - 1];
+                } else {
+                    t = s[j] > 0 ? 1 : 0;
+                }
+                const double d0 = c.delta0[t], d1 = c.delta1[t];
+                const double R0 = __dadd_rn(1.0, __dmul_rn(d0, __dsub_rn(1.0, g0)));
+                double detratio;
+                double R1 = 0.0;
+                if (twoflv) {
+                    R1 = __dadd_rn(1.0, __dmul_rn(d1, __dsub_rn(1.0, g1)));
+                    detratio = __dmul_rn(R0, R1);
+                } else {
+                    detratio = __dmul_rn(R0, R0);
+                }
+                if (ghq) detratio = __ddiv_rn(__dmul_rn(detratio, gr), gq);
+                const double p = __dmul_rn(c.wboson[t], detratio);
+                if (p < 0.0) c.n_neg_p += 1;
+                int accept;
+                if (p > 1.0) {
+                    accept = 1;
+                } else {
+                    const uint64_t w = dqmc_philox_word(c.key, c.ctr);
+                    c.ctr += 1;
+                    accept = dqmc_word_to_uniform(w) < p;
+                }
+                c.proposals += 1;
+                if (accept) {
+                    x.s->sxd[0] = __ddiv_rn(d0, R0);
+                    x.s->sxd[1] = twoflv ? __ddiv_rn(d1, R1) : 0.0;
+                    s[j] = ghq ? (int8_t)xnew : (int8_t)(-s[j]);
+                    c.accepted += 1;
+                    break;
+                }
             }
-            const double d0 = c.delta0[t], d1 = c.delta1[t];
-            const double R0 = __dadd_rn(1.0, __dmul_rn(d0, __dsub_rn(1.0, g0)));
-            double detratio;
-            double R1 = 0.0;
-            if (twoflv) {
-                R1 = __dadd_rn(1.0, __dmul_rn(d1, __dsub_rn(1.0, g1)));
-                detratio = __dmul_rn(R0, R1);
-            } else {
-                detratio = __dmul_rn(R0, R0);
-            }
-            if (ghq) detratio = __ddiv_rn(__dmul_rn(detratio, gr), gq);
-            const double p = __dmul_rn(c.wboson[t], detratio);
-            if (p < 0.0) c.n_neg_p += 1;
-            int accept;
-            if (p > 1.0) {
-                accept = 1;
-            } else {
-                const uint64_t w = dqmc_philox_word(c.key, c.ctr);
-                c.ctr += 1;
-                accept = dqmc_word_to_uniform(w) < p;
-            }
-            c.proposals += 1;
-            x.s->sxi[2 + (i & 1)] = accept;
-            if (accept) {
-                x.s->sxd[0] = __ddiv_rn(d0, R0);
-                x.s->sxd[1] = twoflv ? __ddiv_rn(d1, R1) : 0.0;
-                s[i] = ghq ? (int8_t)xnew : (int8_t)(-s[i]);
-                c.accepted += 1;
-            }
+            // double-buffered slot: thread 0 writes the next round's slot
+            // while slow threads may still read this one
+            x.s->sxi[2 + (round & 1)] = j;
+        }
+        __syncthreads();  // also: the previous round's update is complete
+        const int j = x.s->sxi[2 + (round & 1)];
+        ++round;
+        if (j >= n) break;
+        acc_count += 1;
+        for (int e = tid; e < nf * n; e += DQMC_NT) {
+            const int b = e / n, k = e % n;
+            const double* g = c.G + (size_t)b * x.nn;
+            double ig = -g[(size_t)j * n + k];
+            if (k == j) ig += 1.0;
+            x.s->r1.col[b][k] = ig;
+            x.s->r1.row[b][k] = x.s->sxd[b] * g[(size_t)k * n + j];
         }
         __syncthreads();
-        // double-buffered flag: thread 0 writes slot (i+1)&1 next while slow
-        // threads may still read slot i&1 here
-        if (x.s->sxi[2 + (i & 1)]) {
-            acc_count += 1;
-            for (int e = threadIdx.x; e < nf * n; e += DQMC_NT) {
-                const int b = e / n, j = e % n;
-                const double* g = c.G + (size_t)b * x.nn;
-                double ig = -g[(size_t)i * n + j];
-                if (j == i) ig += 1.0;
-                x.s->r1.col[b][j] = ig;
-                x.s->r1.row[b][j] = x.s->sxd[b] * g[(size_t)j * n + i];
+        if (warp == 0) {
+            for (int e = lane; e < nf * n; e += 32) {
+                const int b = e / n, k = e % n;
+                diag[e] = fma(-x.s->r1.col[b][k], x.s->r1.row[b][k], diag[e]);
             }
-            __syncthreads();
+            __syncwarp();
+        } else {
+            const int w = tid - 32, nw = DQMC_NT / 32 - 1;
             for (int b = 0; b < nf; ++b) {
                 double* g = c.G + (size_t)b * x.nn;
                 const double* cl = x.s->r1.col[b];
                 const double* rw = x.s->r1.row[b];
-                for (int k = threadIdx.x & 63; k < n; k += 64) {
+                for (int k = w & 31; k < n; k += 32) {
                     const double ck = -cl[k];
-                    for (int l = threadIdx.x >> 6; l < n; l += DQMC_NT / 64)
+                    for (int l = w >> 5; l < n; l += nw)
                         g[k + (size_t)l * n] = fma(ck, rw[l], g[k + (size_t)l * n]);
                 }
             }
-            __syncthreads();
         }
+        i = j + 1;
     }
     return acc_count;
 }

@@ -346,9 +346,11 @@ __device__ __noinline__ void udt_pivot(int n, double* __restrict__ U, double* __
 // (sIn, sU: n*(n+1) doubles each, leading dimension n+1).  Same algorithm and
 // outputs as udt_pivot, organised for GB300's narrow FP64 pipe, where every
 // FP64 warp instruction costs the same pipe time however few lanes do useful
-// work: two threads per column run the dot products and updates down the
-// column (one shuffle to combine), instead of a warp per column with a
-// five-level reduction.  The column norms that the reference recomputes each
+// work and a dependent FP64 instruction waits about one warp-instruction pass
+// of the pipe: four threads per column, each with two independent
+// accumulation chains, run the dot products and updates down the column (two
+// shuffles to combine), instead of a warp per column with a five-level
+// reduction.  The column norms that the reference recomputes each
 // step (indmaxcolumn) come out of the reflector-application pass, which
 // already holds the updated columns; the pivot search compares the norms'
 // bit patterns on the integer pipe (non-negative doubles order like their
@@ -363,16 +365,25 @@ __device__ __noinline__ void udt_pivot_sm(int n, double* __restrict__ U, double*
     for (int e = tid; e < n * n; e += DQMC_NT) sIn[(e % n) + (e / n) * ld] = In[e];
     for (int i = tid; i < n; i += DQMC_NT) piv[i] = i + 1;
     __syncthreads();
-    // initial squared column norms: two threads per column (the guard is
-    // warp-uniform so every lane of a participating warp reaches the shuffle)
-    if (warp * 32 < 2 * n) {
-        const bool act = tid < 2 * n;
-        const int col = act ? (tid >> 1) : 0, h = tid & 1;
+    // initial squared column norms: four threads per column, two accumulation
+    // chains each (the guard is warp-uniform so every lane of a participating
+    // warp reaches the shuffles)
+    if (warp * 32 < 4 * n) {
+        const bool act = tid < 4 * n;
+        const int col = act ? (tid >> 2) : 0, h = tid & 3;
         const double* a = sIn + col * ld;
-        double q = 0.0;
-        if (act)
-            for (int r = h; r < n; r += 2) q = fma(a[r], a[r], q);
+        double q0 = 0.0, q1 = 0.0;
+        if (act) {
+            int r = h;
+            for (; r + 4 < n; r += 8) {
+                q0 = fma(a[r], a[r], q0);
+                q1 = fma(a[r + 4], a[r + 4], q1);
+            }
+            if (r < n) q0 = fma(a[r], a[r], q0);
+        }
+        double q = q0 + q1;
         q += __shfl_xor_sync(0xffffffffu, q, 1);
+        q += __shfl_xor_sync(0xffffffffu, q, 2);
         if (act && h == 0) sv[col] = q;
     }
     __syncthreads();
@@ -425,30 +436,50 @@ __device__ __noinline__ void udt_pivot_sm(int n, double* __restrict__ U, double*
             if (lane == 0) { tau[j] = t; sxd[0] = t; }
         }
         __syncthreads();
-        // reflectorApply! (UDT.jl:53-70) fused with the next step's column norms
+        // reflectorApply! (UDT.jl:53-70) fused with the next step's column
+        // norms: four threads per column, two accumulation chains each
         const int ncols = n - j - 1;
-        if (warp * 32 < 2 * ncols) {
+        if (warp * 32 < 4 * ncols) {
             const double t = sxd[0];
             const double* x = sIn + j * ld;
-            const bool act = tid < 2 * ncols;
-            const int col = j + 1 + (tid >> 1), h = tid & 1;
+            const bool act = tid < 4 * ncols;
+            const int col = j + 1 + (tid >> 2), h = tid & 3;
             double* a = sIn + (act ? col : j) * ld;
             const double aj = act ? a[j] : 0.0;
-            double s = 0.0;
-            if (act)
-                for (int r = j + 1 + h; r < n; r += 2) s = fma(x[r], a[r], s);
+            double s0 = 0.0, s1 = 0.0;
+            if (act) {
+                int r = j + 1 + h;
+                for (; r + 4 < n; r += 8) {
+                    s0 = fma(x[r], a[r], s0);
+                    s1 = fma(x[r + 4], a[r + 4], s1);
+                }
+                if (r < n) s0 = fma(x[r], a[r], s0);
+            }
+            double s = s0 + s1;
             s += __shfl_xor_sync(0xffffffffu, s, 1);
+            s += __shfl_xor_sync(0xffffffffu, s, 2);
             const double vAj = t * (aj + s);
-            double q = 0.0;
+            double q0 = 0.0, q1 = 0.0;
             if (act) {
                 if (h == 0) a[j] = aj - vAj;
-                for (int r = j + 1 + h; r < n; r += 2) {
-                    double v = fma(-x[r], vAj, a[r]);
-                    a[r] = v;
-                    q = fma(v, v, q);
+                int r = j + 1 + h;
+                for (; r + 4 < n; r += 8) {
+                    const double v0 = fma(-x[r], vAj, a[r]);
+                    const double v1 = fma(-x[r + 4], vAj, a[r + 4]);
+                    a[r] = v0;
+                    a[r + 4] = v1;
+                    q0 = fma(v0, v0, q0);
+                    q1 = fma(v1, v1, q1);
+                }
+                if (r < n) {
+                    const double v0 = fma(-x[r], vAj, a[r]);
+                    a[r] = v0;
+                    q0 = fma(v0, v0, q0);
                 }
             }
+            double q = q0 + q1;
             q += __shfl_xor_sync(0xffffffffu, q, 1);
+            q += __shfl_xor_sync(0xffffffffu, q, 2);
             if (act && h == 0) sv[col] = q;
         }
         __syncthreads();
@@ -463,21 +494,29 @@ __device__ __noinline__ void udt_pivot_sm(int n, double* __restrict__ U, double*
     __syncthreads();
     for (int k = n - 2; k >= 0; --k) {
         const int ncols = n - k;
-        if (warp * 32 < 2 * ncols) {
+        if (warp * 32 < 4 * ncols) {
             const double* v = sIn + k * ld;
             const double t = tau[k];
-            const bool act = tid < 2 * ncols;
-            const int col = k + (tid >> 1), h = tid & 1;
+            const bool act = tid < 4 * ncols;
+            const int col = k + (tid >> 2), h = tid & 3;
             double* u = sU + (act ? col : k) * ld;
             const double uk = act ? u[k] : 0.0;
-            double s = 0.0;
-            if (act)
-                for (int r = k + 1 + h; r < n; r += 2) s = fma(v[r], u[r], s);
+            double s0 = 0.0, s1 = 0.0;
+            if (act) {
+                int r = k + 1 + h;
+                for (; r + 4 < n; r += 8) {
+                    s0 = fma(v[r], u[r], s0);
+                    s1 = fma(v[r + 4], u[r + 4], s1);
+                }
+                if (r < n) s0 = fma(v[r], u[r], s0);
+            }
+            double s = s0 + s1;
             s += __shfl_xor_sync(0xffffffffu, s, 1);
+            s += __shfl_xor_sync(0xffffffffu, s, 2);
             const double vB = t * (uk + s);
             if (act) {
                 if (h == 0) u[k] = uk - vB;
-                for (int r = k + 1 + h; r < n; r += 2) u[r] = fma(-v[r], vB, u[r]);
+                for (int r = k + 1 + h; r < n; r += 4) u[r] = fma(-v[r], vB, u[r]);
             }
         }
         __syncthreads();
@@ -509,7 +548,13 @@ __device__ __noinline__ void udt_pivot_sm(int n, double* __restrict__ U, double*
 // by 1/T[j,j] instead of dividing).  Rows of A are independent: one thread per
 // row runs the forward substitution.
 __device__ __noinline__ void rdivp(int n, double* __restrict__ A, const double* __restrict__ T,
-                      double* __restrict__ O, const int* __restrict__ piv, bool block_form) {
+                      double* __restrict__ O, const int* __restrict__ piv, bool block_form,
+                      double* __restrict__ rcp) {
+    // 1/T[j,j] once per column (the block form's invtjj); the dense form's
+    // division x / T[j,j] becomes the same multiply (rounding-level change),
+    // which keeps DP divisions off the narrow FP64 pipe's critical path
+    (void)block_form;
+    for (int j = threadIdx.x; j < n; j += DQMC_NT) rcp[j] = 1.0 / T[(size_t)j * n + j];
     for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
         int i = e % n, j = e / n;
         O[e] = A[i + (size_t)(piv[j] - 1) * n];
@@ -518,10 +563,15 @@ __device__ __noinline__ void rdivp(int n, double* __restrict__ A, const double* 
     for (int i = threadIdx.x; i < n; i += DQMC_NT) {
         for (int j = 0; j < n; ++j) {
             const double* tj = T + (size_t)j * n;
-            double x = O[i + (size_t)j * n];
-            for (int k = 0; k < j; ++k) x = fma(-A[i + (size_t)k * n], tj[k], x);
-            double tjj = tj[j];
-            A[i + (size_t)j * n] = block_form ? x * (1.0 / tjj) : x / tjj;
+            // two independent accumulation chains halve the dependent-FMA latency
+            double x0 = O[i + (size_t)j * n], x1 = 0.0;
+            int k = 0;
+            for (; k + 1 < j; k += 2) {
+                x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
+                x1 = fma(-A[i + (size_t)(k + 1) * n], tj[k + 1], x1);
+            }
+            if (k < j) x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
+            A[i + (size_t)j * n] = (x0 + x1) * rcp[j];
         }
     }
     __syncthreads();
