@@ -475,6 +475,34 @@ __device__ __noinline__ void propagate(const Ctx& x) {
     }
 }
 
+#define DQMC_DELAY 16  // pending rank-1 updates per flush when G is in global memory
+
+// G -= U W for the pending updates (U: n x p columns u_m = (I - G)[:, i_m],
+// W: p x n rows w_m = (Delta/R) G[i_m, :], stored column / row contiguous
+// with stride n), one flavour block.  Each thread keeps its row's p entries
+// of U in registers.
+__device__ void flush_delayed(const Ctx& x, int p) {
+    const int n = x.n;
+    for (int b = 0; b < x.nf; ++b) {
+        double* g = x.c->G + (size_t)b * x.nn;
+        const double* U = x.c->tmp2 + (size_t)b * x.nn;
+        const double* W = x.c->currU + (size_t)b * x.nn;
+        for (int k = threadIdx.x & 63; k < n; k += 64) {
+            double uk[DQMC_DELAY];
+#pragma unroll
+            for (int m = 0; m < DQMC_DELAY; ++m) uk[m] = m < p ? U[(size_t)m * n + k] : 0.0;
+            for (int l = threadIdx.x >> 6; l < n; l += DQMC_NT / 64) {
+                double v = g[k + (size_t)l * n];
+#pragma unroll
+                for (int m = 0; m < DQMC_DELAY; ++m)
+                    if (m < p) v = fma(-uk[m], W[(size_t)m * n + l], v);
+                g[k + (size_t)l * n] = v;
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // sweep_spatial (local_updates.jl:23-60) with propose_local / accept_local!
 // (fields.jl:58-84, 176-209, 271-286, 340-344, 388-393, 440-449, 497-503,
 // 563-573, 627-637).  Thread 0 makes the sequential decisions with the
@@ -500,6 +528,11 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     __syncthreads();
     long long acc_count = 0;
     int i = 0, round = 0;
+    // G in global memory: delay the rank-1 updates and apply them DQMC_DELAY
+    // at a time (one pass over G instead of one per accepted move)
+    const bool delayed = !x.s->gres;
+    const int kcap = n < DQMC_DELAY ? n : DQMC_DELAY;  // U, W columns fit the n*n scratch
+    int pending = 0;
     while (true) {
         if (tid == 0) {
             int j = i;
@@ -558,17 +591,52 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
         __syncthreads();  // also: the previous round's update is complete
         const int j = x.s->sxi[2 + (round & 1)];
         ++round;
-        if (j >= n) break;
+        if (j >= n) {
+            if (pending > 0) flush_delayed(x, pending);
+            break;
+        }
         acc_count += 1;
         for (int e = tid; e < nf * n; e += DQMC_NT) {
             const int b = e / n, k = e % n;
             const double* g = c.G + (size_t)b * x.nn;
-            double ig = -g[(size_t)j * n + k];
+            double gkj = g[(size_t)j * n + k], gjk = g[(size_t)k * n + j];
+            if (delayed) {
+                // current G[k, j] and G[j, k] with the pending updates applied
+                const double* U = c.tmp2 + (size_t)b * x.nn;
+                const double* W = c.currU + (size_t)b * x.nn;
+                for (int m = 0; m < pending; ++m) {
+                    gkj = fma(-U[(size_t)m * n + k], W[(size_t)m * n + j], gkj);
+                    gjk = fma(-U[(size_t)m * n + j], W[(size_t)m * n + k], gjk);
+                }
+            }
+            double ig = -gkj;
             if (k == j) ig += 1.0;
+            const double rw = x.s->sxd[b] * gjk;
             x.s->r1.col[b][k] = ig;
-            x.s->r1.row[b][k] = x.s->sxd[b] * g[(size_t)k * n + j];
+            x.s->r1.row[b][k] = rw;
+            if (delayed) {
+                c.tmp2[(size_t)b * x.nn + (size_t)pending * n + k] = ig;
+                c.currU[(size_t)b * x.nn + (size_t)pending * n + k] = rw;
+            }
         }
         __syncthreads();
+        if (delayed) {
+            if (warp == 0) {
+                for (int e = lane; e < nf * n; e += 32) {
+                    const int b = e / n, k = e % n;
+                    diag[e] = fma(-x.s->r1.col[b][k], x.s->r1.row[b][k], diag[e]);
+                }
+                __syncwarp();
+            }
+            ++pending;
+            if (pending == kcap) {
+                __syncthreads();
+                flush_delayed(x, pending);
+                pending = 0;
+            }
+            i = j + 1;
+            continue;
+        }
         if (warp == 0) {
             for (int e = lane; e < nf * n; e += 32) {
                 const int b = e / n, k = e % n;

@@ -165,3 +165,21 @@ def test_async_sweep_and_query(pkg, lib, oracle):
         pass
     st = h.stats(0)
     assert st["proposals"] == 2 * 2 * param.slices * len(model.l)
+
+
+@pytest.mark.parametrize("lattice,L,field", [("square", 10, "DensityHirschField"),
+                                             ("honeycomb", 6, "MagneticHirschField")])
+def test_large_n_delayed_updates(pkg, lib, oracle, lattice, L, field):
+    """n > 64: G stays in global memory and the rank-1 updates are applied in
+    delayed blocks; decisions and fields still replay the oracle exactly."""
+    h, oc, model, param, fld = _pair(pkg, lib, oracle, field, L=L, lattice=lattice, beta=1.0,
+                                     safe_mult=5, seed=31)
+    assert len(model.l) > 64
+    h.init_random_field(0)
+    oc.init_random_conf()
+    h.initialize_run()
+    oc.initialize_run()
+    h.sweep(1)
+    oc.sweeps(1)
+    assert np.array_equal(h.get_field(0), oc.get_conf())
+    assert maxdiff(h.greens(0), oc.greens()) < TOL_G
