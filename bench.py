@@ -34,7 +34,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
-METRIC = "DQMC sweeps/s/GPU (plain FP64 path, batched ensemble)"
+# the headline metric; ``value`` is the plain FP64 path on the batched
+# ensemble, the mixed / batched / served figures ride along in the same line
+METRIC = "DQMC sweeps/s/GPU, batched+served vs plain FP64, at |ΔG|≤1e-6; p50/p99 latency"
 
 WORKLOADS = {
     # name: (lattice L, U (reference convention), beta, safe_mult, field, description)
@@ -151,7 +153,8 @@ def run_reference(args, pkg, rank):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * wall / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded random HS fields)",
-        "config": {"workload": desc, "chains": threads, "ensemble": "independent chains"},
+        "config": {"workload": desc, "path": "CPU restatement, FP64", "chains": threads,
+                   "ensemble": "independent chains"},
         "cpu_baseline": {"value": value, "unit": "sweeps/s", "cores": cores, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "sweeps/s", "h2d_bytes_per_step": 0,
@@ -468,7 +471,8 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (seeded random Hubbard-Stratonovich fields)",
-            "config": {"workload": desc, "chains_per_gpu": B_chains, "parallelism": f"replicas{world}",
+            "config": {"workload": desc, "path": "plain FP64 (value); mixed, batched, served below",
+                       "chains_per_gpu": B_chains, "parallelism": f"replicas{world}",
                        "l2": "working set larger than L2 (no flush needed)",
                        "chain_bytes": int(_lib.load().dqmc_chain_bytes(_lib.ChainConfig(
                            n, nf, M, param.safe_mult, fld.kind, 1, fld.alpha, 0), 0))},

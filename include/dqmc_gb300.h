@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define DQMC_GB300_ABI_VERSION 1
+#define DQMC_GB300_ABI_VERSION 3
 
 /* status codes */
 #define DQMC_OK 0
@@ -55,8 +55,9 @@ extern "C" {
 
 /* arithmetic of the wraps and slice-matrix chains */
 #define DQMC_PREC_FP64 0  /* everything FP64 (parity path) */
-#define DQMC_PREC_MIXED 1 /* wraps in FP32-split arithmetic; UDT, reconstruction,
-                             determinant ratios and rank-1 updates in FP64 */
+#define DQMC_PREC_MIXED 1 /* wraps and slice-matrix chains as double-float products
+                             on the FP32 pipe; UDT, reconstruction, determinant
+                             ratios and rank-1 updates in FP64 */
 
 typedef struct dqmc_handle dqmc_handle;
 
@@ -152,6 +153,78 @@ int dqmc_set_greens(dqmc_handle* h, int chain, const double* in);
 int dqmc_calculate_greens(dqmc_handle* h, int chain, int slice, int safe_mult, double* out);
 /* which: 0 u_stack, 1 t_stack (nf*n*n), 2 d_stack (nf*n); idx 1-based (stack.jl:13-15) */
 int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out);
+
+/* ---- equal-time measurements on the device ----------------------------------
+ * Replaces: the measurement step of run! (DQMC.jl:205-222: after every
+ * measure_rate-th sweep past thermalisation) with the equal-time kernels the
+ * reference evaluates on greens!(mc) (greens.jl:94-125): occupation
+ * (occupation.jl:44-55), double occupancy and the interaction energy
+ * (HubbardModel.jl:160-183), the z spin-density correlation
+ * (spin_density.jl:182-227, tau = 0) reduced to S^z(q) for the caller's q,
+ * and the equal-time G (constructors/greens.jl:39-40), binned as
+ * BinningAnalysis' LogBinner does (generic.jl:57-69).  The values stay on the
+ * device: no G download per measurement.  Measurements run inside dqmc_sweep,
+ * dqmc_sweep_async and dqmc_pool_run whenever a chain completes a sweep whose
+ * count (the chain's sweep counter after the sweep) is a multiple of
+ * measure_rate. */
+typedef struct {
+    int32_t enable;        /* 1: measure; 0: stop measuring (accumulators are kept) */
+    int32_t measure_rate;  /* >= 1 */
+    int32_t greens_mean;   /* 1: also accumulate the physical G */
+    int32_t reserved;
+    int64_t sweep;         /* the chain's sweep counter now (mc.last_sweep); < 0 keeps it */
+    double U;              /* the model's U (reference sign convention) */
+    const double* q_cos;   /* n_sites values cos(q . r_i), or NULL: no S^z(q) */
+    const double* q_sin;   /* n_sites values sin(q . r_i), or NULL (zeros) */
+} dqmc_measure_config;
+
+/* Scalars: 0 density per site, 1 double occupancy <n_up n_down> per site,
+ * 2 interaction energy, 3 S^z(q) = (1/n) sum_ij cos(q.(r_i - r_j)) <m_z(i) m_z(j)>.
+ * error[k]: standard error of the mean from the highest binning level with at
+ * least 32 bins (level 0 when there is none; +inf below two measurements). */
+typedef struct {
+    int64_t count;
+    double mean[4];
+    double error[4];
+    int32_t error_level[4];
+} dqmc_observables;
+
+/* chain = -1: every chain of the handle (q given: all chains need the same n_sites). */
+int dqmc_set_measurements(dqmc_handle* h, int chain, const dqmc_measure_config* cfg);
+/* Clear the accumulators (chain = -1: all). */
+int dqmc_reset_measurements(dqmc_handle* h, int chain);
+/* Means and binning errors; occupation (n_flavors*n, block-major, or NULL) and
+ * greens (n_flavors*n*n physical G, or NULL) receive the means of those. */
+int dqmc_get_measurements(dqmc_handle* h, int chain, dqmc_observables* out, double* occupation,
+                          double* greens);
+
+/* ---- global updates and replica exchange -------------------------------------
+ * Replaces: update(::GlobalFlip / ::GlobalShuffle, mc, model, field)
+ * (global_updates.jl:188-203, 244-278: propose_conf!, propose_global_from_conf,
+ * inv_det, accept_global!) for every chain of the handle in one launch.  The
+ * chains must be between sweeps (current_slice 1, direction +1, as after
+ * dqmc_initialize_run or a whole number of sweeps).  accepted (may be NULL)
+ * receives n_chains 0/1 flags.  GlobalShuffle draws its permutation from the
+ * chain's stream (Fisher-Yates, j = floor(w (i+1) / 2^64)). */
+#define DQMC_GLOBAL_FLIP 0
+#define DQMC_GLOBAL_SHUFFLE 1
+int dqmc_global_update(dqmc_handle* h, int kind, int32_t* accepted);
+/* Replaces: SimpleScheduler(LocalSweep(), GlobalFlip() or GlobalShuffle())
+ * (scheduler.jl:258-289): from now on every dqmc_sweep call's sweeps run the
+ * global update first, except the first sweep after this call.  kind = -1
+ * turns it off.  chain = -1: all chains. */
+int dqmc_set_global_schedule(dqmc_handle* h, int chain, int kind);
+/* Replaces: update(::ReplicaExchange, ...) (parallel_updates.jl:116-150)
+ * between chains of this handle (no MPI / Distributed.jl): partner[i] = j
+ * pairs chain i with chain j (partner[j] = i; -1: not exchanging).  Each chain
+ * weighs adopting its partner's configuration, the lower index's uniform
+ * decides for the pair against the product of the two weights, and accepted
+ * pairs swap configurations and rebuild their stacks.  Paired chains need the
+ * same n_sites, n_flavors, slices and field kind (their U, mu, beta/dtau
+ * hopping may differ).  accepted (may be NULL): n_chains 0/1 flags. */
+int dqmc_replica_exchange(dqmc_handle* h, const int32_t* partner, int32_t* accepted);
+/* accepted / proposed global and replica moves since creation */
+int dqmc_get_global_stats(dqmc_handle* h, int chain, int64_t* accepted, int64_t* proposals);
 
 /* ---- pools: batched and served chains -------------------------------------
  * Replaces: a set of independent simulations driven one after another

@@ -45,6 +45,20 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class MeasureConfig(C.Structure):
+    _fields_ = [("enable", C.c_int32), ("measure_rate", C.c_int32), ("greens_mean", C.c_int32),
+                ("reserved", C.c_int32), ("sweep", C.c_int64), ("U", C.c_double),
+                ("q_cos", C.POINTER(C.c_double)), ("q_sin", C.POINTER(C.c_double))]
+
+
+class Observables(C.Structure):
+    _fields_ = [("count", C.c_int64), ("mean", C.c_double * 4), ("error", C.c_double * 4),
+                ("error_level", C.c_int32 * 4)]
+
+
+# scalar observables of the device accumulators, in dqmc_observables order
+OBSERVABLES = ["density", "double_occupancy", "interaction_energy", "sz_structure_factor"]
+
 EXPORTS = [
     "dqmc_create", "dqmc_destroy", "dqmc_last_error", "dqmc_abi_version", "dqmc_chain_bytes",
     "dqmc_set_hopping", "dqmc_set_field", "dqmc_get_field", "dqmc_init_random_field",
@@ -54,7 +68,13 @@ EXPORTS = [
     "dqmc_get_stack", "dqmc_set_stream", "dqmc_get_timers", "dqmc_calculate_greens_noalloc",
     "dqmc_pool_create", "dqmc_pool_admit", "dqmc_pool_release", "dqmc_pool_set_quota",
     "dqmc_pool_run", "dqmc_pool_slot", "dqmc_pool_free_bytes",
+    "dqmc_set_measurements", "dqmc_reset_measurements", "dqmc_get_measurements",
+    "dqmc_global_update", "dqmc_set_global_schedule", "dqmc_replica_exchange",
+    "dqmc_get_global_stats",
 ]
+
+GLOBAL_FLIP = 0
+GLOBAL_SHUFFLE = 1
 
 PHASES = ["sweep_spatial", "wrap", "slice_chain", "udt", "greens", "prop_check", "t_update",
           "other"]
@@ -106,6 +126,14 @@ def load(path: str = LIB_PATH):
     L.dqmc_pool_slot.argtypes = [P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                  C.POINTER(C.c_int32)]
     L.dqmc_pool_free_bytes.argtypes = [P]
+    L.dqmc_set_measurements.argtypes = [P, C.c_int, C.POINTER(MeasureConfig)]
+    L.dqmc_reset_measurements.argtypes = [P, C.c_int]
+    L.dqmc_global_update.argtypes = [P, C.c_int, C.c_void_p]
+    L.dqmc_set_global_schedule.argtypes = [P, C.c_int, C.c_int]
+    L.dqmc_replica_exchange.argtypes = [P, C.c_void_p, C.c_void_p]
+    L.dqmc_get_global_stats.argtypes = [P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
+    L.dqmc_get_measurements.argtypes = [P, C.c_int, C.POINTER(Observables), C.c_void_p,
+                                        C.c_void_p]
     L.dqmc_pool_free_bytes.restype = C.c_int64
     _lib = L
     return L
@@ -258,6 +286,61 @@ class Handle:
         buf = self._mat_buf(chain)
         check(load().dqmc_calculate_greens(self.h, chain, int(slice_), int(safe_mult), dptr(buf)))
         return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
+
+    def set_measurements(self, chain=-1, enable=True, rate=1, greens=False, sweep=-1, U=0.0,
+                         q=None):
+        """Device-side equal-time measurements after every ``rate``-th sweep.
+        ``q`` = (cos(q.r_i), sin(q.r_i)) arrays of length n_sites for S^z(q)."""
+        qc = qs = None
+        if q is not None:
+            qc = np.ascontiguousarray(q[0], dtype=np.float64)
+            qs = np.ascontiguousarray(q[1], dtype=np.float64)
+        m = MeasureConfig(int(bool(enable)), int(rate), int(bool(greens)), 0, int(sweep),
+                          float(U),
+                          qc.ctypes.data_as(C.POINTER(C.c_double)) if qc is not None else None,
+                          qs.ctypes.data_as(C.POINTER(C.c_double)) if qs is not None else None)
+        check(load().dqmc_set_measurements(self.h, chain, C.byref(m)))
+
+    def reset_measurements(self, chain=-1):
+        check(load().dqmc_reset_measurements(self.h, chain))
+
+    def measurements(self, chain):
+        """Means and binning errors of the device accumulators."""
+        cfg = self.cfg(chain)
+        o = Observables()
+        occ = np.zeros(cfg.n_flavors * cfg.n_sites)
+        g = self._mat_buf(chain)
+        check(load().dqmc_get_measurements(self.h, chain, C.byref(o), occ.ctypes.data,
+                                           g.ctypes.data))
+        out = {"count": o.count, "occupation": occ.reshape(cfg.n_flavors, cfg.n_sites),
+               "greens": buf_to_blocks(g, cfg.n_flavors, cfg.n_sites)}
+        for k, name in enumerate(OBSERVABLES):
+            out[name] = (o.mean[k], o.error[k])
+            out[name + "_level"] = o.error_level[k]
+        return out
+
+    def global_update(self, kind=GLOBAL_FLIP):
+        """One global move of every chain; returns the accepted flags."""
+        acc = np.zeros(self.n_chains, dtype=np.int32)
+        check(load().dqmc_global_update(self.h, int(kind), acc.ctypes.data))
+        return acc.astype(bool)
+
+    def set_global_schedule(self, kind, chain=-1):
+        """A global move before every sweep but the first (kind None: off)."""
+        check(load().dqmc_set_global_schedule(self.h, int(chain), -1 if kind is None else int(kind)))
+
+    def replica_exchange(self, partners):
+        """Replica exchange between paired chains (partners[i] = j, -1: none)."""
+        p = np.ascontiguousarray(partners, dtype=np.int32)
+        assert p.size == self.n_chains
+        acc = np.zeros(self.n_chains, dtype=np.int32)
+        check(load().dqmc_replica_exchange(self.h, p.ctypes.data, acc.ctypes.data))
+        return acc.astype(bool)
+
+    def global_stats(self, chain):
+        a, p = C.c_int64(), C.c_int64()
+        check(load().dqmc_get_global_stats(self.h, chain, C.byref(a), C.byref(p)))
+        return a.value, p.value
 
     def stack(self, chain, which, idx):
         cfg = self.cfg(chain)

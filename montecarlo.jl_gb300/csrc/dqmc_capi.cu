@@ -44,7 +44,7 @@ struct Layout {
     size_t bytes;
     size_t off_conf, off_hop, off_G, off_Gtmp, off_Ul, off_Ur, off_Tl, off_Tr, off_tmp1, off_tmp2,
         off_currU, off_out, off_ustack, off_tstack, off_dstack, off_Dl, off_Dr, off_tempv,
-        off_pivot;
+        off_pivot, off_meas, off_qcs, off_tconf, off_tempvf;
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -66,6 +66,10 @@ Layout layout_of(const dqmc_chain_config& c, int prec) {
     L.off_Dr = o; o = align256(o + nf * n * sizeof(double));
     L.off_tempv = o; o = align256(o + nf * n * sizeof(double));
     L.off_pivot = o; o = align256(o + nf * n * sizeof(int));
+    L.off_meas = o; o = align256(o + DQMC_MEAS_DOUBLES(n, nf) * sizeof(double));
+    L.off_qcs = o; o = align256(o + 2 * n * sizeof(double));
+    L.off_tconf = o; o = align256(o + n * c.slices);
+    L.off_tempvf = o; o = align256(o + nf * n * sizeof(double));
     L.bytes = o;
     return L;
 }
@@ -189,6 +193,14 @@ void fill_descriptor(DqmcChain& d, const dqmc_chain_config& c, char* b, const La
     d.Dl = (double*)(b + L.off_Dl); d.Dr = (double*)(b + L.off_Dr);
     d.tempv = (double*)(b + L.off_tempv);
     d.pivot = (int*)(b + L.off_pivot);
+    d.meas = (double*)(b + L.off_meas);
+    d.qcs = nullptr;  // set with the measurement's q
+    d.meas_rate = 1;
+    d.temp_conf = (int8_t*)(b + L.off_tconf);
+    d.tempvf = (double*)(b + L.off_tempvf);
+    d.alpha_field = c.alpha;
+    d.partner = -1;
+    d.global_kind = -1;
     d.key = c.seed; d.ctr = 0;
     d.current_slice = 0; d.current_range = 1; d.direction = 1;
     d.active = 1;
@@ -434,9 +446,12 @@ static void fill_stats(const DqmcChain& d, dqmc_stats* s) {
     s->status = d.status;
 }
 
+static int check_scheduled(dqmc_handle* h);
+
 int dqmc_sweep(dqmc_handle* h, int n_sweeps, dqmc_stats* stats) {
     if (!h) return fail(DQMC_ERR_INVALID, "null handle");
     if (n_sweeps < 0) return fail(DQMC_ERR_INVALID, "dqmc_sweep: n_sweeps < 0");
+    if (int st = check_scheduled(h)) return st;
     int st = launch(h, DQMC_OP_SWEEP, n_sweeps, 0, true);
     if (st != DQMC_OK) return st;
     if (stats)
@@ -447,6 +462,7 @@ int dqmc_sweep(dqmc_handle* h, int n_sweeps, dqmc_stats* stats) {
 int dqmc_sweep_async(dqmc_handle* h, int n_sweeps) {
     if (!h) return fail(DQMC_ERR_INVALID, "null handle");
     if (n_sweeps < 0) return fail(DQMC_ERR_INVALID, "dqmc_sweep_async: n_sweeps < 0");
+    if (int st = check_scheduled(h)) return st;
     return launch(h, DQMC_OP_SWEEP, n_sweeps, 0, false);
 }
 
@@ -559,6 +575,201 @@ int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out) {
     }
     const double* base = which == 0 ? d.ustack : d.tstack;
     return download_mat(h, chain, base + (idx - 1) * ms, out);
+}
+
+/* ---- equal-time measurements ---------------------------------------------- */
+
+int dqmc_set_measurements(dqmc_handle* h, int chain, const dqmc_measure_config* cfg) {
+    if (!h || !cfg) return fail(DQMC_ERR_INVALID, "dqmc_set_measurements: null argument");
+    if (cfg->enable && cfg->measure_rate < 1)
+        return fail(DQMC_ERR_INVALID, "dqmc_set_measurements: measure_rate < 1");
+    if (!(cfg->U == cfg->U)) return fail(DQMC_ERR_INVALID, "dqmc_set_measurements: U is NaN");
+    int lo = chain, hi = chain + 1;
+    if (chain == -1) { lo = 0; hi = (int)h->cfg.size(); }
+    else if (int st = check_chain(h, chain)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    for (int i = lo; i < hi; ++i) {
+        DqmcChain& d = h->host[i];
+        if (!d.active) continue;  // free pool slot
+        if (cfg->q_cos && chain == -1 && h->cfg[i].n_sites != h->cfg[lo].n_sites)
+            return fail(DQMC_ERR_INVALID, "dqmc_set_measurements(-1): chains have different n_sites");
+        d.meas_enable = cfg->enable ? 1 : 0;
+        if (cfg->measure_rate >= 1) d.meas_rate = cfg->measure_rate;
+        d.meas_greens = cfg->greens_mean ? 1 : 0;
+        d.meas_U = cfg->U;
+        if (cfg->sweep >= 0) d.sweep = cfg->sweep;
+        if (cfg->q_cos) {
+            const size_t n = (size_t)d.n;
+            double* q = (double*)((char*)d.meas + (h->lay[i].off_qcs - h->lay[i].off_meas));
+            std::vector<double> buf(2 * n, 0.0);
+            for (size_t k = 0; k < n; ++k) {
+                buf[k] = cfg->q_cos[k];
+                if (cfg->q_sin) buf[n + k] = cfg->q_sin[k];
+            }
+            CUDA_TRY(cudaMemcpyAsync(q, buf.data(), 2 * n * sizeof(double), cudaMemcpyHostToDevice,
+                                     h->stream),
+                     "upload structure-factor phases");
+            CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+            d.qcs = q;
+        } else {
+            d.qcs = nullptr;
+        }
+    }
+    h->host_dirty = true;
+    return DQMC_OK;
+}
+
+int dqmc_reset_measurements(dqmc_handle* h, int chain) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    int lo = chain, hi = chain + 1;
+    if (chain == -1) { lo = 0; hi = (int)h->cfg.size(); }
+    else if (int st = check_chain(h, chain)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    for (int i = lo; i < hi; ++i) {
+        const DqmcChain& d = h->host[i];
+        if (!d.active) continue;
+        CUDA_TRY(cudaMemsetAsync(d.meas, 0, DQMC_MEAS_DOUBLES(d.n, d.nf) * sizeof(double), h->stream),
+                 "clear measurement accumulators");
+    }
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+int dqmc_get_measurements(dqmc_handle* h, int chain, dqmc_observables* out, double* occupation,
+                          double* greens) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!out) return fail(DQMC_ERR_INVALID, "dqmc_get_measurements: null out");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    const DqmcChain& d = h->host[chain];
+    const size_t nd = DQMC_MEAS_DOUBLES(d.n, d.nf);
+    std::vector<double> m(nd);
+    CUDA_TRY(cudaMemcpyAsync(m.data(), d.meas, nd * sizeof(double), cudaMemcpyDeviceToHost, h->stream),
+             "download measurement accumulators");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    const double cnt = m[0];
+    out->count = (int64_t)cnt;
+    for (int k = 0; k < DQMC_MEAS_SCALARS; ++k) {
+        const double* lv = m.data() + DQMC_MEAS_HEADER + (size_t)k * DQMC_MEAS_LEVELS * DQMC_MEAS_BIN_WORDS;
+        out->mean[k] = lv[0] > 0 ? lv[1] : NAN;
+        // highest level with >= 32 bins, else level 0 (LogBinner's std_error)
+        int use = -1;
+        for (int l = 0; l < DQMC_MEAS_LEVELS; ++l)
+            if (lv[l * DQMC_MEAS_BIN_WORDS] >= 32.0) use = l;
+        if (use < 0) use = 0;
+        const double nb = lv[use * DQMC_MEAS_BIN_WORDS], m2 = lv[use * DQMC_MEAS_BIN_WORDS + 2];
+        out->error[k] = nb >= 2.0 ? sqrt(m2 / (nb - 1.0) / nb) : INFINITY;
+        out->error_level[k] = use;
+    }
+    const size_t nocc = (size_t)d.nf * d.n;
+    if (occupation)
+        for (size_t e = 0; e < nocc; ++e) occupation[e] = cnt > 0 ? m[DQMC_MEAS_OCC_OFF + e] / cnt : NAN;
+    if (greens) {
+        const size_t ng = (size_t)d.nf * d.n * d.n;
+        for (size_t e = 0; e < ng; ++e)
+            greens[e] = cnt > 0 ? m[DQMC_MEAS_OCC_OFF + nocc + e] / cnt : NAN;
+    }
+    return DQMC_OK;
+}
+
+/* ---- global updates and replica exchange ----------------------------------- */
+
+static int check_between_sweeps(dqmc_handle* h) {
+    for (size_t i = 0; i < h->host.size(); ++i) {
+        const DqmcChain& d = h->host[i];
+        if (d.active && (d.current_slice != 1 || d.direction != 1))
+            return fail(DQMC_ERR_INVALID, "chain " + std::to_string(i) +
+                                              " is not between sweeps (initialize_run first; "
+                                              "global moves need current_slice 1, direction +1)");
+    }
+    return DQMC_OK;
+}
+
+// sweeps with a scheduled global update must start between sweeps
+static int check_scheduled(dqmc_handle* h) {
+    bool any = false;
+    for (const DqmcChain& d : h->host) any = any || (d.active && d.global_kind >= 0);
+    if (!any) return DQMC_OK;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    return check_between_sweeps(h);
+}
+
+int dqmc_global_update(dqmc_handle* h, int kind, int32_t* accepted) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (kind != DQMC_GLOBAL_FLIP && kind != DQMC_GLOBAL_SHUFFLE)
+        return fail(DQMC_ERR_INVALID, "dqmc_global_update: unknown kind");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    if (int st = check_between_sweeps(h)) return st;
+    std::vector<long long> before(h->host.size());
+    for (size_t i = 0; i < h->host.size(); ++i) before[i] = h->host[i].g_accepted;
+    if (int st = launch(h, DQMC_OP_GLOBAL, kind, 0, true)) return st;
+    if (accepted)
+        for (size_t i = 0; i < h->host.size(); ++i)
+            accepted[i] = h->host[i].active ? (int32_t)(h->host[i].g_accepted - before[i]) : 0;
+    return DQMC_OK;
+}
+
+int dqmc_set_global_schedule(dqmc_handle* h, int chain, int kind) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (kind != -1 && kind != DQMC_GLOBAL_FLIP && kind != DQMC_GLOBAL_SHUFFLE)
+        return fail(DQMC_ERR_INVALID, "dqmc_set_global_schedule: unknown kind");
+    int lo = chain, hi = chain + 1;
+    if (chain == -1) { lo = 0; hi = (int)h->cfg.size(); }
+    else if (int st = check_chain(h, chain)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    for (int i = lo; i < hi; ++i) {
+        if (!h->host[i].active) continue;
+        h->host[i].global_kind = kind;
+        h->host[i].sched_calls = 0;
+    }
+    h->host_dirty = true;
+    return DQMC_OK;
+}
+
+int dqmc_replica_exchange(dqmc_handle* h, const int32_t* partner, int32_t* accepted) {
+    if (!h || !partner) return fail(DQMC_ERR_INVALID, "dqmc_replica_exchange: null argument");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    const int nc = (int)h->host.size();
+    for (int i = 0; i < nc; ++i) {
+        const int j = partner[i];
+        if (j == -1) continue;
+        if (j < 0 || j >= nc || j == i || partner[j] != i)
+            return fail(DQMC_ERR_INVALID, "dqmc_replica_exchange: partners must pair chains "
+                                          "(partner[partner[i]] == i)");
+        if (!h->host[i].active || !h->host[j].active)
+            return fail(DQMC_ERR_INVALID, "dqmc_replica_exchange: partner slot holds no chain");
+        const dqmc_chain_config &a = h->cfg[i], &b = h->cfg[j];
+        if (a.n_sites != b.n_sites || a.n_flavors != b.n_flavors || a.slices != b.slices ||
+            a.field != b.field)
+            return fail(DQMC_ERR_INVALID, "dqmc_replica_exchange: paired chains need the same "
+                                          "n_sites, n_flavors, slices and field kind");
+    }
+    if (int st = check_between_sweeps(h)) return st;
+    std::vector<long long> before(nc);
+    for (int i = 0; i < nc; ++i) {
+        before[i] = h->host[i].g_accepted;
+        h->host[i].partner = h->host[i].active ? partner[i] : -1;
+    }
+    h->host_dirty = true;
+    int st = launch(h, DQMC_OP_REPLICA_WEIGHT, 0, 0, true);
+    if (st == DQMC_OK) st = launch(h, DQMC_OP_REPLICA_ACCEPT, 0, 0, true);
+    for (int i = 0; i < nc; ++i) h->host[i].partner = -1;
+    h->host_dirty = true;
+    if (st != DQMC_OK) return st;
+    if (accepted)
+        for (int i = 0; i < nc; ++i)
+            accepted[i] = partner[i] >= 0 ? (int32_t)(h->host[i].g_accepted - before[i]) : 0;
+    return DQMC_OK;
+}
+
+int dqmc_get_global_stats(dqmc_handle* h, int chain, int64_t* accepted, int64_t* proposals) {
+    if (int st = check_chain(h, chain)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    if (accepted) *accepted = h->host[chain].g_accepted;
+    if (proposals) *proposals = h->host[chain].g_proposals;
+    return DQMC_OK;
 }
 
 /* ---- pools ------------------------------------------------------------------ */

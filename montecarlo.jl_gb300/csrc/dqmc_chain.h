@@ -52,7 +52,46 @@ struct DqmcChain {
     // slice visits the chain may run, slice visits run so far
     int active, needs_build;
     long long visits_quota, visits_done;
+    // equal-time measurements on the device (measure() in dqmc_chain_ops.cuh):
+    // on/off, sweeps between measurements, accumulate the mean physical G,
+    // the chain's sweep counter (the reference's mc.last_sweep), U for the
+    // interaction energy, cos/sin(q.r_i) for S^z(q) (2n values, or NULL) and
+    // the accumulator block (layout DQMC_MEAS_*)
+    int meas_enable, meas_rate, meas_greens, pad2;
+    long long sweep;
+    double meas_U;
+    const double* qcs;
+    double* meas;
+    // global updates (global_updates.jl) and replica exchange between chains
+    // (parallel_updates.jl): temp_conf(field) (n*M), stack.tempvf (nf*n),
+    // acceptance counters, the weight and uniform of the last replica-weight
+    // step, the replica partner (-1: none), a global update scheduled before
+    // every sweep but the first (-1: none; 0 flip, 1 shuffle) and the
+    // scheduler calls made with it
+    int8_t* temp_conf;
+    double* tempvf;
+    double alpha_field;
+    long long g_accepted, g_proposals;
+    double r_weight, r_prob;
+    int partner, global_kind;
+    long long sched_calls;
 };
+
+// Measurement accumulators of one chain (doubles):
+//   [0] measurements taken, [1..3] unused
+//   log binners: scalar k, level l at DQMC_MEAS_HEADER + (k * LEVELS + l) * 5:
+//     {completed bins, Welford mean, Welford M2, pending value, pending flag}
+//     (level l bins 2^l consecutive values)
+//   occupation sums nf*n at DQMC_MEAS_OCC_OFF, then G sums nf*n*n
+// Scalars: 0 density per site, 1 double occupancy, 2 interaction energy,
+// 3 S^z(q).
+#define DQMC_MEAS_SCALARS 4
+#define DQMC_MEAS_LEVELS 32
+#define DQMC_MEAS_HEADER 4
+#define DQMC_MEAS_BIN_WORDS 5
+#define DQMC_MEAS_OCC_OFF (DQMC_MEAS_HEADER + DQMC_MEAS_SCALARS * DQMC_MEAS_LEVELS * DQMC_MEAS_BIN_WORDS)
+#define DQMC_MEAS_DOUBLES(n, nf) \
+    ((size_t)DQMC_MEAS_OCC_OFF + (size_t)(nf) * (n) + (size_t)(nf) * (n) * (n))
 
 enum { DQMC_PHASE_SWEEP_SPATIAL = 0, DQMC_PHASE_WRAP = 1, DQMC_PHASE_SLICE_CHAIN = 2,
        DQMC_PHASE_UDT = 3, DQMC_PHASE_GREENS = 4, DQMC_PHASE_PROP_CHECK = 5,
@@ -60,7 +99,9 @@ enum { DQMC_PHASE_SWEEP_SPATIAL = 0, DQMC_PHASE_WRAP = 1, DQMC_PHASE_SLICE_CHAIN
 
 enum { DQMC_OP_SWEEP = 0, DQMC_OP_BUILD = 1, DQMC_OP_GREENS_AT = 2, DQMC_OP_PHYSICAL = 3,
        DQMC_OP_BUILD_FWD = 4, DQMC_OP_PROPAGATE = 5, DQMC_OP_SWEEP_SPATIAL = 6,
-       DQMC_OP_RUN = 7 /* time-sliced: arg0 = budget in microseconds */ };
+       DQMC_OP_RUN = 7 /* time-sliced: arg0 = budget in microseconds */,
+       DQMC_OP_GLOBAL = 8 /* arg0: 0 GlobalFlip, 1 GlobalShuffle */,
+       DQMC_OP_REPLICA_WEIGHT = 9, DQMC_OP_REPLICA_ACCEPT = 10 };
 
 // DqmcChain::prec values (same numbers as DQMC_PREC_* of the C ABI)
 #define DQMC_PREC_FP64_ID 0

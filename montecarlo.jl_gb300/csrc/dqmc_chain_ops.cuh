@@ -237,8 +237,10 @@ __device__ __noinline__ void add_slice_sequence_right(const Ctx& x, int idx) {
     phase_stop(x, DQMC_PHASE_T_UPDATE, t0);
 }
 
-// calculate_greens_AVX! (stack.jl:442-496), per flavour block
-__device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout) {
+// calculate_greens_AVX! (stack.jl:442-496), per flavour block.  finish =
+// false stops after the second UDT: calculate_inv_greens_udt
+// (global_updates.jl:26-49), leaving det(G) = 1 / prod(Dr) up to phases.
+__device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout, bool finish = true) {
     DqmcChain& c = *x.c;
     const int n = x.n;
     const bool bf = x.nf > 1;
@@ -263,6 +265,7 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout) {
         for (int i = threadIdx.x; i < n; i += DQMC_NT) tr[(size_t)i * n + i] += dr[i];
         __syncthreads();
         udt_one(x, ul, dr, tr, b, false);
+        if (!finish) continue;
         rdivp(n, ur, tr, g, pv, bf, x.s->sv);
         mm<false, false>(n, tr, tl, ul, x.s->tiles);
         for (int i = threadIdx.x; i < n; i += DQMC_NT) dl[i] = 1.0 / dr[i];
@@ -661,10 +664,11 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     return acc_count;
 }
 
-// calculate_greens(mc, slice, output, field, safe_mult) (stack.jl:525-583)
-__device__ __noinline__ void calculate_greens_at(const Ctx& x, int slice, int safe_mult, double* out) {
+// the UDT chains of calculate_greens(mc, slice, ...) (stack.jl:525-583) and
+// of inv_det (global_updates.jl:65-133): Ur,Dr,Tr = B(slice+1)'...B(M)' and
+// Ul,Dl,Tl = B(slice)...B(1), stabilised every safe_mult slices
+__device__ __noinline__ void udt_chains_from_scratch(const Ctx& x, int slice, int safe_mult) {
     DqmcChain& c = *x.c;
-    if (safe_mult <= 0) safe_mult = c.k;
     const int sz = x.nf * (int)x.nn;
     mat_ident(x, c.currU);
     mat_ident(x, c.Ur);
@@ -710,7 +714,158 @@ __device__ __noinline__ void calculate_greens_at(const Ctx& x, int slice, int sa
         __syncthreads();
         mm_blocks(x, c.Tl, c.tmp1, c.tmp2);
     }
+}
+
+// calculate_greens(mc, slice, output, field, safe_mult) (stack.jl:525-583)
+__device__ __noinline__ void calculate_greens_at(const Ctx& x, int slice, int safe_mult, double* out) {
+    if (safe_mult <= 0) safe_mult = x.c->k;
+    udt_chains_from_scratch(x, slice, safe_mult);
     calculate_greens(x, out);
+}
+
+// ---- global updates ---------------------------------------------------------
+
+// sum of a configuration's entries (exact), all threads get it
+__device__ long long conf_sum(const Ctx& x, const int8_t* conf) {
+    const int cnt = x.n * x.c->M;
+    long long v = 0;
+    for (int e = threadIdx.x; e < cnt; e += DQMC_NT) v += conf[e];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    long long* red = reinterpret_cast<long long*>(x.s->red);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    long long t = 0;
+    for (int w = 0; w < DQMC_NW; ++w) t += red[w];
+    __syncthreads();
+    return t;
+}
+
+// propose_global_from_conf (global_updates.jl:137-166) for the proposal
+// `prop` replacing `old`, at current_slice 1: tempvf = Dl of the current G,
+// inv_det(current_slice - 1) with the proposal (G_tmp as scratch, so G is
+// untouched), detratio = prod tempvf_i Dr_i (squared for one flavour block),
+// Delta E_boson = E(prop) - E(old) (fields.jl:395, 451, 544, 614).  Returns
+// p = exp(-Delta E) detratio to thread 0 (sxd[1]).
+__device__ __noinline__ void global_weight(const Ctx& x, const int8_t* prop, const int8_t* old) {
+    DqmcChain& c = *x.c;
+    const int cnt = x.nf * x.n;
+    copy(cnt, c.tempvf, c.Dl);
+    __syncthreads();
+    int8_t* own = c.conf;
+    if (threadIdx.x == 0) c.conf = const_cast<int8_t*>(prop);  // the slice matrices read c.conf
+    __syncthreads();
+    udt_chains_from_scratch(x, c.current_slice - 1, c.k);
+    calculate_greens(x, c.Gtmp, false);
+    __syncthreads();
+    if (threadIdx.x == 0) c.conf = own;
+    const bool dens = (c.kind == 0 || c.kind == 2);
+    const long long s_new = dens ? conf_sum(x, prop) : 0;
+    const long long s_old = dens ? conf_sum(x, old) : 0;
+    if (threadIdx.x == 0) {
+        double detratio = 1.0;
+        for (int i = 0; i < cnt; ++i) detratio = __dmul_rn(detratio, __dmul_rn(c.tempvf[i], c.Dr[i]));
+        const double dE = dens ? __dsub_rn(__dmul_rn(c.alpha_field, (double)s_new),
+                                           __dmul_rn(c.alpha_field, (double)s_old))
+                               : 0.0;
+        if (x.nf == 1) detratio = __dmul_rn(detratio, detratio);
+        x.s->sxd[1] = __dmul_rn(exp(-dE), detratio);
+    }
+    __syncthreads();
+}
+
+// global_update (global_updates.jl:188-203) after propose_conf! of
+// GlobalFlip (kind 0, :244-256: s -> -s, GHQ x -> 5 - x) or GlobalShuffle
+// (kind 1, :270-278: Fisher-Yates over the whole configuration with
+// j = floor(w (i+1) / 2^64) from the chain's stream, i = nM-1 ... 1);
+// accepted: accept_global! (:169-185: full rebuild), rejected: the old
+// configuration back.  G must be in global memory.
+__device__ __noinline__ void global_update(const Ctx& x, int kind) {
+    DqmcChain& c = *x.c;
+    const int cnt = x.n * c.M;
+    const bool ghq = c.kind >= 2;
+    for (int e = threadIdx.x; e < cnt; e += DQMC_NT) c.temp_conf[e] = c.conf[e];
+    __syncthreads();
+    if (kind == 0) {
+        for (int e = threadIdx.x; e < cnt; e += DQMC_NT)
+            c.conf[e] = ghq ? (int8_t)(5 - c.temp_conf[e]) : (int8_t)(-c.temp_conf[e]);
+    } else if (threadIdx.x == 0) {
+        for (int i = cnt - 1; i >= 1; --i) {
+            const uint64_t w = dqmc_philox_word(c.key, c.ctr);
+            c.ctr += 1;
+            const int j = (int)__umul64hi(w, (unsigned long long)(i + 1));
+            const int8_t t = c.conf[i];
+            c.conf[i] = c.conf[j];
+            c.conf[j] = t;
+        }
+    }
+    __syncthreads();
+    global_weight(x, c.conf, c.temp_conf);
+    if (threadIdx.x == 0) {
+        const double p = fabs(x.s->sxd[1]);
+        int acc = 1;
+        if (!(p > 1.0)) {
+            const uint64_t w = dqmc_philox_word(c.key, c.ctr);
+            c.ctr += 1;
+            acc = dqmc_word_to_uniform(w) < p;
+        }
+        c.g_proposals += 1;
+        c.g_accepted += acc;
+        x.s->sxi[0] = acc;
+    }
+    __syncthreads();
+    if (x.s->sxi[0]) {
+        reverse_build_stack(x);
+        propagate(x);
+    } else {
+        for (int e = threadIdx.x; e < cnt; e += DQMC_NT) c.conf[e] = c.temp_conf[e];
+        __syncthreads();
+    }
+}
+
+// ReplicaExchange (parallel_updates.jl:116-150) between chains of one launch,
+// step 1: the weight exp(-Delta E) detratio of adopting the partner's
+// configuration (copied into temp_conf: the partner's own buffer is only read)
+// and one uniform draw.  Nothing of the chain's configuration or G changes.
+__device__ __noinline__ void replica_weight(const Ctx& x, const DqmcChain* all) {
+    DqmcChain& c = *x.c;
+    const int cnt = x.n * c.M;
+    const int8_t* pc = all[c.partner].conf;
+    for (int e = threadIdx.x; e < cnt; e += DQMC_NT) c.temp_conf[e] = pc[e];
+    __syncthreads();
+    global_weight(x, c.temp_conf, c.conf);
+    if (threadIdx.x == 0) {
+        c.r_weight = x.s->sxd[1];
+        const uint64_t w = dqmc_philox_word(c.key, c.ctr);
+        c.ctr += 1;
+        c.r_prob = dqmc_word_to_uniform(w);
+    }
+    __syncthreads();
+}
+
+// step 2 (a later launch, so both weights are final): w = w_self w_partner,
+// the lower chain index's uniform decides for both; accepted chains take the
+// partner's configuration (from temp_conf) and rebuild.
+__device__ __noinline__ void replica_accept(const Ctx& x, const DqmcChain* all, int self) {
+    DqmcChain& c = *x.c;
+    const DqmcChain& q = all[c.partner];
+    if (threadIdx.x == 0) {
+        const double w = __dmul_rn(c.r_weight, q.r_weight);
+        const double u = self < c.partner ? c.r_prob : q.r_prob;
+        const int acc = u < w;
+        c.g_proposals += 1;
+        c.g_accepted += acc;
+        x.s->sxi[0] = acc;
+    }
+    __syncthreads();
+    if (x.s->sxi[0]) {
+        const int cnt = x.n * c.M;
+        for (int e = threadIdx.x; e < cnt; e += DQMC_NT) c.conf[e] = c.temp_conf[e];
+        __syncthreads();
+        reverse_build_stack(x);
+        propagate(x);
+    }
 }
 
 // _greens! (greens.jl:114-125): out = eThalfplus * (G * eThalfminus)
@@ -722,6 +877,110 @@ __device__ __noinline__ void greens_physical(const Ctx& x, const double* src, do
         mm<true, false>(x.n, blk(out, x, b), c.eThinv, blk(c.tmp1, x, b), x.s->tiles);
         __syncthreads();
     }
+}
+
+// One value into the log binner of scalar k: level l keeps the Welford mean
+// and M2 of the completed bins of 2^l consecutive values (the binning levels
+// of BinningAnalysis' LogBinner); a completed pair moves up as its mean.
+// Thread 0 only.
+__device__ void binner_push(double* m, int k, double v) {
+    for (int l = 0; l < DQMC_MEAS_LEVELS; ++l) {
+        double* b = m + DQMC_MEAS_HEADER + (k * DQMC_MEAS_LEVELS + l) * DQMC_MEAS_BIN_WORDS;
+        const double cnt = b[0] + 1.0;
+        const double d = v - b[1];
+        b[0] = cnt;
+        b[1] += d / cnt;
+        b[2] += d * (v - b[1]);
+        if (b[4] == 0.0) {
+            b[3] = v;
+            b[4] = 1.0;
+            return;
+        }
+        v = 0.5 * (b[3] + v);
+        b[4] = 0.0;
+    }
+}
+
+// Equal-time measurements of the current G (the reference measures after a
+// sweep, DQMC.jl:205-222), all on the device: the physical G (greens!,
+// greens.jl:94-125), then per site i with d_b = G^b_ii (one block: d_2 = d_1)
+//   density            (1/n) sum_i (1 - d_1) + (1 - d_2)          (occupation.jl:44-55)
+//   double occupancy   (1/n) sum_i (1 - d_1)(1 - d_2)
+//   interaction energy -U sum_i (d_1 - 1/2)(d_2 - 1/2)            (HubbardModel.jl:160-183)
+//   S^z(q)             (1/n) sum_ij cos(q.(r_i - r_j)) <m_z(i) m_z(j)> with the
+//                      equal-time Wick form of full_sdc_z_kernel (spin_density.jl:182-227):
+//                      m_i m_j + (2/nf) sum_b (delta_ij - G^b_ji) G^b_ij, m_i = d_2 - d_1
+// pushed into the chain's log binners, plus running sums of the occupations
+// 1 - d_b and (optionally) of the physical G.
+__device__ __noinline__ void measure(const Ctx& x) {
+    DqmcChain& c = *x.c;
+    const int n = x.n, nf = x.nf;
+    const size_t nn = x.nn;
+    greens_physical(x, c.G, c.out);
+    const double* g1 = c.out;
+    const double* g2 = c.out + (size_t)(nf - 1) * nn;
+    double* occ = c.meas + DQMC_MEAS_OCC_OFF;
+    const double* qc = c.qcs;
+    const double* qs = c.qcs ? c.qcs + n : nullptr;
+    double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < n; i += DQMC_NT) {
+        const double d1 = g1[(size_t)i * n + i], d2 = g2[(size_t)i * n + i];
+        acc[0] += (1.0 - d1) + (1.0 - d2);
+        acc[1] += (1.0 - d1) * (1.0 - d2);
+        acc[2] += (d1 - 0.5) * (d2 - 0.5);
+        if (qc) {
+            const double m = d2 - d1;
+            acc[3] += qc[i] * m;
+            acc[4] += qs[i] * m;
+        }
+        occ[i] += 1.0 - d1;
+        if (nf > 1) occ[n + i] += 1.0 - d2;
+    }
+    if (qc) {
+        for (int b = 0; b < nf; ++b) {
+            const double* g = c.out + (size_t)b * nn;
+            for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
+                const int i = e % n, j = e / n;
+                const double w = qc[i] * qc[j] + qs[i] * qs[j];
+                acc[5] += w * ((i == j ? 1.0 : 0.0) - g[(size_t)i * n + j]) * g[e];
+            }
+        }
+    }
+    if (c.meas_greens) {
+        double* gs = occ + (size_t)nf * n;
+        for (int e = threadIdx.x; e < nf * (int)nn; e += DQMC_NT) gs[e] += c.out[e];
+    }
+    // block reduction of the six partial sums through the staging tiles
+    double* red = x.s->tiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+        const double v = warp_sum(acc[q]);
+        if (lane == 0) red[q * DQMC_NW + warp] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t[6];
+        for (int q = 0; q < 6; ++q) {
+            t[q] = 0.0;
+            for (int w = 0; w < DQMC_NW; ++w) t[q] += red[q * DQMC_NW + w];
+        }
+        const double inv_n = 1.0 / n;
+        binner_push(c.meas, 0, t[0] * inv_n);
+        binner_push(c.meas, 1, t[1] * inv_n);
+        binner_push(c.meas, 2, -c.meas_U * t[2]);
+        binner_push(c.meas, 3, qc ? (t[3] * t[3] + t[4] * t[4] + (2.0 / nf) * t[5]) * inv_n : 0.0);
+        c.meas[0] += 1.0;
+    }
+    __syncthreads();
+}
+
+// end of a sweep: count it and measure at the measurement points
+__device__ void after_sweep(const Ctx& x) {
+    if (threadIdx.x == 0) x.c->sweep += 1;
+    __syncthreads();
+    if (x.c->meas_enable && x.c->meas && x.c->meas_rate > 0 && x.c->sweep % x.c->meas_rate == 0)
+        measure(x);
 }
 
 }  // namespace

@@ -68,6 +68,7 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
                 s->sxi[1] = (global_ns() - t_start) >= budget;
             }
             __syncthreads();
+            if (s->c.visits_done % (2 * s->c.M) == 0) after_sweep(x);
             if (s->sxi[1]) break;
         }
         if (in_arena) g_to_global(x);
@@ -77,12 +78,24 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
         const bool res = g_resident_possible(x);
         if (res) g_to_arena(x);
         for (int sw = 0; sw < arg0; ++sw) {
+            // SimpleScheduler(LocalSweep(), <global update>) (scheduler.jl:281-289):
+            // every call after the first starts with the global update
+            if (s->c.global_kind >= 0) {
+                if (s->c.sched_calls > 0) {
+                    if (res) g_to_global(x);
+                    global_update(x, s->c.global_kind);
+                    if (res) g_to_arena(x);
+                }
+                if (threadIdx.x == 0) s->c.sched_calls += 1;
+                __syncthreads();
+            }
             for (int t = 0; t < 2 * s->c.M; ++t) {
                 long long t0 = phase_start();
                 sweep_spatial(x);
                 phase_stop(x, DQMC_PHASE_SWEEP_SPATIAL, t0);
                 propagate(x);
             }
+            after_sweep(x);
         }
         if (res) g_to_global(x);
         break;
@@ -106,6 +119,15 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
     case DQMC_OP_SWEEP_SPATIAL:
         sweep_spatial(x);
         break;
+    case DQMC_OP_GLOBAL:
+        global_update(x, arg0);
+        break;
+    case DQMC_OP_REPLICA_WEIGHT:
+        if (s->c.partner >= 0) replica_weight(x, chains);
+        break;
+    case DQMC_OP_REPLICA_ACCEPT:
+        if (s->c.partner >= 0) replica_accept(x, chains, (int)blockIdx.x);
+        break;
     default:
         break;
     }
@@ -127,6 +149,14 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
         g.needs_build = s->c.needs_build;
         g.visits_quota = s->c.visits_quota;
         g.visits_done = s->c.visits_done;
+        g.sweep = s->c.sweep;
+        g.g_accepted = s->c.g_accepted;
+        g.g_proposals = s->c.g_proposals;
+        g.sched_calls = s->c.sched_calls;
+        if (op == DQMC_OP_REPLICA_WEIGHT) {  // read by the partner in the next launch only
+            g.r_weight = s->c.r_weight;
+            g.r_prob = s->c.r_prob;
+        }
         if (s->c.status) g.status = s->c.status;
     }
 }

@@ -5,7 +5,11 @@ keyword parameters, random field initialisation from the seed, the stack
 build of ``initialize_run`` and the sweep loop of ``run!`` with measurements
 every ``measure_rate`` sweeps after thermalisation.  The sweeps, wraps,
 stabilisations and Green's functions run in libdqmc_gb300.so; measurements
-are evaluated on the downloaded physical Green's function.
+are evaluated on the device after every ``measure_rate``-th sweep past
+thermalisation (density, double occupancy, interaction energy, S^z(q),
+occupations and the mean physical G, log-binned on the device; see
+``observables``), and user measurement kernels additionally on the
+downloaded physical Green's function.
 """
 from __future__ import annotations
 
@@ -32,13 +36,16 @@ class DQMC:
     """``DQMC(model; seed, field, measurements, thermalization, sweeps,
     measure_rate, beta, delta_tau | slices, safe_mult, ...)``.
 
-    Extra keywords of this implementation: ``precision`` ("fp64" or "mixed")
-    and ``device``.
+    Extra keywords of this implementation: ``precision`` ("fp64" or "mixed"),
+    ``device``, ``device_measurements`` (default True: the on-device
+    equal-time observables) and ``structure_factor_q`` (the q of S^z(q),
+    default (pi, pi, ...)).
     """
 
     def __init__(self, model, *, seed: int = -1, field=None, measurements=None,
                  thermalization_measurements=None, last_sweep: int = 0, measure_rate: int = 10,
-                 precision: str = "fp64", device: int = 0, **kwargs):
+                 precision: str = "fp64", device: int = 0, device_measurements: bool = True,
+                 structure_factor_q=None, **kwargs):
         self.model = model
         self.parameters = DQMCParameters.make(measure_rate=measure_rate, **kwargs)
         fcls = field if field is not None else model.choose_field()
@@ -64,6 +71,13 @@ class DQMC:
         self.initialized = False
         self.analysis = {}
         self.max_sweeps_per_launch = 50
+        self.device_measurements = device_measurements
+        pos = model.l.positions()
+        q = np.full(pos.shape[1], np.pi) if structure_factor_q is None else \
+            np.asarray(structure_factor_q, dtype=float)
+        ph = pos @ q
+        self._q_phases = (np.cos(ph), np.sin(ph))
+        self._dev_meas_on = None
 
     # -- stack --------------------------------------------------------------
     def init(self):
@@ -113,6 +127,8 @@ class DQMC:
             else:
                 k = total - self.last_sweep
             k = max(1, min(k, total - self.last_sweep, self.max_sweeps_per_launch))
+            if self.device_measurements:
+                self._device_measure(self.last_sweep >= th)
             self.handle.sweep(k)
             self.last_sweep += k
             if self.last_sweep > th and self.last_sweep % p.measure_rate == 0:
@@ -133,6 +149,23 @@ class DQMC:
             print(f"DQMC run: {total} sweeps, acceptance {self.analysis['acceptance']:.3f}, "
                   f"max propagation error {self.analysis['max_propagation_error']:.2e}")
         return ExitCode.SUCCESS
+
+    def _device_measure(self, on):
+        """Switch the device accumulators on (past thermalisation) or off; the
+        device counts sweeps from ``last_sweep`` and measures at every
+        multiple of ``measure_rate`` while on."""
+        if self._dev_meas_on is on:
+            return
+        self.handle.set_measurements(0, enable=on, rate=self.parameters.measure_rate,
+                                     greens=True, sweep=self.last_sweep, U=self.model.U,
+                                     q=self._q_phases)
+        self._dev_meas_on = on
+
+    def observables(self):
+        """The on-device equal-time measurements: ``(mean, error)`` of the
+        density, double occupancy, interaction energy and S^z(q), the mean
+        occupations and physical G, and the number of measurements."""
+        return self.handle.measurements(0)
 
     def _measure(self):
         G = self.greens(physical=True)

@@ -70,6 +70,9 @@ struct OcChain {
     int current_slice, current_range, direction;
     double prop_err_all, prop_err_reported;
     long n_prop_err, n_neg_p, accepted;
+    int8_t* temp_conf;            /* temp_conf(field): the configuration before a global move */
+    double* tempvf;               /* stack.tempvf: Dl of the current G during a global move */
+    long g_accepted, g_proposals;
 };
 
 int oc_generate_chunks(int length, int max_chunk, int* first, int* last) {
@@ -279,10 +282,12 @@ void oc_rdivp(int n, double* A, const double* T, double* O, const int64_t* pivot
     }
 }
 
-/* calculate_greens_AVX!, stack.jl:442-496; all operations act per flavour block */
-static void calc_greens_blocks(int n, int nf, double* Ul, double* Dl, double* Tl, double* Ur,
-                               double* Dr, double* Tr, double* G, int64_t* pivot, double* temp,
-                               double* scratch) {
+/* calculate_greens_AVX!, stack.jl:442-496; all operations act per flavour block.
+ * finish = 0 stops after the second UDT: calculate_inv_greens_udt
+ * (global_updates.jl:26-49), which leaves det(G) = 1/prod(Dr) up to phases. */
+static void calc_greens_blocks_part(int n, int nf, double* Ul, double* Dl, double* Tl, double* Ur,
+                                    double* Dr, double* Tr, double* G, int64_t* pivot, double* temp,
+                                    double* scratch, int finish) {
     size_t nn = (size_t)n * n;
     for (int b = 0; b < nf; ++b) {
         double *ul = Ul + b * nn, *tl = Tl + b * nn, *ur = Ur + b * nn, *tr = Tr + b * nn,
@@ -299,12 +304,19 @@ static void calc_greens_blocks(int n, int nf, double* Ul, double* Dl, double* Tl
         gemm_tn(n, tr, tl, ur, scratch);         /* Tr = Tl' * Ur         */
         for (int i = 0; i < n; ++i) tr[(size_t)i * n + i] += dr[i]; /* rvadd! */
         oc_udt_pivot(n, ul, dr, tr, pv, tv, 0);  /* Ul, Dr, Tr = udt(Tr)  */
+        if (!finish) continue;
         oc_rdivp(n, ur, tr, g, pv, nf > 1);      /* Ur = Ur * Tr^-1       */
         gemm_nn(n, tr, tl, ul);                  /* Tr = Tl * Ul          */
         for (int i = 0; i < n; ++i) dl[i] = 1.0 / dr[i]; /* vinv!        */
         diag_right(n, ul, ur, dl);               /* Ul = Ur * Dl          */
         gemm_nt(n, g, ul, tr, scratch);          /* G = Ul * Tr'          */
     }
+}
+
+static void calc_greens_blocks(int n, int nf, double* Ul, double* Dl, double* Tl, double* Ur,
+                               double* Dr, double* Tr, double* G, int64_t* pivot, double* temp,
+                               double* scratch) {
+    calc_greens_blocks_part(n, nf, Ul, Dl, Tl, Ur, Dr, Tr, G, pivot, temp, scratch, 1);
 }
 
 void oc_calculate_greens_avx(int n, int nf, double* Ul, double* Dl, double* Tl, double* Ur,
@@ -341,6 +353,8 @@ OcChain* oc_create(int n, int nf, int M, int safe_mult, int kind, double alpha,
     memcpy(c->eTh, eTh, nn * sizeof(double));
     memcpy(c->eThinv, eThinv, nn * sizeof(double));
     c->conf = (int8_t*)calloc((size_t)n * M, 1);
+    c->temp_conf = (int8_t*)calloc((size_t)n * M, 1);
+    c->tempvf = dalloc((size_t)nf * n);
     c->key = seed; c->ctr = 0;
     size_t ms = (size_t)nf * nn;
     c->u_stack = dalloc(ms * (c->nr + 1));
@@ -367,6 +381,7 @@ void oc_destroy(OcChain* c) {
     if (!c) return;
     free(c->rfirst); free(c->rlast);
     free(c->eT2); free(c->eT2inv); free(c->eTh); free(c->eThinv); free(c->conf);
+    free(c->temp_conf); free(c->tempvf);
     free(c->u_stack); free(c->t_stack); free(c->d_stack);
     free(c->Ul); free(c->Ur); free(c->Tl); free(c->Tr); free(c->Dl); free(c->Dr);
     free(c->greens); free(c->greens_temp); free(c->tmp1); free(c->tmp2); free(c->curr_U);
@@ -730,9 +745,10 @@ long oc_local_sweeps(OcChain* c, int nsweeps) {
     return acc;
 }
 
-/* calculate_greens(mc, slice, output, field, safe_mult), stack.jl:525-583 */
-void oc_calculate_greens_at(OcChain* c, int slice, double* out, int safe_mult) {
-    if (safe_mult <= 0) safe_mult = c->k;
+/* the UDT chains of calculate_greens(mc, slice, ...) (stack.jl:525-583) and of
+ * inv_det (global_updates.jl:65-133): Ur,Dr,Tr = B(slice+1)'...B(M)' and
+ * Ul,Dl,Tl = B(slice)...B(1), stabilised every safe_mult slices */
+static void udt_chains_from_scratch(OcChain* c, int slice, int safe_mult) {
     mat_identity(c, c->curr_U); mat_identity(c, c->Ur); vec_ones(c, c->Dr); mat_identity(c, c->Tr);
     if (slice + 1 <= c->M) {
         for (int k = c->M; k >= slice + 1; --k) {
@@ -765,7 +781,167 @@ void oc_calculate_greens_at(OcChain* c, int slice, double* out, int safe_mult) {
         mat_copy(c, c->tmp2, c->Tl);
         gemm_blocks(c, c->Tl, c->tmp1, c->tmp2);
     }
+}
+
+/* calculate_greens(mc, slice, output, field, safe_mult), stack.jl:525-583 */
+void oc_calculate_greens_at(OcChain* c, int slice, double* out, int safe_mult) {
+    if (safe_mult <= 0) safe_mult = c->k;
+    udt_chains_from_scratch(c, slice, safe_mult);
     calculate_greens(c, out);
+}
+
+/* ------------------------------------------------------------ global updates */
+
+/* inv_det, global_updates.jl:65-133: the stack of the current configuration
+ * from scratch, then calculate_inv_greens_udt into greens_temp; returns Dr
+ * (det(G) = 1 / prod(Dr), phases ignored as the reference does) */
+static const double* inv_det(OcChain* c, int slice) {
+    udt_chains_from_scratch(c, slice, c->k);
+    calc_greens_blocks_part(c->n, c->nf, c->Ul, c->Dl, c->Tl, c->Ur, c->Dr, c->Tr, c->greens_temp,
+                            c->pivot, c->tempv, c->scratch, 0);
+    return c->Dr;
+}
+
+/* energy_boson, fields.jl:395, 451, 544, 614 */
+static double energy_boson(const OcChain* c, const int8_t* conf) {
+    if (c->kind == OC_MAGNETIC_HIRSCH || c->kind == OC_MAGNETIC_GHQ) return 0.0;
+    long sum = 0;
+    for (size_t i = 0; i < (size_t)c->n * c->M; ++i) sum += conf[i];
+    return c->alpha * (double)sum;
+}
+
+/* propose_global_from_conf, global_updates.jl:137-166, with conf = the
+ * proposal and old = the configuration it replaces: det ratio and
+ * Delta E_boson = E(conf) - E(old) */
+static double propose_global(OcChain* c, const int8_t* old, double* dEb) {
+    const int cnt = c->nf * c->n;
+    memcpy(c->tempvf, c->Dl, (size_t)cnt * sizeof(double));
+    const double* Dr = inv_det(c, c->current_slice - 1);
+    double detratio = 1.0;
+    for (int i = 0; i < cnt; ++i) detratio *= c->tempvf[i] * Dr[i];
+    *dEb = energy_boson(c, c->conf) - energy_boson(c, old);
+    if (c->nf == 1) detratio = detratio * detratio;
+    return detratio;
+}
+
+/* accept_global!, global_updates.jl:169-185: full rebuild */
+static void accept_global(OcChain* c) {
+    oc_reverse_build_stack(c);
+    oc_propagate(c);
+}
+
+double oc_global_detratio(OcChain* c, const int8_t* proposal, double* dEb) {
+    const size_t cnt = (size_t)c->n * c->M;
+    memcpy(c->temp_conf, c->conf, cnt);
+    memcpy(c->conf, proposal, cnt);
+    double r = propose_global(c, c->temp_conf, dEb);
+    memcpy(c->conf, c->temp_conf, cnt);
+    return r;
+}
+
+/* global_update (global_updates.jl:188-203) after propose_conf! of
+ * GlobalFlip (:244-256: s -> -s, GHQ x -> 5 - x) or GlobalShuffle
+ * (:270-278: a Fisher-Yates shuffle of the whole configuration drawing
+ * j = floor(w (i+1) / 2^64) from the chain's stream for i = nM-1 ... 1) */
+int oc_global_update(OcChain* c, int kind) {
+    const size_t cnt = (size_t)c->n * c->M;
+    const int ghq = (c->kind == OC_DENSITY_GHQ || c->kind == OC_MAGNETIC_GHQ);
+    memcpy(c->temp_conf, c->conf, cnt);
+    if (kind == 0) {
+        for (size_t i = 0; i < cnt; ++i) c->conf[i] = ghq ? (int8_t)(5 - c->conf[i]) : (int8_t)(-c->conf[i]);
+    } else {
+        for (size_t i = cnt - 1; i >= 1; --i) {
+            uint64_t w = next_word(c);
+            size_t j = (size_t)(((unsigned __int128)w * (unsigned __int128)(i + 1)) >> 64);
+            int8_t t = c->conf[i]; c->conf[i] = c->conf[j]; c->conf[j] = t;
+        }
+    }
+    double dEb;
+    double detratio = propose_global(c, c->temp_conf, &dEb);
+    double p = fabs(exp(-dEb) * detratio);
+    int acc = (p > 1.0) ? 1 : (oc_word_to_uniform(next_word(c)) < p);
+    c->g_proposals++;
+    if (acc) {
+        accept_global(c);
+        c->g_accepted++;
+    } else {
+        memcpy(c->conf, c->temp_conf, cnt);
+    }
+    return acc;
+}
+
+/* the local half of ReplicaExchange (parallel_updates.jl:116-150): the
+ * weight exp(-Delta E) * detratio of adopting the partner's configuration and
+ * one uniform draw; the configuration is left unchanged */
+void oc_replica_weight(OcChain* c, const int8_t* partner_conf, double* weight, double* prob) {
+    double dEb;
+    double detratio = oc_global_detratio(c, partner_conf, &dEb);
+    *weight = exp(-dEb) * detratio;
+    *prob = oc_word_to_uniform(next_word(c));
+}
+
+/* accept_global! with the partner's configuration */
+void oc_replica_accept(OcChain* c, const int8_t* partner_conf) {
+    memcpy(c->conf, partner_conf, (size_t)c->n * c->M);
+    accept_global(c);
+    c->g_accepted++;
+}
+
+/* a local move of site i (0-based) at the current slice to field value
+ * x_new (the reference's propose_local + accept_local!, fields.jl:340-344,
+ * 388-393, 440-449, 497-503, 563-573, 627-637); returns p = exp(-dE) detratio */
+double oc_local_move_to(OcChain* c, int i, int x_new) {
+    int n = c->n;
+    size_t nn = NN(c);
+    int8_t* s = c->conf + (size_t)(c->current_slice - 1) * n;
+    double delta[2] = {0.0, 0.0}, R[2] = {1.0, 1.0}, detratio, dEb, p;
+    double* g0 = c->greens;
+    double* g1 = c->greens + nn;
+    int x_old = s[i];
+    switch (c->kind) {
+    case OC_DENSITY_HIRSCH:
+        dEb = -2.0 * c->alpha * (double)s[i];
+        delta[0] = exp(dEb) - 1.0;
+        R[0] = 1.0 + delta[0] * (1.0 - g0[(size_t)i * n + i]);
+        detratio = R[0] * R[0];
+        p = exp(-dEb) * detratio;
+        break;
+    case OC_MAGNETIC_HIRSCH:
+        dEb = -2.0 * c->alpha * (double)s[i];
+        delta[0] = exp(+dEb) - 1.0;
+        delta[1] = exp(-dEb) - 1.0;
+        R[0] = 1.0 + delta[0] * (1.0 - g0[(size_t)i * n + i]);
+        R[1] = 1.0 + delta[1] * (1.0 - g1[(size_t)i * n + i]);
+        detratio = R[0] * R[1];
+        p = detratio;
+        break;
+    case OC_DENSITY_GHQ:
+        dEb = c->alpha * (c->eta[x_new - 1] - c->eta[x_old - 1]);
+        delta[0] = exp(dEb) - 1.0;
+        R[0] = 1.0 + delta[0] * (1.0 - g0[(size_t)i * n + i]);
+        detratio = R[0] * R[0] * c->gam[x_new - 1] / c->gam[x_old - 1];
+        p = exp(-dEb) * detratio;
+        break;
+    default: {
+        double er = exp(c->alpha * (c->eta[x_new - 1] - c->eta[x_old - 1]));
+        delta[0] = er - 1.0;
+        delta[1] = 1.0 / er - 1.0;
+        R[0] = 1.0 + delta[0] * (1.0 - g0[(size_t)i * n + i]);
+        R[1] = 1.0 + delta[1] * (1.0 - g1[(size_t)i * n + i]);
+        detratio = R[0] * R[1] * c->gam[x_new - 1] / c->gam[x_old - 1];
+        p = detratio;
+        break;
+    }
+    }
+    for (int b = 0; b < c->nf; ++b)
+        update_block(n, c->greens + b * nn, R[b], delta[b], i, c->tempv, c->scratch);
+    s[i] = (int8_t)x_new;
+    return p;
+}
+
+void oc_get_global_stats(const OcChain* c, long* accepted, long* proposals) {
+    *accepted = c->g_accepted;
+    *proposals = c->g_proposals;
 }
 
 /* _greens!, greens.jl:114-125: eThalfplus * (G * eThalfminus) */

@@ -78,6 +78,22 @@ void oc_get_stack(const OcChain* c, int which, int idx, double* out);
  *            max reported (>1e-7), negative-p count, accepted total] */
 void oc_get_analysis(const OcChain* c, double* out5);
 
+/* global updates (global_updates.jl), at current_slice 1, direction +1:
+ * kind 0 GlobalFlip, 1 GlobalShuffle; returns 1 when accepted */
+int oc_global_update(OcChain* c, int kind);
+/* propose_global_from_conf for `proposal` (n*M): det ratio, Delta E_boson;
+ * the chain's configuration is left unchanged (G, stacks are not) */
+double oc_global_detratio(OcChain* c, const int8_t* proposal, double* dEb);
+/* ReplicaExchange's local half (parallel_updates.jl:116-150): weight of
+ * adopting partner_conf and one uniform draw */
+void oc_replica_weight(OcChain* c, const int8_t* partner_conf, double* weight, double* prob);
+/* accept_global! with partner_conf */
+void oc_replica_accept(OcChain* c, const int8_t* partner_conf);
+/* propose_local + accept_local! of site i (0-based) to value x_new at the
+ * current slice; returns p = exp(-Delta E) detratio */
+double oc_local_move_to(OcChain* c, int i, int x_new);
+void oc_get_global_stats(const OcChain* c, long* accepted, long* proposals);
+
 /* stand-alone linalg kernels for unit tests */
 /* udt_AVX_pivot!, UDT.jl:216-309 (one n x n block) */
 void oc_udt_pivot(int n, double* U, double* D, double* input, int64_t* pivot,

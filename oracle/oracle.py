@@ -97,6 +97,15 @@ def lib():
                                        C.POINTER(C.c_uint32)]
         L.oc_generate_chunks.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.oc_generate_chunks.restype = C.c_int
+        L.oc_global_update.argtypes = [P, C.c_int]
+        L.oc_global_update.restype = C.c_int
+        L.oc_global_detratio.argtypes = [P, C.c_void_p, dp]
+        L.oc_global_detratio.restype = C.c_double
+        L.oc_replica_weight.argtypes = [P, C.c_void_p, dp, dp]
+        L.oc_replica_accept.argtypes = [P, C.c_void_p]
+        L.oc_local_move_to.argtypes = [P, C.c_int, C.c_int]
+        L.oc_local_move_to.restype = C.c_double
+        L.oc_get_global_stats.argtypes = [P, C.POINTER(C.c_long), C.POINTER(C.c_long)]
         L.oc_run_chains_threaded.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
         L.oc_run_chains_threaded.restype = C.c_double
         _lib = L
@@ -244,6 +253,35 @@ class OracleChain:
         buf = np.zeros(self.nf * self.n * self.n)
         lib().oc_get_stack(self.h, which, idx, _dp(buf))
         return self._buf_to_blocks(buf, self.nf, self.n)
+
+    # --- global updates (global_updates.jl, parallel_updates.jl)
+    def global_update(self, kind=0):
+        """GlobalFlip (kind 0) or GlobalShuffle (kind 1); True when accepted."""
+        return bool(lib().oc_global_update(self.h, int(kind)))
+
+    def global_detratio(self, proposal):
+        c = np.asfortranarray(proposal, dtype=np.int8)
+        dE = np.zeros(1)
+        r = lib().oc_global_detratio(self.h, c.ctypes.data, _dp(dE))
+        return r, float(dE[0])
+
+    def replica_weight(self, partner_conf):
+        c = np.asfortranarray(partner_conf, dtype=np.int8)
+        w, p = np.zeros(1), np.zeros(1)
+        lib().oc_replica_weight(self.h, c.ctypes.data, _dp(w), _dp(p))
+        return float(w[0]), float(p[0])
+
+    def replica_accept(self, partner_conf):
+        c = np.asfortranarray(partner_conf, dtype=np.int8)
+        lib().oc_replica_accept(self.h, c.ctypes.data)
+
+    def local_move_to(self, i, x_new):
+        return lib().oc_local_move_to(self.h, int(i), int(x_new))
+
+    def global_stats(self):
+        a, p = C.c_long(), C.c_long()
+        lib().oc_get_global_stats(self.h, C.byref(a), C.byref(p))
+        return a.value, p.value
 
     def analysis(self):
         out = np.zeros(5)

@@ -79,3 +79,34 @@ def test_mixed_sweeps_track_fp64(pkg, lib, oracle):
     G = h.greens(0)
     Gref = oc.calculate_greens_at(st["current_slice"] - 1)
     assert maxdiff(G, Gref) <= TOL_MIXED
+
+
+def test_mixed_16x16_beta10_every_stabilisation(pkg, lib, oracle):
+    """The mixed-precision workload itself: 16x16 repulsive Hubbard (n = 256,
+    two flavours), beta = 10, M = 100, safe_mult = 10.  G of the mixed path
+    from scratch at every stabilisation slice (chunk boundary) against FP64:
+    the FP64 oracle at three of them, the FP64 GPU path (itself pinned to the
+    oracle at 1e-10) at all eleven."""
+    model, param, fld, exps = make_setup(pkg, L=16, U=-4.0, beta=10.0, safe_mult=10,
+                                         field=pkg.MagneticHirschField)
+    cfg = [chain_config(lib, model, param, fld, 4)]
+    hm = lib.Handle(cfg, precision=lib.PREC_MIXED)
+    hd = lib.Handle(cfg, precision=lib.PREC_FP64)
+    oc = oracle_chain(oracle, model, param, fld, exps, 4)
+    for h in (hm, hd):
+        h.set_hopping(-1, exps)
+        h.init_random_field(0)
+    oc.init_random_conf()
+    assert np.array_equal(hm.get_field(0), oc.get_conf())
+    bounds = sorted({0, param.slices} | {b for _, b in pkg.generate_chunks(param.slices, 10)})
+    assert len(bounds) == 11
+    worst_oracle, worst_fp64 = 0.0, 0.0
+    for sl in bounds:
+        gm = hm.calculate_greens(0, sl)
+        worst_fp64 = max(worst_fp64, maxdiff(gm, hd.calculate_greens(0, sl)))
+        if sl in (0, 50, 100):
+            worst_oracle = max(worst_oracle, maxdiff(gm, oc.calculate_greens_at(sl)))
+    print(f"16x16 beta=10: max |dG| mixed vs FP64 oracle {worst_oracle:.2e}, "
+          f"vs FP64 GPU at every stabilisation {worst_fp64:.2e}")
+    assert worst_oracle <= TOL_MIXED
+    assert worst_fp64 <= TOL_MIXED

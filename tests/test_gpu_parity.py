@@ -183,3 +183,23 @@ def test_large_n_delayed_updates(pkg, lib, oracle, lattice, L, field):
     oc.sweeps(1)
     assert np.array_equal(h.get_field(0), oc.get_conf())
     assert maxdiff(h.greens(0), oc.greens()) < TOL_G
+
+
+def test_max_size_16x16_two_flavours(pkg, lib, oracle):
+    """The largest lattice of the workloads (16x16, n = 256, two flavours):
+    G from scratch at several slices, then one full sweep replayed bit-exactly
+    (G in global memory, delayed rank-16 updates)."""
+    h, oc, model, param, fld = _pair(pkg, lib, oracle, "MagneticHirschField", L=16, beta=2.0,
+                                     safe_mult=10, seed=9)
+    assert len(model.l) == 256
+    h.init_random_field(0)
+    oc.init_random_conf()
+    for sl in (0, 10, param.slices):
+        assert maxdiff(h.calculate_greens(0, sl), oc.calculate_greens_at(sl)) < TOL_G, sl
+    h.initialize_run()
+    oc.initialize_run()
+    h.sweep(1)
+    oc.sweeps(1)
+    assert np.array_equal(h.get_field(0), oc.get_conf())
+    assert h.get_rng(0)[1] == oc.rng_counter()
+    assert maxdiff(h.greens(0), oc.greens()) < TOL_G

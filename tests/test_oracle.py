@@ -201,3 +201,70 @@ def test_replay_determinism(oracle, pkg):
     # Hirsch fields draw one uniform per proposal with p <= 1 only
     props = 3 * 2 * param.slices * len(model.l)
     assert len(model.l) * param.slices < a.rng_counter() <= len(model.l) * param.slices + props
+
+
+@pytest.mark.parametrize("U,mu,field", [(1.0, 0.5, "DensityHirschField"),
+                                        (1.0, 0.5, "DensityGHQField"),
+                                        (-1.0, 0.0, "MagneticHirschField"),
+                                        (-1.0, 0.0, "MagneticGHQField")])
+def test_global_update_equals_product_of_local_updates(oracle, pkg, U, mu, field):
+    """The backbone check of the reference's global and parallel updates
+    (test/updates.jl:186-236): the probability of a global move to a shuffled
+    configuration equals the product of the local-move probabilities along a
+    path of single-site moves to the same configuration, and both end in the
+    same configuration, slice and Green's function."""
+    model, param, fld, exps = make_setup(pkg, L=2, U=U, mu=mu, beta=2.0,
+                                         field=getattr(pkg, field))
+    rng = np.random.default_rng(8)
+    ghq = "GHQ" in field
+    for trial in range(5):
+        conf0 = (rng.integers(1, 5, size=(4, param.slices)) if ghq else
+                 rng.choice([-1, 1], size=(4, param.slices))).astype(np.int8)
+        o1 = oracle_chain(oracle, model, param, fld, exps, 3 + trial)
+        o2 = oracle_chain(oracle, model, param, fld, exps, 3 + trial)
+        for o in (o1, o2):
+            o.set_conf(conf0)
+            o.initialize_run()
+        target = np.asfortranarray(rng.permuted(conf0.ravel(order="F")).reshape(conf0.shape,
+                                                                                order="F"))
+        detratio, dE = o1.global_detratio(target)
+        global_p = abs(np.exp(-dE) * detratio)
+        o1.replica_accept(target)
+        local_p = 1.0
+        for _ in range(param.slices):
+            t = o2.state()["current_slice"]
+            cur = o2.get_conf()
+            for i in range(4):
+                if cur[i, t - 1] != target[i, t - 1]:
+                    local_p *= o2.local_move_to(i, int(target[i, t - 1]))
+            o2.propagate()
+        for _ in range(param.slices):
+            o2.propagate()
+        assert abs(local_p - global_p) <= 1.5e-8 * abs(global_p), (local_p, global_p)
+        assert np.array_equal(o1.get_conf(), o2.get_conf())
+        assert o1.state()["current_slice"] == o2.state()["current_slice"]
+        assert maxdiff(o1.greens(), o2.greens()) < 1e-10
+
+
+@pytest.mark.parametrize("field", FIELDS)
+def test_global_flip_and_shuffle_keep_stack_consistent(oracle, pkg, field):
+    """Global moves (accepted or rejected) leave a valid chain: G equals the
+    from-scratch G of the resulting configuration, rejected moves restore the
+    configuration, and local sweeps continue without propagation errors."""
+    model, param, fld, exps = make_setup(pkg, L=2, U=FIELD_U[field], beta=2.0, safe_mult=5,
+                                         field=getattr(pkg, field))
+    o = oracle_chain(oracle, model, param, fld, exps, 21)
+    o.init_random_conf()
+    o.initialize_run()
+    n_acc = 0
+    for k in range(12):
+        before = o.get_conf()
+        acc = o.global_update(k % 2)
+        n_acc += acc
+        if not acc:
+            assert np.array_equal(o.get_conf(), before)
+        assert o.state()["current_slice"] == 1 and o.state()["direction"] == 1
+        assert maxdiff(o.greens(), o.calculate_greens_at(0)) < 1e-9
+        o.sweeps(1)
+    assert o.global_stats() == (n_acc, 12)
+    assert o.analysis()["propagation_error_reported"] < 1e-6
