@@ -24,3 +24,4 @@ def run(mc, **kwargs):
     """``run!(mc)`` of the reference (DQMC.jl:252)."""
     return mc.run(**kwargs)
 from .serving import Request, Server, poisson_stream, request_config, run_ensemble  # noqa: F401
+from .tempering import neighbour_partners, run_tempering  # noqa: F401,E402

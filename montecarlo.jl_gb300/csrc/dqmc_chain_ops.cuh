@@ -190,7 +190,27 @@ __device__ void mat_ident(const Ctx& x, double* A) {
     for (int b = 0; b < x.nf; ++b) ident(x.n, blk(A, x, b));
 }
 
+// two flavour blocks that fit the shared-memory QR: factor them together
+__device__ __forceinline__ bool paired(const Ctx& x) { return x.nf == 2 && x.n <= 64; }
+__device__ __forceinline__ UdtJob udt_job(const Ctx& x, double* U, double* D, double* In, int b) {
+    return UdtJob{blk(U, x, b), D + b * x.n, blk(In, x, b), x.c->pivot + b * x.n,
+                  x.c->tempv + b * x.n};
+}
+__device__ __forceinline__ void udt_pair(const Ctx& x, double* U, double* D, double* In, bool apply) {
+    udt_pivot_sm2(x.n, udt_job(x, U, D, In, 0), udt_job(x, U, D, In, 1), apply, x.s->arena,
+                  x.s->sv, x.s->sxd);
+}
+__device__ __forceinline__ void rdivp_pair(const Ctx& x, double* A, double* T, double* O) {
+    const int n = x.n;
+    rdivp2(n, A, T, O, x.c->pivot, blk(A, x, 1), blk(T, x, 1), blk(O, x, 1), x.c->pivot + n,
+           x.s->sv);
+}
+
 __device__ __noinline__ void udt_blocks(const Ctx& x, double* U, double* D, double* In, bool apply) {
+    if (paired(x)) {
+        udt_pair(x, U, D, In, apply);
+        return;
+    }
     for (int b = 0; b < x.nf; ++b) udt_one(x, blk(U, x, b), D + b * x.n, blk(In, x, b), b, apply);
 }
 __device__ __noinline__ void mm_blocks(const Ctx& x, double* C, double* A, double* B) {
@@ -237,10 +257,51 @@ __device__ __noinline__ void add_slice_sequence_right(const Ctx& x, int idx) {
     phase_stop(x, DQMC_PHASE_T_UPDATE, t0);
 }
 
+// calculate_greens_AVX! for two flavour blocks in lock step (the blocks are
+// independent; each sees exactly the per-block sequence below), so that the
+// two QR factorisations and the two triangular solves of each step run
+// together.
+__device__ __noinline__ void calculate_greens_pair(const Ctx& x, double* Gout, bool finish) {
+    DqmcChain& c = *x.c;
+    const int n = x.n;
+    double* sm = x.s->tiles;
+    for (int b = 0; b < 2; ++b) mm<false, true>(n, blk(Gout, x, b), blk(c.Tl, x, b), blk(c.Tr, x, b), sm);
+    __syncthreads();
+    for (int b = 0; b < 2; ++b) dright(n, blk(c.Tr, x, b), blk(Gout, x, b), c.Dr + b * n);
+    __syncthreads();
+    for (int b = 0; b < 2; ++b) dleft(n, blk(Gout, x, b), c.Dl + b * n, blk(c.Tr, x, b));
+    __syncthreads();
+    udt_pair(x, c.Tr, c.Dr, Gout, false);
+    for (int b = 0; b < 2; ++b) mm<false, false>(n, blk(c.Tl, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b), sm);
+    __syncthreads();
+    rdivp_pair(x, c.Ur, Gout, c.Ul);
+    for (int b = 0; b < 2; ++b) mm<true, false>(n, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ur, x, b), sm);
+    __syncthreads();
+    for (int e = threadIdx.x; e < 2 * n; e += DQMC_NT) {
+        const int b = e / n, i = e % n;
+        blk(c.Tr, x, b)[(size_t)i * n + i] += c.Dr[b * n + i];
+    }
+    __syncthreads();
+    udt_pair(x, c.Ul, c.Dr, c.Tr, false);
+    if (!finish) return;
+    rdivp_pair(x, c.Ur, c.Tr, Gout);
+    for (int b = 0; b < 2; ++b) mm<false, false>(n, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ul, x, b), sm);
+    for (int e = threadIdx.x; e < 2 * n; e += DQMC_NT) c.Dl[e] = 1.0 / c.Dr[e];
+    __syncthreads();
+    for (int b = 0; b < 2; ++b) dright(n, blk(c.Ul, x, b), blk(c.Ur, x, b), c.Dl + b * n);
+    __syncthreads();
+    for (int b = 0; b < 2; ++b) mm<false, true>(n, blk(Gout, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b), sm);
+    __syncthreads();
+}
+
 // calculate_greens_AVX! (stack.jl:442-496), per flavour block.  finish =
 // false stops after the second UDT: calculate_inv_greens_udt
 // (global_updates.jl:26-49), leaving det(G) = 1 / prod(Dr) up to phases.
 __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout, bool finish = true) {
+    if (paired(x)) {
+        calculate_greens_pair(x, Gout, finish);
+        return;
+    }
     DqmcChain& c = *x.c;
     const int n = x.n;
     const bool bf = x.nf > 1;

@@ -543,6 +543,246 @@ __device__ __noinline__ void udt_pivot_sm(int n, double* __restrict__ U, double*
     __syncthreads();
 }
 
+// One flavour block's operands of udt_pivot_sm2.
+struct UdtJob {
+    double* U;
+    double* D;
+    double* In;
+    int* piv;
+    double* tau;
+};
+
+// udt_pivot_sm for the two flavour blocks of a BlockDiagonal matrix at once
+// (UDT.jl:352-370 runs them one after the other; they are independent):
+// threads 0-127 factor block 0, threads 128-255 block 1, each in its own half
+// of `arena` (n <= 64, leading dimension n + 1) with two threads per column;
+// the serial reflector step of the two blocks runs on warps 0 and 5 (different
+// SM sub-partitions), so the two latency chains overlap, and Q is accumulated
+// directly in U (global memory) instead of a second shared-memory block.
+// sv: 2 * 64 doubles (block g at g * 64); sxd: 2 doubles.  Same algorithm and
+// pivot rule as udt_pivot_sm.
+__device__ __noinline__ void udt_pivot_sm2(int n, UdtJob j0, UdtJob j1, bool apply,
+                                           double* arena, double* sv, double* sxd) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int g = tid >> 7, gtid = tid & 127, gwarp = gtid >> 5;
+    const UdtJob J = g ? j1 : j0;
+    const int ld = n + 1;
+    double* sIn = arena + (size_t)g * 64 * 65;
+    double* svg = sv + g * 64;
+    for (int e = gtid; e < n * n; e += 128) sIn[(e % n) + (e / n) * ld] = J.In[e];
+    for (int i = gtid; i < n; i += 128) J.piv[i] = i + 1;
+    __syncthreads();
+    // initial squared column norms: two threads per column, two chains each
+    if (gwarp * 32 < 2 * n) {
+        const bool act = gtid < 2 * n;
+        const int col = act ? (gtid >> 1) : 0, h = gtid & 1;
+        const double* a = sIn + col * ld;
+        double q0 = 0.0, q1 = 0.0;
+        if (act) {
+            int r = h;
+            for (; r + 2 < n; r += 4) {
+                q0 = fma(a[r], a[r], q0);
+                q1 = fma(a[r + 2], a[r + 2], q1);
+            }
+            if (r < n) q0 = fma(a[r], a[r], q0);
+        }
+        double q = q0 + q1;
+        q += __shfl_xor_sync(0xffffffffu, q, 1);
+        if (act && h == 0) svg[col] = q;
+    }
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {
+        if (gwarp == g) {  // warp 0 for block 0, warp 5 for block 1
+            long long best = -1;
+            int bi = j;  // never out of range, also when every norm is NaN
+            for (int col = j + lane; col < n; col += 32) {
+                long long v = __double_as_longlong(svg[col]);
+                if (v > best) { best = v; bi = col; }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+                int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+                if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+            }
+            const int jm = bi;
+            const double normu = __longlong_as_double(best);
+            if (jm != j) {
+                double* a = sIn + jm * ld;
+                double* b = sIn + j * ld;
+                for (int r = lane; r < n; r += 32) {
+                    double t = a[r];
+                    a[r] = b[r];
+                    b[r] = t;
+                }
+                if (lane == 0) {
+                    int tp = J.piv[jm];
+                    J.piv[jm] = J.piv[j];
+                    J.piv[j] = tp;
+                    svg[jm] = svg[j];
+                }
+            }
+            __syncwarp();
+            double* x = sIn + j * ld;
+            double xi1 = x[j];
+            double t = 0.0;
+            if (normu != 0.0) {
+                double nu = copysign(sqrt(normu), xi1);
+                xi1 += nu;
+                const double inv = 1.0 / xi1;
+                __syncwarp();
+                for (int r = j + 1 + lane; r < n; r += 32) x[r] = x[r] * inv;
+                if (lane == 0) x[j] = -nu;
+                t = xi1 / nu;
+            }
+            if (lane == 0) { J.tau[j] = t; sxd[g] = t; }
+        }
+        __syncthreads();
+        const int ncols = n - j - 1;
+        if (gwarp * 32 < 2 * ncols) {
+            const double t = sxd[g];
+            const double* x = sIn + j * ld;
+            const bool act = gtid < 2 * ncols;
+            const int col = j + 1 + (gtid >> 1), h = gtid & 1;
+            double* a = sIn + (act ? col : j) * ld;
+            const double aj = act ? a[j] : 0.0;
+            double s0 = 0.0, s1 = 0.0;
+            if (act) {
+                int r = j + 1 + h;
+                for (; r + 2 < n; r += 4) {
+                    s0 = fma(x[r], a[r], s0);
+                    s1 = fma(x[r + 2], a[r + 2], s1);
+                }
+                if (r < n) s0 = fma(x[r], a[r], s0);
+            }
+            double s = s0 + s1;
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            const double vAj = t * (aj + s);
+            double q0 = 0.0, q1 = 0.0;
+            if (act) {
+                if (h == 0) a[j] = aj - vAj;
+                int r = j + 1 + h;
+                for (; r + 2 < n; r += 4) {
+                    const double v0 = fma(-x[r], vAj, a[r]);
+                    const double v1 = fma(-x[r + 2], vAj, a[r + 2]);
+                    a[r] = v0;
+                    a[r + 2] = v1;
+                    q0 = fma(v0, v0, q0);
+                    q1 = fma(v1, v1, q1);
+                }
+                if (r < n) {
+                    const double v0 = fma(-x[r], vAj, a[r]);
+                    a[r] = v0;
+                    q0 = fma(v0, v0, q0);
+                }
+            }
+            double q = q0 + q1;
+            q += __shfl_xor_sync(0xffffffffu, q, 1);
+            if (act && h == 0) svg[col] = q;
+        }
+        __syncthreads();
+    }
+    // Calculate Q (UDT.jl:272-289), accumulated in U
+    for (int e = gtid; e < n * n; e += 128) {
+        int i = e % n, c = e / n;
+        J.U[e] = (i == c) ? 1.0 : 0.0;
+    }
+    __syncthreads();
+    if (gtid == 0) J.U[(size_t)(n - 1) * n + (n - 1)] -= J.tau[n - 1];
+    __syncthreads();
+    for (int k = n - 2; k >= 0; --k) {
+        const int ncols = n - k;
+        if (gwarp * 32 < 2 * ncols) {
+            const double* v = sIn + k * ld;
+            const double t = J.tau[k];
+            const bool act = gtid < 2 * ncols;
+            const int col = k + (gtid >> 1), h = gtid & 1;
+            double* u = J.U + (size_t)(act ? col : k) * n;
+            const double uk = act ? u[k] : 0.0;
+            double s0 = 0.0, s1 = 0.0;
+            if (act) {
+                int r = k + 1 + h;
+                for (; r + 2 < n; r += 4) {
+                    s0 = fma(v[r], u[r], s0);
+                    s1 = fma(v[r + 2], u[r + 2], s1);
+                }
+                if (r < n) s0 = fma(v[r], u[r], s0);
+            }
+            double s = s0 + s1;
+            s += __shfl_xor_sync(0xffffffffu, s, 1);
+            const double vB = t * (uk + s);
+            if (act) {
+                if (h == 0) u[k] = uk - vB;
+                for (int r = k + 1 + h; r < n; r += 2) u[r] = fma(-v[r], vB, u[r]);
+            }
+        }
+        __syncthreads();
+    }
+    // D (UDT.jl:293-301); 1/D per row as the reference's _apply_pivot!
+    for (int i = gtid; i < n; i += 128) {
+        double xx = fabs(sIn[i * ld + i]);
+        double d = (xx == 0.0) ? 1.0 : xx;
+        J.D[i] = d;
+        svg[i] = 1.0 / d;
+    }
+    __syncthreads();
+    // _apply_pivot! (UDT.jl:311-334), straight from shared memory
+    for (int e = gtid; e < n * n; e += 128) {
+        int i = e % n, jj = e / n;
+        const double v = sIn[i + jj * ld];
+        if (apply) {
+            J.In[i + (size_t)(J.piv[jj] - 1) * n] = (jj >= i) ? svg[i] * v : 0.0;
+        } else {
+            J.In[e] = (jj >= i) ? svg[i] * v : v;
+        }
+    }
+    __syncthreads();
+}
+
+// rdivp for the two flavour blocks at once (n <= 64): threads 0-63 run the
+// rows of block 0 and threads 64-127 those of block 1 (four warps, one per SM
+// sub-partition, where one block alone keeps two of them busy).  rcp: 2 * 64
+// doubles.  Same arithmetic per row as rdivp.
+__device__ __noinline__ void rdivp2(int n, double* A0, const double* T0, double* O0, const int* p0,
+                                    double* A1, const double* T1, double* O1, const int* p1,
+                                    double* rcp) {
+    const int tid = threadIdx.x;
+    for (int e = tid; e < 2 * n; e += DQMC_NT) {
+        const int b = e / n, j = e % n;
+        const double* T = b ? T1 : T0;
+        rcp[b * 64 + j] = 1.0 / T[(size_t)j * n + j];
+    }
+    for (int e = tid; e < 2 * n * n; e += DQMC_NT) {
+        const int b = e / (n * n), f = e % (n * n);
+        const int i = f % n, j = f / n;
+        const double* A = b ? A1 : A0;
+        const int* piv = b ? p1 : p0;
+        (b ? O1 : O0)[f] = A[i + (size_t)(piv[j] - 1) * n];
+    }
+    __syncthreads();
+    if (tid < 128) {
+        const int b = tid >> 6, i = tid & 63;
+        if (i < n) {
+            double* A = b ? A1 : A0;
+            const double* T = b ? T1 : T0;
+            const double* O = b ? O1 : O0;
+            const double* rc = rcp + b * 64;
+            for (int j = 0; j < n; ++j) {
+                const double* tj = T + (size_t)j * n;
+                double x0 = O[i + (size_t)j * n], x1 = 0.0;
+                int k = 0;
+                for (; k + 1 < j; k += 2) {
+                    x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
+                    x1 = fma(-A[i + (size_t)(k + 1) * n], tj[k + 1], x1);
+                }
+                if (k < j) x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
+                A[i + (size_t)j * n] = (x0 + x1) * rc[j];
+            }
+        }
+    }
+    __syncthreads();
+}
+
 // rdivp!: A <- A * P * T^-1 with T upper triangular (real.jl:198-226 for the
 // dense form, blockdiagonal.jl:286-324 for the block form, which multiplies
 // by 1/T[j,j] instead of dividing).  Rows of A are independent: one thread per

@@ -38,14 +38,16 @@ class DQMC:
 
     Extra keywords of this implementation: ``precision`` ("fp64" or "mixed"),
     ``device``, ``device_measurements`` (default True: the on-device
-    equal-time observables) and ``structure_factor_q`` (the q of S^z(q),
-    default (pi, pi, ...)).
+    equal-time observables), ``structure_factor_q`` (the q of S^z(q),
+    default (pi, pi, ...)) and ``global_update`` (None, "flip" or "shuffle":
+    the scheduler SimpleScheduler(LocalSweep(), GlobalFlip() / GlobalShuffle()),
+    scheduler.jl:258-289).
     """
 
     def __init__(self, model, *, seed: int = -1, field=None, measurements=None,
                  thermalization_measurements=None, last_sweep: int = 0, measure_rate: int = 10,
                  precision: str = "fp64", device: int = 0, device_measurements: bool = True,
-                 structure_factor_q=None, **kwargs):
+                 structure_factor_q=None, global_update=None, **kwargs):
         self.model = model
         self.parameters = DQMCParameters.make(measure_rate=measure_rate, **kwargs)
         fcls = field if field is not None else model.choose_field()
@@ -78,12 +80,18 @@ class DQMC:
         ph = pos @ q
         self._q_phases = (np.cos(ph), np.sin(ph))
         self._dev_meas_on = None
+        if global_update not in (None, "flip", "shuffle"):
+            raise ValueError("global_update must be None, 'flip' or 'shuffle'")
+        self.global_update = global_update
 
     # -- stack --------------------------------------------------------------
     def init(self):
         """init! + the stack part of initialize_run (DQMC.jl:144-179)."""
         self.handle.set_field(0, np.asfortranarray(self.field.conf))
         self.handle.initialize_run()
+        if self.global_update is not None:
+            self.handle.set_global_schedule(
+                _lib.GLOBAL_FLIP if self.global_update == "flip" else _lib.GLOBAL_SHUFFLE, 0)
         self.initialized = True
 
     @property
@@ -138,6 +146,7 @@ class DQMC:
         st = self.handle.stats(0)
         self.analysis = dict(
             acceptance=(st["accepted"] - acc0) / max(1, st["proposals"] - prop0),
+            global_moves=self.handle.global_stats(0),
             propagation_errors=st["propagation_errors"],
             max_propagation_error=st["max_propagation_error"],
             negative_probability=st["negative_probability"],

@@ -40,14 +40,28 @@ def _same(h, ocs):
 
 @pytest.mark.parametrize("field", FIELDS)
 def test_global_flip_and_shuffle_replay_oracle(pkg, lib, oracle, field):
+    """A flip of a magnetic field is an exact symmetry (up <-> down): its
+    determinant ratio is 1 up to rounding, so whether p > 1 (no uniform drawn)
+    depends on the last bit.  For those moves the test checks the move itself
+    and re-aligns the stream position; every other move replays bit-exactly."""
     mu = 0.3 if field.startswith("Density") else 0.0
+    magnetic = field.startswith("Magnetic")
     specs = [(4, field, FIELD_U[field], mu, 2.0), (3, field, FIELD_U[field], mu, 1.0)]
     h, ocs = _pairs(pkg, lib, oracle, specs)
     for k in range(4):
         kind = k % 2
         acc = h.global_update(kind)
         for j, o in enumerate(ocs):
-            assert bool(acc[j]) == o.global_update(kind), (k, j)
+            oacc = o.global_update(kind)
+            if magnetic and kind == 0:
+                cur = o.get_conf().astype(np.int16)
+                flipped = (5 - cur) if "GHQ" in field else -cur
+                d, _ = o.global_detratio(flipped.astype(np.int8))  # a flip back: ratio 1
+                assert abs(d - 1.0) < 1e-9
+                assert bool(acc[j]) and oacc
+                h.set_rng(j, h.get_rng(j)[0], o.rng_counter())
+            else:
+                assert bool(acc[j]) == oacc, (k, j)
         _same(h, ocs)
         h.sweep(1)
         for o in ocs:
@@ -118,3 +132,19 @@ def test_global_update_needs_chains_between_sweeps(pkg, lib):
     assert e.value.code == 1
     with pytest.raises(lib.DQMCError):
         h.replica_exchange([0])
+
+
+def test_parallel_tempering_in_u(pkg, lib):
+    """Four replicas of the 4x4 repulsive model at U = 2, 3, 4, 5 exchange
+    configurations with their neighbours every sweep; the device
+    observables order with U (double occupancy falls as U grows)."""
+    reps = [(pkg.HubbardModel(pkg.SquareLattice(4), U=-u), 2.0, 0.1, 10, 300 + j)
+            for j, u in enumerate((2.0, 3.0, 4.0, 5.0))]
+    out = pkg.run_tempering(reps, rounds=60, thermalization=20)
+    assert len(out["exchange_acceptance"]) == 3
+    assert all(0.0 <= a <= 1.0 for a in out["exchange_acceptance"])
+    assert sum(out["exchanges_tried"]) == 90
+    assert sum(a for a, _ in out["global_stats"]) > 0
+    docc = [o["double_occupancy"][0] for o in out["observables"]]
+    assert docc[0] > docc[-1]
+    assert all(o["count"] == 60 for o in out["observables"])

@@ -103,3 +103,9 @@ def test_config_recorder_roundtrip(pkg):
         assert len(rec) == 3
         for i, c in enumerate(confs[1::2]):
             assert np.array_equal(rec[i], c)
+
+
+def test_neighbour_partners(pkg):
+    """Replica-exchange rounds pair neighbours, alternating even and odd pairs."""
+    assert pkg.neighbour_partners(5, False).tolist() == [1, 0, 3, 2, -1]
+    assert pkg.neighbour_partners(5, True).tolist() == [-1, 2, 1, 4, 3]
