@@ -90,12 +90,17 @@ __device__ __forceinline__ void phase_stop(const Ctx& x, int phase, long long t0
 // mixed-precision chain the double-float product on the FP32 pipe.  The UDT,
 // the Green's reconstruction, the T updates, the determinant ratios and the
 // rank-1 updates stay FP64 on every chain.
+// Every transposed left operand (TA) of these products is a hopping
+// exponential, which is symmetric, so the double-float product reads it
+// untransposed (identical sums; the untransposed staging needs fewer
+// registers).  Below n = 48 the mixed path keeps the FP64 product: the
+// matrices are too small for the split arithmetic to pay.
 template <bool TA, bool TB>
 __device__ __forceinline__ void smm(const Ctx& x, bool wrap, double* C, const double* A,
                                     const double* B) {
     (void)wrap;
-    if (x.c->prec == DQMC_PREC_MIXED_ID)
-        mm_df<TA, TB>(x.n, C, A, B, x.s->tiles);
+    if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48)
+        mm_df<false, TB>(x.n, C, A, B, x.s->tiles);
     else
         mm<TA, TB>(x.n, C, A, B, x.s->tiles);
 }

@@ -61,7 +61,12 @@ __device__ __noinline__ void mm(int n, double* __restrict__ C, const double* __r
     double* sB = sm + 16 * 64;  // [16][64]: sB[kk*64 + j]
     const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
     for (int n0 = 0; n0 < n; n0 += 64) {
+        // 16-column / 16-row groups of this tile that hold any output (all four
+        // for n a multiple of 64; one for n = 16): the others are not computed
+        const int qn = min(4, (n - n0 + 15) >> 4);
         for (int m0 = 0; m0 < n; m0 += 64) {
+            const int rn = min(4, (n - m0 + 15) >> 4);
+            const bool full = (rn == 4) && (qn == 4);
             double acc[4][4];
 #pragma unroll
             for (int r = 0; r < 4; ++r)
@@ -89,17 +94,35 @@ __device__ __noinline__ void mm(int n, double* __restrict__ C, const double* __r
                     sB[kk * 64 + jj] = v;
                 }
                 __syncthreads();
+                if (full) {
 #pragma unroll
-                for (int kk = 0; kk < 16; ++kk) {
-                    double a[4], b[4];
+                    for (int kk = 0; kk < 16; ++kk) {
+                        double a[4], b[4];
 #pragma unroll
-                    for (int r = 0; r < 4; ++r) a[r] = sA[kk * 64 + tx + 16 * r];
+                        for (int r = 0; r < 4; ++r) a[r] = sA[kk * 64 + tx + 16 * r];
 #pragma unroll
-                    for (int q = 0; q < 4; ++q) b[q] = sB[kk * 64 + ty + 16 * q];
+                        for (int q = 0; q < 4; ++q) b[q] = sB[kk * 64 + ty + 16 * q];
 #pragma unroll
-                    for (int r = 0; r < 4; ++r)
+                        for (int r = 0; r < 4; ++r)
 #pragma unroll
-                        for (int q = 0; q < 4; ++q) acc[r][q] = fma(a[r], b[q], acc[r][q]);
+                            for (int q = 0; q < 4; ++q) acc[r][q] = fma(a[r], b[q], acc[r][q]);
+                    }
+                } else {
+                    for (int kk = 0; kk < 16; ++kk) {
+                        double a[4], b[4];
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) a[r] = r < rn ? sA[kk * 64 + tx + 16 * r] : 0.0;
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) b[q] = q < qn ? sB[kk * 64 + ty + 16 * q] : 0.0;
+#pragma unroll
+                        for (int r = 0; r < 4; ++r) {
+                            if (r < rn) {
+#pragma unroll
+                                for (int q = 0; q < 4; ++q)
+                                    if (q < qn) acc[r][q] = fma(a[r], b[q], acc[r][q]);
+                            }
+                        }
+                    }
                 }
                 __syncthreads();
             }
