@@ -259,6 +259,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
     ap.add_argument("--chains", type=int, default=0, help="ensemble size (default 2 per SM)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"],
+                    help="arithmetic of the timed ensemble (mixed: for profiling that path)")
     ap.add_argument("--cpu-budget", type=float, default=15.0, help="seconds of CPU-baseline work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
@@ -324,7 +326,8 @@ def main():
     from montecarlo_gb300 import replicas
 
     seed0 = replicas.chain_seeds(rank, B_chains)[0]  # disjoint seeds per rank
-    h = _lib.Handle(configs(seed0))
+    prec_main = _lib.PREC_MIXED if args.precision == "mixed" else _lib.PREC_FP64
+    h = _lib.Handle(configs(seed0), precision=prec_main)
     h.set_hopping(-1, exps)
     h.init_random_field(-1)
     # a dedicated stream: the library launches on it and the CUDA events below
@@ -367,7 +370,7 @@ def main():
     h.close()
 
     # ---- end to end through the C ABI with host buffers
-    h2 = _lib.Handle(configs(seed0 + 10_000))
+    h2 = _lib.Handle(configs(seed0 + 10_000), precision=prec_main)
     pin = torch.empty(4 * n * n, dtype=torch.float64, pin_memory=True)
     pin_np = pin.numpy().reshape(4, n, n)
     for m in range(4):
@@ -480,9 +483,12 @@ def main():
         line = {
             "metric": METRIC, "value": value, "unit": "sweeps/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f64+df32",
             "data": "synthetic (seeded random Hubbard-Stratonovich fields)",
-            "config": {"workload": desc, "path": "plain FP64 (value); mixed, batched, served below",
+            "config": {"workload": desc,
+                       "path": ("plain FP64" if args.precision == "fp64" else "mixed") +
+                               " (value); mixed, batched, served below",
                        "chains_per_gpu": B_chains, "parallelism": f"replicas{world}",
                        "l2": "working set larger than L2 (no flush needed)",
                        "chain_bytes": int(_lib.load().dqmc_chain_bytes(_lib.ChainConfig(

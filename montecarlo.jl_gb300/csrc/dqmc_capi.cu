@@ -44,7 +44,7 @@ struct Layout {
     size_t bytes;
     size_t off_conf, off_hop, off_G, off_Gtmp, off_Ul, off_Ur, off_Tl, off_Tr, off_tmp1, off_tmp2,
         off_currU, off_out, off_ustack, off_tstack, off_dstack, off_Dl, off_Dr, off_tempv,
-        off_pivot, off_meas, off_qcs, off_tconf, off_tempvf;
+        off_pivot, off_meas, off_qcs, off_tconf, off_tempvf, off_hopdf;
 };
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -70,6 +70,7 @@ Layout layout_of(const dqmc_chain_config& c, int prec) {
     L.off_qcs = o; o = align256(o + 2 * n * sizeof(double));
     L.off_tconf = o; o = align256(o + n * c.slices);
     L.off_tempvf = o; o = align256(o + nf * n * sizeof(double));
+    L.off_hopdf = o; o = align256(o + 2 * n * n * sizeof(float2));
     L.bytes = o;
     return L;
 }
@@ -183,6 +184,8 @@ void fill_descriptor(DqmcChain& d, const dqmc_chain_config& c, char* b, const La
     double* hop = (double*)(b + L.off_hop);
     d.conf = (int8_t*)(b + L.off_conf);
     d.eT2 = hop; d.eT2inv = hop + nn; d.eTh = hop + 2 * nn; d.eThinv = hop + 3 * nn;
+    d.eT2df = (const float2*)(b + L.off_hopdf);
+    d.eT2invdf = d.eT2df + nn;
     d.G = (double*)(b + L.off_G); d.Gtmp = (double*)(b + L.off_Gtmp);
     d.Ul = (double*)(b + L.off_Ul); d.Ur = (double*)(b + L.off_Ur);
     d.Tl = (double*)(b + L.off_Tl); d.Tr = (double*)(b + L.off_Tr);
@@ -340,6 +343,18 @@ int dqmc_set_hopping(dqmc_handle* h, int chain, const double* a, const double* b
             CUDA_TRY(cudaMemcpyAsync(dst[m], src[m], nn * sizeof(double), cudaMemcpyHostToDevice,
                                      h->stream),
                      "upload hopping exponentials");
+        // float pairs of exp(-dtau T) and exp(+dtau T): hi = fp32(x), lo = fp32(x - hi)
+        std::vector<float2> split(2 * nn);
+        for (int m = 0; m < 2; ++m)
+            for (size_t e = 0; e < nn; ++e) {
+                const double v = src[m][e];
+                const float hi = (float)v;
+                split[m * nn + e] = make_float2(hi, (float)(v - (double)hi));
+            }
+        CUDA_TRY(cudaMemcpyAsync((void*)h->host[i].eT2df, split.data(), 2 * nn * sizeof(float2),
+                                 cudaMemcpyHostToDevice, h->stream),
+                 "upload split hopping exponentials");
+        CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
     }
     CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
     return DQMC_OK;

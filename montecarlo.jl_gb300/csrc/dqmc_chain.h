@@ -13,6 +13,7 @@
 //                                                       shared by both flavours)
 #pragma once
 #include <stdint.h>
+#include <vector_types.h>
 
 #define DQMC_MAX_CHUNKS 256
 
@@ -33,6 +34,9 @@ struct DqmcChain {
     // buffers
     int8_t* conf;
     const double *eT2, *eT2inv, *eTh, *eThinv;
+    // eT2 and eT2inv split into float pairs (hi, lo) for the mixed path's
+    // double-float products
+    const float2 *eT2df, *eT2invdf;
     double *G, *Gtmp, *ustack, *tstack, *dstack, *Ul, *Ur, *Tl, *Tr, *Dl, *Dr, *tmp1, *tmp2,
         *currU, *tempv, *out;
     int* pivot;

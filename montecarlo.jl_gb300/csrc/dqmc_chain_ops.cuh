@@ -46,16 +46,41 @@ __device__ __forceinline__ double* blk(double* p, const Ctx& x, int b) { return 
 __device__ __forceinline__ bool g_resident_possible(const Ctx& x) {
     return x.n <= 64 && (size_t)x.nf * x.nn <= sizeof(x.s->arena) / sizeof(double);
 }
+// On a mixed-precision chain with n >= 32 the resident G is double-float
+// (float2 per entry, same bytes): the rank-1 updates and the wraps then run
+// entirely on the FP32 pipe; it is rounded back to FP64 whenever it leaves
+// shared memory.  (At n = 16 the split arithmetic costs more than it saves.)
+__device__ __forceinline__ bool df_mode(const Ctx& x) {
+    return x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 32;
+}
+__device__ __forceinline__ bool df_resident(const Ctx& x) { return df_mode(x) && x.s->gres; }
+__device__ __forceinline__ float2* arena_df(const Ctx& x) {
+    return reinterpret_cast<float2*>(x.s->arena);
+}
+// the resident G (either form) as FP64 into dst
+__device__ void g_resident_to(const Ctx& x, double* dst) {
+    if (df_mode(x)) {
+        const float2* a = arena_df(x);
+        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) dst[e] = df_to_d(a[e]);
+    } else {
+        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) dst[e] = x.s->arena[e];
+    }
+}
 __device__ void g_to_arena(const Ctx& x) {
     __syncthreads();
-    for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) x.s->arena[e] = x.s->Gglob[e];
+    if (df_mode(x)) {
+        float2* a = arena_df(x);
+        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) a[e] = d_to_df(x.s->Gglob[e]);
+    } else {
+        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) x.s->arena[e] = x.s->Gglob[e];
+    }
     __syncthreads();
     if (threadIdx.x == 0) { x.c->G = x.s->arena; x.s->gres = 1; }
     __syncthreads();
 }
 __device__ void g_to_global(const Ctx& x) {
     __syncthreads();
-    for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) x.s->Gglob[e] = x.s->arena[e];
+    g_resident_to(x, x.s->Gglob);
     __syncthreads();
     if (threadIdx.x == 0) { x.c->G = x.s->Gglob; x.s->gres = 0; }
     __syncthreads();
@@ -99,10 +124,16 @@ template <bool TA, bool TB>
 __device__ __forceinline__ void smm(const Ctx& x, bool wrap, double* C, const double* A,
                                     const double* B) {
     (void)wrap;
-    if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48)
-        mm_df<false, TB>(x.n, C, A, B, x.s->tiles);
-    else
+    const DqmcChain& c = *x.c;
+    if (c.prec == DQMC_PREC_MIXED_ID && x.n >= 48) {
+        // the transposed operand is eT2 or eT2inv: take its float-pair split
+        if (TA)
+            mm_dfx<true, false, false>(x.n, C, A == c.eT2 ? c.eT2df : c.eT2invdf, B, x.s->tiles);
+        else
+            mm_dfx<false, true, false>(x.n, C, A, B == c.eT2 ? c.eT2df : c.eT2invdf, x.s->tiles);
+    } else {
         mm<TA, TB>(x.n, C, A, B, x.s->tiles);
+    }
 }
 
 // interaction_matrix_exp! (fields.jl:380-386, 429-438, 548-560, 618-624)
@@ -170,8 +201,62 @@ __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* 
     }
 }
 
+// wrap_greens! of the resident double-float G of a mixed chain: the same
+// four slice-matrix steps with double-float diagonals (exact float pairs of
+// the interaction exponentials) and double-float products; tmp1 holds the
+// float-pair intermediate.
+__device__ __noinline__ void wrap_greens_df(const Ctx& x, int curr_slice, int direction) {
+    const DqmcChain& c = *x.c;
+    const int n = x.n;
+    float2* G = arena_df(x);
+    float2* T = reinterpret_cast<float2*>(c.tmp1);
+    float2* ev = reinterpret_cast<float2*>(x.s->ev + 256);  // beyond the nf*n FP64 entries
+    const int slice = direction == -1 ? curr_slice - 1 : curr_slice;
+    for (int half = 0; half < 2; ++half) {
+        // direction +1: B(l) G B(l)^-1 = eT2 (eV (G eV^-1)) eT2inv, as
+        //   slice_left then slice_inv_right; direction -1: B(l)^-1 G B(l) as
+        //   slice_inv_left then slice_right (stack.jl:319-357)
+        const bool inverse = (direction == 1) ? (half == 1) : (half == 0);
+        interaction_exp(x, slice, inverse);
+        for (int e = threadIdx.x; e < x.nf * n; e += DQMC_NT) ev[e] = d_to_df(x.s->ev[e]);
+        __syncthreads();
+        const float2* hop = inverse ? c.eT2invdf : c.eT2df;
+        for (int b = 0; b < x.nf; ++b) {
+            float2* g = G + (size_t)b * x.nn;
+            float2* t = T + (size_t)b * x.nn;
+            const float2* d = ev + b * n;
+            if (half == 0) {
+                if (direction == 1) {  // G <- eT2 * (eV * G)
+                    dleft_df(n, t, d, g);
+                    __syncthreads();
+                    mm_dfx<true, true, true>(n, g, hop, t, x.s->tiles);
+                } else {                 // G <- eV^-1 * (eT2inv * G)
+                    mm_dfx<true, true, true>(n, t, hop, g, x.s->tiles);
+                    __syncthreads();
+                    dleft_df(n, g, d, t);
+                }
+            } else {
+                if (direction == 1) {  // G <- (G * eV^-1) * eT2inv
+                    dright_df(n, t, g, d);
+                    __syncthreads();
+                    mm_dfx<true, true, true>(n, g, t, hop, x.s->tiles);
+                } else {                 // G <- (G * eT2) * eV
+                    mm_dfx<true, true, true>(n, t, g, hop, x.s->tiles);
+                    __syncthreads();
+                    dright_df(n, g, t, d);
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
 // wrap_greens! (stack.jl:594-603)
 __device__ void wrap_greens(const Ctx& x, double* gf, int curr_slice, int direction) {
+    if (df_resident(x) && gf == x.c->G) {
+        wrap_greens_df(x, curr_slice, direction);
+        return;
+    }
     if (direction == -1) {
         slice_inv_left(x, curr_slice - 1, gf, true);
         slice_right(x, curr_slice - 1, gf, true);
@@ -590,9 +675,15 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     const bool twoflv = (nf == 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     double* diag = x.s->ev;  // [nf * n] mirror of the diagonals (ev is free here)
+    // mixed chain with G resident: G is double-float; decisions still use FP64
+    // values (the diagonal and the update vectors are formed in FP64), the
+    // n x n rank-1 update runs in double-float on the FP32 pipe
+    const bool dfg = df_resident(x);
+    const float2* gdf = arena_df(x);
     for (int e = tid; e < nf * n; e += DQMC_NT) {
         const int b = e / n, k = e % n;
-        diag[e] = c.G[(size_t)b * x.nn + (size_t)k * n + k];
+        const size_t at = (size_t)b * x.nn + (size_t)k * n + k;
+        diag[e] = dfg ? df_to_d(gdf[at]) : c.G[at];
     }
     __syncthreads();
     long long acc_count = 0;
@@ -668,7 +759,15 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
         for (int e = tid; e < nf * n; e += DQMC_NT) {
             const int b = e / n, k = e % n;
             const double* g = c.G + (size_t)b * x.nn;
-            double gkj = g[(size_t)j * n + k], gjk = g[(size_t)k * n + j];
+            double gkj, gjk;
+            if (dfg) {
+                const float2* gb = gdf + (size_t)b * x.nn;
+                gkj = df_to_d(gb[(size_t)j * n + k]);
+                gjk = df_to_d(gb[(size_t)k * n + j]);
+            } else {
+                gkj = g[(size_t)j * n + k];
+                gjk = g[(size_t)k * n + j];
+            }
             if (delayed) {
                 // current G[k, j] and G[j, k] with the pending updates applied
                 const double* U = c.tmp2 + (size_t)b * x.nn;
@@ -683,6 +782,10 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
             const double rw = x.s->sxd[b] * gjk;
             x.s->r1.col[b][k] = ig;
             x.s->r1.row[b][k] = rw;
+            if (dfg) {  // float pairs of -col and row behind the FP64 vectors (n <= 64)
+                reinterpret_cast<float2*>(x.s->r1.col[b] + 256)[k] = d_to_df(-ig);
+                reinterpret_cast<float2*>(x.s->r1.row[b] + 256)[k] = d_to_df(rw);
+            }
             if (delayed) {
                 c.tmp2[(size_t)b * x.nn + (size_t)pending * n + k] = ig;
                 c.currU[(size_t)b * x.nn + (size_t)pending * n + k] = rw;
@@ -712,6 +815,18 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 diag[e] = fma(-x.s->r1.col[b][k], x.s->r1.row[b][k], diag[e]);
             }
             __syncwarp();
+        } else if (dfg) {
+            const int w = tid - 32, nw = DQMC_NT / 32 - 1;
+            for (int b = 0; b < nf; ++b) {
+                float2* g = arena_df(x) + (size_t)b * x.nn;
+                const float2* cl = reinterpret_cast<const float2*>(x.s->r1.col[b] + 256);
+                const float2* rw = reinterpret_cast<const float2*>(x.s->r1.row[b] + 256);
+                for (int k = w & 31; k < n; k += 32) {
+                    const float2 ck = cl[k];
+                    for (int l = w >> 5; l < n; l += nw)
+                        g[k + (size_t)l * n] = df_fma(ck, rw[l], g[k + (size_t)l * n]);
+                }
+            }
         } else {
             const int w = tid - 32, nw = DQMC_NT / 32 - 1;
             for (int b = 0; b < nf; ++b) {
@@ -982,7 +1097,13 @@ __device__ __noinline__ void measure(const Ctx& x) {
     DqmcChain& c = *x.c;
     const int n = x.n, nf = x.nf;
     const size_t nn = x.nn;
-    greens_physical(x, c.G, c.out);
+    const double* src = c.G;
+    if (df_resident(x)) {  // FP64 snapshot of the double-float resident G
+        g_resident_to(x, x.s->Gglob);
+        __syncthreads();
+        src = x.s->Gglob;
+    }
+    greens_physical(x, src, c.out);
     const double* g1 = c.out;
     const double* g2 = c.out + (size_t)(nf - 1) * nn;
     double* occ = c.meas + DQMC_MEAS_OCC_OFF;

@@ -232,6 +232,143 @@ __device__ __noinline__ void mm_df(int n, double* __restrict__ C, const double* 
     }
 }
 
+// ---- double-float storage (the mixed path's shared-memory G) ----------------
+// A value is a float pair (hi, lo) with |lo| <= ulp(hi) / 2: ~48 significant
+// bits.
+__device__ __forceinline__ float2 d_to_df(double v) {
+    const float h = __double2float_rn(v);
+    return make_float2(h, __double2float_rn(v - (double)h));
+}
+__device__ __forceinline__ double df_to_d(float2 v) { return (double)v.x + (double)v.y; }
+// (hi, lo) from an unnormalised pair (Fast2Sum, |s| >= |t|)
+__device__ __forceinline__ float2 df_norm(float s, float t) {
+    const float h = __fadd_rn(s, t);
+    return make_float2(h, __fsub_rn(t, __fsub_rn(h, s)));
+}
+// a * b for double-float a, b (TwoProd by fmaf; the lo * lo term is dropped)
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b) {
+    const float p = __fmul_rn(a.x, b.x);
+    const float e = __fmaf_rn(a.x, b.x, -p);
+    return df_norm(p, __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, e)));
+}
+// g + a * b (the rank-1 update's element step): TwoProd, TwoSum, renormalise
+__device__ __forceinline__ float2 df_fma(float2 a, float2 b, float2 g) {
+    const float p = __fmul_rn(a.x, b.x);
+    const float pe = __fmaf_rn(a.x, b.x, -p);
+    const float pl = __fmaf_rn(a.x, b.y, __fmaf_rn(a.y, b.x, pe));
+    const float s = __fadd_rn(g.x, p);
+    const float z = __fsub_rn(s, g.x);
+    const float er = __fadd_rn(__fsub_rn(g.x, __fsub_rn(s, z)), __fsub_rn(p, z));
+    return df_norm(s, __fadd_rn(__fadd_rn(g.y, pl), er));
+}
+// C = Diagonal(d) * B and C = A * Diagonal(d) on double-float matrices
+__device__ __forceinline__ void dleft_df(int n, float2* __restrict__ C, const float2* __restrict__ d,
+                                         const float2* __restrict__ B) {
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) C[e] = df_mul(d[e % n], B[e]);
+}
+__device__ __forceinline__ void dright_df(int n, float2* __restrict__ C, const float2* __restrict__ A,
+                                          const float2* __restrict__ d) {
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) C[e] = df_mul(A[e], d[e / n]);
+}
+
+// mm_df without transposes, with each operand either FP64 or already split
+// (ADF / BDF: a float2 array) and the result FP64 or double-float (CDF).
+// The split hopping exponentials and the shared-memory G of the mixed path
+// enter without any FP64 instruction.  Same arithmetic as mm_df.
+template <bool ADF, bool BDF, bool CDF>
+__device__ __noinline__ void mm_dfx(int n, void* __restrict__ Cv, const void* __restrict__ Av,
+                                    const void* __restrict__ Bv, double* smd) {
+    float* sAh = reinterpret_cast<float*>(smd);  // [16][64]: sAh[kk*64 + m]
+    float* sAl = sAh + 16 * 64;
+    float* sBh = sAl + 16 * 64;                   // [16][64]: sBh[kk*64 + j]
+    float* sBl = sBh + 16 * 64;
+    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
+    for (int n0 = 0; n0 < n; n0 += 64) {
+        for (int m0 = 0; m0 < n; m0 += 64) {
+            float sh[4][4], sl[4][4], xx[4][4];
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) sh[r][q] = sl[r][q] = xx[r][q] = 0.f;
+            for (int k0 = 0; k0 < n; k0 += 16) {
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int e = tid + t * DQMC_NT;
+                    const int mm_ = e & 63, kk = e >> 6;
+                    const int gm = m0 + mm_, gk = k0 + kk;
+                    float2 v = make_float2(0.f, 0.f);
+                    if (gm < n && gk < n) {
+                        const size_t at = gm + (size_t)gk * n;
+                        v = ADF ? static_cast<const float2*>(Av)[at]
+                                : d_to_df(static_cast<const double*>(Av)[at]);
+                    }
+                    sAh[kk * 64 + mm_] = v.x;
+                    sAl[kk * 64 + mm_] = v.y;
+                }
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int e = tid + t * DQMC_NT;
+                    const int kk = e & 15, jj = e >> 4;
+                    const int gk = k0 + kk, gj = n0 + jj;
+                    float2 v = make_float2(0.f, 0.f);
+                    if (gk < n && gj < n) {
+                        const size_t at = gk + (size_t)gj * n;
+                        v = BDF ? static_cast<const float2*>(Bv)[at]
+                                : d_to_df(static_cast<const double*>(Bv)[at]);
+                    }
+                    sBh[kk * 64 + jj] = v.x;
+                    sBl[kk * 64 + jj] = v.y;
+                }
+                __syncthreads();
+#pragma unroll 4
+                for (int kk = 0; kk < 16; ++kk) {
+                    float ah[4], al[4], bh[4], bl[4];
+#pragma unroll
+                    for (int r = 0; r < 4; ++r) {
+                        ah[r] = sAh[kk * 64 + tx + 16 * r];
+                        al[r] = sAl[kk * 64 + tx + 16 * r];
+                    }
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) {
+                        bh[q] = sBh[kk * 64 + ty + 16 * q];
+                        bl[q] = sBl[kk * 64 + ty + 16 * q];
+                    }
+#pragma unroll
+                    for (int r = 0; r < 4; ++r)
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) {
+                            const float p = __fmul_rn(ah[r], bh[q]);
+                            const float pe = __fmaf_rn(ah[r], bh[q], -p);
+                            const float t = __fadd_rn(sh[r][q], p);
+                            const float z = __fsub_rn(t, sh[r][q]);
+                            const float er = __fadd_rn(__fsub_rn(sh[r][q], __fsub_rn(t, z)),
+                                                       __fsub_rn(p, z));
+                            sh[r][q] = t;
+                            sl[r][q] = __fadd_rn(sl[r][q], __fadd_rn(er, pe));
+                            xx[r][q] = __fmaf_rn(ah[r], bl[q], __fmaf_rn(al[r], bh[q], xx[r][q]));
+                        }
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int gm = m0 + tx + 16 * r, gj = n0 + ty + 16 * q;
+                    if (gm < n && gj < n) {
+                        const size_t at = gm + (size_t)gj * n;
+                        if (CDF)
+                            static_cast<float2*>(Cv)[at] =
+                                df_norm(sh[r][q], __fadd_rn(sl[r][q], xx[r][q]));
+                        else
+                            static_cast<double*>(Cv)[at] =
+                                (double)sh[r][q] + ((double)sl[r][q] + (double)xx[r][q]);
+                    }
+                }
+        }
+    }
+}
+
 // udt_AVX_pivot! (UDT.jl:216-334) on one n x n block: Householder QR with
 // column pivoting (column norms recomputed every step, as indmaxcolumn does),
 // explicit Q by backward accumulation, D = |diag R| (0 -> 1), T = D^-1 R
