@@ -5,6 +5,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <string>
 #include <map>
 #include <vector>
@@ -96,6 +97,7 @@ struct dqmc_handle {
     std::map<size_t, size_t> free_blocks;  // offset -> bytes
     std::vector<size_t> slot_off, slot_bytes;
     DqmcChain* pinned = nullptr;           // pinned mirror for graph replays
+    int n_max = 0;                         // largest n_sites of a fixed handle's chains
     cudaGraphExec_t graph = nullptr;
     int graph_budget_us = -1;
 };
@@ -140,7 +142,8 @@ int launch(dqmc_handle* h, int op, int arg0, int arg1, bool sync) {
         int st = push_descriptors(h);
         if (st != DQMC_OK) return st;
     }
-    CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), op, arg0, arg1, h->stream),
+    CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), op, arg0, arg1, h->stream,
+                                      h->pool ? 0 : h->n_max),
              "chain kernel launch");
     if (!sync) {
         h->busy = true;
@@ -270,6 +273,7 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
     h->device = device;
     h->precision = precision;
     h->cfg.assign(chains, chains + n_chains);
+    for (int i = 0; i < n_chains; ++i) h->n_max = std::max(h->n_max, (int)chains[i].n_sites);
     size_t total = 0;
     std::vector<size_t> base(n_chains);
     for (int i = 0; i < n_chains; ++i) {
@@ -533,7 +537,8 @@ static int launch_one(dqmc_handle* h, int chain, int op, int arg0, int arg1) {
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
     if (h->host_dirty) if (int st = push_descriptors(h)) return st;
-    CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains + chain, 1, op, arg0, arg1, h->stream),
+    CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains + chain, 1, op, arg0, arg1, h->stream,
+                                      h->cfg[chain].n_sites),
              "chain kernel launch");
     CUDA_TRY(cudaStreamSynchronize(h->stream), "chain kernel");
     return pull_descriptors(h);
@@ -912,7 +917,7 @@ int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph) {
         CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         cudaError_t e1 = cudaMemcpyAsync(h->d_chains, h->pinned, bytes, cudaMemcpyHostToDevice, h->stream);
         cudaError_t e2 = dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), DQMC_OP_RUN,
-                                                  budget_us, 0, h->stream);
+                                                  budget_us, 0, h->stream, 0);
         cudaError_t e3 = cudaMemcpyAsync(h->pinned, h->d_chains, bytes, cudaMemcpyDeviceToHost, h->stream);
         cudaError_t e4 = cudaStreamEndCapture(h->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {

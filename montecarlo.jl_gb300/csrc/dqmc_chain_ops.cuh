@@ -25,10 +25,14 @@ struct Smem {
     double red[DQMC_NW];
     int sxi[4];
     DqmcChain c;                 // this CTA's chain (state mutated here, written back at exit)
-    double arena[2 * 64 * 65];   // shared-memory QR of one block when n <= 64; between
-                                 // stabilisations of a sweep it holds G (G-resident mode)
     double* Gglob;               // the chain's G in global memory
     int gres;                    // G currently lives in `arena`
+    int arena_cap;               // doubles of `arena` this launch allocated
+    // last member: a launch allocates only the 2 n (n + 1) doubles its chains
+    // use (max over chains with n <= 64).  Shared-memory QR of one or two
+    // blocks when n <= 64; between stabilisations of a sweep it holds G
+    // (G-resident mode).
+    double arena[2 * 64 * 65];
 };
 
 struct Ctx {
@@ -44,7 +48,7 @@ __device__ __forceinline__ double* blk(double* p, const Ctx& x, int b) { return 
 // rank-1 updates and wraps, and moves to global memory while a stabilisation
 // needs the arena for its QR factorisations.
 __device__ __forceinline__ bool g_resident_possible(const Ctx& x) {
-    return x.n <= 64 && (size_t)x.nf * x.nn <= sizeof(x.s->arena) / sizeof(double);
+    return x.n <= 64 && (size_t)x.nf * x.nn <= (size_t)x.s->arena_cap;
 }
 // On a mixed-precision chain with n >= 32 the resident G is double-float
 // (float2 per entry, same bytes): the rank-1 updates and the wraps then run

@@ -715,19 +715,23 @@ struct UdtJob {
 // udt_pivot_sm for the two flavour blocks of a BlockDiagonal matrix at once
 // (UDT.jl:352-370 runs them one after the other; they are independent):
 // threads 0-127 factor block 0, threads 128-255 block 1, each in its own half
-// of `arena` (n <= 64, leading dimension n + 1) with two threads per column;
-// the serial reflector step of the two blocks runs on warps 0 and 5 (different
+// of `arena` (n <= 64, leading dimension n + 1, block g at g n (n + 1)) with
+// two threads per column;
+// the serial reflector step of the two blocks runs on warps 0 and 7 (different
 // SM sub-partitions), so the two latency chains overlap, and Q is accumulated
 // directly in U (global memory) instead of a second shared-memory block.
 // sv: 2 * 64 doubles (block g at g * 64); sxd: 2 doubles.  Same algorithm and
 // pivot rule as udt_pivot_sm.
 __device__ __noinline__ void udt_pivot_sm2(int n, UdtJob j0, UdtJob j1, bool apply,
                                            double* arena, double* sv, double* sxd) {
-    const int tid = threadIdx.x, lane = tid & 31;
-    const int g = tid >> 7, gtid = tid & 127, gwarp = gtid >> 5;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    // block 1 numbers its warps backwards (warp 7 first): when a late step
+    // keeps only the first warps of each block busy, the two blocks' warps
+    // sit on different SM sub-partitions
+    const int g = tid >> 7, gwarp = g ? 7 - warp : warp, gtid = gwarp * 32 + lane;
     const UdtJob J = g ? j1 : j0;
     const int ld = n + 1;
-    double* sIn = arena + (size_t)g * 64 * 65;
+    double* sIn = arena + (size_t)g * n * ld;
     double* svg = sv + g * 64;
     for (int e = gtid; e < n * n; e += 128) sIn[(e % n) + (e / n) * ld] = J.In[e];
     for (int i = gtid; i < n; i += 128) J.piv[i] = i + 1;
@@ -752,7 +756,7 @@ __device__ __noinline__ void udt_pivot_sm2(int n, UdtJob j0, UdtJob j1, bool app
     }
     __syncthreads();
     for (int j = 0; j < n; ++j) {
-        if (gwarp == g) {  // warp 0 for block 0, warp 5 for block 1
+        if (gwarp == 0) {  // warp 0 for block 0, warp 7 for block 1
             long long best = -1;
             int bi = j;  // never out of range, also when every norm is NaN
             for (int col = j + lane; col < n; col += 32) {

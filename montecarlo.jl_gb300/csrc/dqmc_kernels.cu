@@ -11,8 +11,13 @@
 
 namespace dqmc {
 
-__global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, int nchains, int op,
-                                                        int arg0, int arg1) {
+// MINB CTAs per SM: 2 in general (128 registers a thread); 4 for ensembles of
+// small lattices (n <= 32), whose chains are latency-bound and leave the
+// pipes idle, so that twice as many chains share an SM.
+template <int MINB>
+__global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains, int nchains,
+                                                           int op, int arg0, int arg1,
+                                                           int arena_cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem* s = reinterpret_cast<Smem*>(smem_raw);
     if ((int)blockIdx.x >= nchains) return;
@@ -33,6 +38,7 @@ __global__ void __launch_bounds__(DQMC_NT, 2) chain_kernel(DqmcChain* chains, in
     if (threadIdx.x == 0) {
         s->Gglob = s->c.G;
         s->gres = 0;
+        s->arena_cap = arena_cap;
     }
     __syncthreads();
     if (!s->c.active) return;  // free pool slot
@@ -173,8 +179,12 @@ cudaError_t dqmc_prepare_chain_kernel() {
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
     if (!g_attr_set[dev]) {
-        e = cudaFuncSetAttribute(dqmc::chain_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        e = cudaFuncSetAttribute(dqmc::chain_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)sizeof(dqmc::Smem));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dqmc::chain_kernel<4>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)sizeof(dqmc::Smem));
         if (e != cudaSuccess) return e;
         g_attr_set[dev] = true;
     }
@@ -182,10 +192,20 @@ cudaError_t dqmc_prepare_chain_kernel() {
 }
 
 cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
-                                     cudaStream_t stream) {
+                                     cudaStream_t stream, int n_max) {
     cudaError_t e = dqmc_prepare_chain_kernel();
     if (e != cudaSuccess) return e;
-    dqmc::chain_kernel<<<nchains, DQMC_NT, sizeof(dqmc::Smem), stream>>>(d_chains, nchains, op,
-                                                                          arg0, arg1);
+    // arena the chains need: 2 n (n + 1) doubles for the largest n <= 64
+    // (n_max <= 0: unknown, e.g. a pool whose chains change between replays:
+    // the whole arena)
+    const int na = (n_max <= 0 || n_max > 64) ? 64 : n_max;
+    const int cap = 2 * na * (na + 1);
+    const size_t smem = offsetof(dqmc::Smem, arena) + (size_t)cap * sizeof(double);
+    if (n_max > 0 && n_max <= 32)
+        dqmc::chain_kernel<4><<<nchains, DQMC_NT, smem, stream>>>(d_chains, nchains, op, arg0,
+                                                                  arg1, cap);
+    else
+        dqmc::chain_kernel<2><<<nchains, DQMC_NT, smem, stream>>>(d_chains, nchains, op, arg0,
+                                                                  arg1, cap);
     return cudaGetLastError();
 }
