@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define DQMC_GB300_ABI_VERSION 3
+#define DQMC_GB300_ABI_VERSION 4
 
 /* status codes */
 #define DQMC_OK 0
@@ -153,6 +153,17 @@ int dqmc_set_greens(dqmc_handle* h, int chain, const double* in);
 int dqmc_calculate_greens(dqmc_handle* h, int chain, int slice, int safe_mult, double* out);
 /* which: 0 u_stack, 1 t_stack (nf*n*n), 2 d_stack (nf*n); idx 1-based (stack.jl:13-15) */
 int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out);
+/* Replaces: calculate_greens(mc, k, l) / greens(mc, k, l) through the
+ * UnequalTimeStack (unequal_time_stack.jl:124-178, 326-338, 400-697): the
+ * unequal-time G(k, l) = <c(k dtau) c^dagger(l dtau)> of the chain's current
+ * configuration for npairs pairs (0 <= k, l <= M), out: npairs * nf*n*n.
+ * physical = 1 applies the _greens! transform (greens.jl:114-125).  The
+ * forward, backward and inverse stacks are built once per call (the chain's
+ * workspace for them, (4(nr+1) + 2nr + 3) nf n^2 doubles, is allocated on the
+ * first call).  Overwrites the stack scratch Ul..Tr, curr_U, tmp1, tmp2,
+ * pivot and tempv, as the reference's greens(mc, k, l) does. */
+int dqmc_calculate_greens_kl(dqmc_handle* h, int chain, const int32_t* k, const int32_t* l,
+                             int npairs, int physical, double* out);
 
 /* ---- equal-time measurements on the device ----------------------------------
  * Replaces: the measurement step of run! (DQMC.jl:205-222: after every

@@ -70,7 +70,7 @@ EXPORTS = [
     "dqmc_pool_run", "dqmc_pool_slot", "dqmc_pool_free_bytes",
     "dqmc_set_measurements", "dqmc_reset_measurements", "dqmc_get_measurements",
     "dqmc_global_update", "dqmc_set_global_schedule", "dqmc_replica_exchange",
-    "dqmc_get_global_stats",
+    "dqmc_get_global_stats", "dqmc_calculate_greens_kl",
 ]
 
 GLOBAL_FLIP = 0
@@ -129,6 +129,8 @@ def load(path: str = LIB_PATH):
     L.dqmc_set_measurements.argtypes = [P, C.c_int, C.POINTER(MeasureConfig)]
     L.dqmc_reset_measurements.argtypes = [P, C.c_int]
     L.dqmc_global_update.argtypes = [P, C.c_int, C.c_void_p]
+    L.dqmc_calculate_greens_kl.argtypes = [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                           dp]
     L.dqmc_set_global_schedule.argtypes = [P, C.c_int, C.c_int]
     L.dqmc_replica_exchange.argtypes = [P, C.c_void_p, C.c_void_p]
     L.dqmc_get_global_stats.argtypes = [P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]
@@ -318,6 +320,18 @@ class Handle:
             out[name] = (o.mean[k], o.error[k])
             out[name + "_level"] = o.error_level[k]
         return out
+
+    def greens_kl(self, chain, pairs, physical=False):
+        """Unequal-time G(k, l) of the chain's configuration for (k, l) pairs."""
+        cfg = self.cfg(chain)
+        k = np.ascontiguousarray([p[0] for p in pairs], dtype=np.int32)
+        l = np.ascontiguousarray([p[1] for p in pairs], dtype=np.int32)
+        per = cfg.n_flavors * cfg.n_sites * cfg.n_sites
+        buf = np.zeros(len(pairs) * per)
+        check(load().dqmc_calculate_greens_kl(self.h, chain, k.ctypes.data, l.ctypes.data,
+                                              len(pairs), int(bool(physical)), dptr(buf)))
+        return [buf_to_blocks(buf[i * per:(i + 1) * per], cfg.n_flavors, cfg.n_sites)
+                for i in range(len(pairs))]
 
     def global_update(self, kind=GLOBAL_FLIP):
         """One global move of every chain; returns the accepted flags."""

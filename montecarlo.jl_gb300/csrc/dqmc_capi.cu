@@ -98,6 +98,7 @@ struct dqmc_handle {
     std::vector<size_t> slot_off, slot_bytes;
     DqmcChain* pinned = nullptr;           // pinned mirror for graph replays
     int n_max = 0;                         // largest n_sites of a fixed handle's chains
+    std::vector<double*> ut_mem;           // per-chain unequal-time workspaces (lazy)
     cudaGraphExec_t graph = nullptr;
     int graph_budget_us = -1;
 };
@@ -312,6 +313,8 @@ int dqmc_destroy(dqmc_handle* h) {
     cudaSetDevice(h->device);
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->arena) cudaFree(h->arena);
+    for (double* p : h->ut_mem)
+        if (p) cudaFree(p);
     if (h->d_chains) cudaFree(h->d_chains);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->pinned) cudaFreeHost(h->pinned);
@@ -694,6 +697,63 @@ int dqmc_get_measurements(dqmc_handle* h, int chain, dqmc_observables* out, doub
     return DQMC_OK;
 }
 
+/* ---- unequal-time Green's function ------------------------------------------ */
+
+int dqmc_calculate_greens_kl(dqmc_handle* h, int chain, const int32_t* k, const int32_t* l,
+                             int npairs, int physical, double* out) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!k || !l || !out || npairs < 1)
+        return fail(DQMC_ERR_INVALID, "dqmc_calculate_greens_kl: bad arguments");
+    const int M = h->cfg[chain].slices;
+    for (int p = 0; p < npairs; ++p)
+        if (k[p] < 0 || k[p] > M || l[p] < 0 || l[p] > M)
+            return fail(DQMC_ERR_INVALID, "dqmc_calculate_greens_kl: slices out of range 0..M");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    DqmcChain& d = h->host[chain];
+    if (h->ut_mem.size() < h->host.size()) h->ut_mem.resize(h->host.size(), nullptr);
+    if (!h->ut_mem[chain]) {
+        CUDA_TRY(cudaMalloc((void**)&h->ut_mem[chain],
+                            DQMC_UT_DOUBLES(d.n, d.nf, d.nr) * sizeof(double)),
+                 "allocate the unequal-time stack");
+    }
+    const size_t ms = (size_t)d.nf * d.n * d.n;
+    std::vector<int32_t> kl(2 * (size_t)npairs);
+    for (int p = 0; p < npairs; ++p) { kl[2 * p] = k[p]; kl[2 * p + 1] = l[p]; }
+    int32_t* d_pairs = nullptr;
+    double* d_out = nullptr;
+    cudaError_t e = cudaMalloc((void**)&d_pairs, kl.size() * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc((void**)&d_out, ms * npairs * sizeof(double));
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_pairs, kl.data(), kl.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                            h->stream);
+    int st = DQMC_OK;
+    if (e != cudaSuccess) {
+        st = cuda_fail(e, "dqmc_calculate_greens_kl: buffers");
+    } else {
+        d.ut = h->ut_mem[chain];
+        d.ut_pairs = d_pairs;
+        d.ut_out = d_out;
+        h->host_dirty = true;
+        st = launch_one(h, chain, DQMC_OP_GREENS_KL, npairs, physical ? 1 : 0);
+        if (st == DQMC_OK && h->host[chain].status != 0)
+            st = fail(DQMC_ERR_NUMERICAL, "chain " + std::to_string(chain) + " reported status " +
+                                              std::to_string(h->host[chain].status));
+        if (st == DQMC_OK) {
+            e = cudaMemcpyAsync(out, d_out, ms * npairs * sizeof(double), cudaMemcpyDeviceToHost,
+                                h->stream);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+            if (e != cudaSuccess) st = cuda_fail(e, "dqmc_calculate_greens_kl: download");
+        }
+        h->host[chain].ut_pairs = nullptr;
+        h->host[chain].ut_out = nullptr;
+        h->host_dirty = true;
+    }
+    if (d_pairs) cudaFree(d_pairs);
+    if (d_out) cudaFree(d_out);
+    return st;
+}
+
 /* ---- global updates and replica exchange ----------------------------------- */
 
 static int check_between_sweeps(dqmc_handle* h) {
@@ -867,6 +927,10 @@ int dqmc_pool_release(dqmc_handle* h, int slot) {
     if (!h->pool) return fail(DQMC_ERR_INVALID, "dqmc_pool_release: not a pool");
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     pool_free(h, h->slot_off[slot], h->slot_bytes[slot]);
+    if ((size_t)slot < h->ut_mem.size() && h->ut_mem[slot]) {
+        cudaFree(h->ut_mem[slot]);
+        h->ut_mem[slot] = nullptr;
+    }
     memset(&h->host[slot], 0, sizeof(DqmcChain));
     h->cfg[slot] = dqmc_chain_config{};
     h->slot_bytes[slot] = 0;

@@ -79,6 +79,13 @@ struct DqmcChain {
     double r_weight, r_prob;
     int partner, global_kind;
     long long sched_calls;
+    // unequal-time Green's function (unequal_time_stack.jl): the chain's
+    // forward / backward / inverse stacks and work matrices (layout in
+    // ut_layout of dqmc_chain_ops.cuh; NULL until first used), and the (k, l)
+    // pairs and output of the current request
+    double* ut;
+    const int* ut_pairs;
+    double* ut_out;
 };
 
 // Measurement accumulators of one chain (doubles):
@@ -105,7 +112,15 @@ enum { DQMC_OP_SWEEP = 0, DQMC_OP_BUILD = 1, DQMC_OP_GREENS_AT = 2, DQMC_OP_PHYS
        DQMC_OP_BUILD_FWD = 4, DQMC_OP_PROPAGATE = 5, DQMC_OP_SWEEP_SPATIAL = 6,
        DQMC_OP_RUN = 7 /* time-sliced: arg0 = budget in microseconds */,
        DQMC_OP_GLOBAL = 8 /* arg0: 0 GlobalFlip, 1 GlobalShuffle */,
-       DQMC_OP_REPLICA_WEIGHT = 9, DQMC_OP_REPLICA_ACCEPT = 10 };
+       DQMC_OP_REPLICA_WEIGHT = 9, DQMC_OP_REPLICA_ACCEPT = 10,
+       DQMC_OP_GREENS_KL = 11 /* arg0 = number of (k, l) pairs */ };
+
+// doubles of a chain's unequal-time workspace: forward and backward U, T
+// ((nr + 1) each) and inverse U, T (nr each) of nf*n*n, their D vectors, and
+// s.U, s.T, s.greens, s.D
+#define DQMC_UT_DOUBLES(n, nf, nr)                                                   \
+    ((size_t)(nf) * (n) * (n) * (4 * ((nr) + 1) + 2 * (nr) + 3) +                    \
+     (size_t)(nf) * (n) * (2 * ((nr) + 1) + (nr) + 1))
 
 // DqmcChain::prec values (same numbers as DQMC_PREC_* of the C ABI)
 #define DQMC_PREC_FP64_ID 0

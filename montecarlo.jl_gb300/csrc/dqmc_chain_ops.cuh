@@ -1176,3 +1176,296 @@ __device__ void after_sweep(const Ctx& x) {
 
 }  // namespace
 }  // namespace dqmc
+
+namespace dqmc {
+namespace {
+
+// ---- unequal-time Green's function (unequal_time_stack.jl) -----------------
+// calculate_greens(mc, k, l) through the UnequalTimeStack: forward, backward
+// and inverse UDT stacks of the current configuration (build_stack,
+// :124-178), then per (k, l) the inverse block, the forward and backward
+// blocks and the stabilised combination (calculate_greens_full1! / full2!,
+// :536-697).  Overwrites Ul..Tr, tmp1, tmp2, curr_U, pivot and tempv, which
+// are scratch between stabilisations (as the reference documents for
+// greens(mc, k, l)).
+
+struct UtView {
+    double *fu, *ft, *bu, *bt, *iu, *it, *U, *T, *G;
+    double *fd, *bd, *id, *D;
+};
+__device__ UtView ut_view(const Ctx& x) {
+    const size_t ms = (size_t)x.nf * x.nn, vs = (size_t)x.nf * x.n;
+    const int nr = x.c->nr;
+    double* p = x.c->ut;
+    UtView v;
+    v.fu = p; p += ms * (nr + 1);
+    v.ft = p; p += ms * (nr + 1);
+    v.bu = p; p += ms * (nr + 1);
+    v.bt = p; p += ms * (nr + 1);
+    v.iu = p; p += ms * nr;
+    v.it = p; p += ms * nr;
+    v.U = p; p += ms;
+    v.T = p; p += ms;
+    v.G = p; p += ms;
+    v.fd = p; p += vs * (nr + 1);
+    v.bd = p; p += vs * (nr + 1);
+    v.id = p; p += vs * nr;
+    v.D = p;
+    return v;
+}
+__device__ __forceinline__ double* utm(const Ctx& x, double* p, int idx) {
+    return p + (size_t)(idx - 1) * x.nf * x.nn;
+}
+__device__ __forceinline__ double* utv(const Ctx& x, double* p, int idx) {
+    return p + (size_t)(idx - 1) * x.nf * x.n;
+}
+
+__device__ void mm_nt_blocks(const Ctx& x, double* C, double* A, double* B) {
+    for (int b = 0; b < x.nf; ++b) mm<false, true>(x.n, blk(C, x, b), blk(A, x, b), blk(B, x, b), x.s->tiles);
+    __syncthreads();
+}
+__device__ void mm_tn_blocks(const Ctx& x, double* C, double* A, double* B) {
+    for (int b = 0; b < x.nf; ++b) mm<true, false>(x.n, blk(C, x, b), blk(A, x, b), blk(B, x, b), x.s->tiles);
+    __syncthreads();
+}
+__device__ void dleft_blocks(const Ctx& x, double* C, const double* d, double* B) {
+    for (int b = 0; b < x.nf; ++b) dleft(x.n, blk(C, x, b), d + b * x.n, blk(B, x, b));
+    __syncthreads();
+}
+__device__ void rdivp_blocks(const Ctx& x, double* A, double* T, double* O) {
+    if (paired(x)) {
+        rdivp_pair(x, A, T, O);
+        return;
+    }
+    for (int b = 0; b < x.nf; ++b)
+        rdivp(x.n, blk(A, x, b), blk(T, x, b), blk(O, x, b), x.c->pivot + b * x.n, x.nf > 1, x.s->sv);
+}
+// vmaxinv! / vmin! (real.jl:143-170), rvadd! (:123-127), copyto!(A, Diagonal(d))
+__device__ void vmaxinv_v(const Ctx& x, double* v, const double* w) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < x.nf * x.n; i += DQMC_NT) v[i] = 1.0 / fmax(1.0, w[i]);
+    __syncthreads();
+}
+__device__ void vmin_v(const Ctx& x, double* v, const double* w) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < x.nf * x.n; i += DQMC_NT) v[i] = fmin(1.0, w[i]);
+    __syncthreads();
+}
+__device__ void vinv_v(const Ctx& x, double* v) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < x.nf * x.n; i += DQMC_NT) v[i] = 1.0 / v[i];
+    __syncthreads();
+}
+__device__ void mat_add(const Ctx& x, double* A, const double* B) {
+    for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) A[e] += B[e];
+    __syncthreads();
+}
+__device__ void mat_diag(const Ctx& x, double* A, const double* d) {
+    for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) {
+        const int b = e / (int)x.nn, f = e % (int)x.nn, i = f % x.n, j = f / x.n;
+        A[e] = (i == j) ? d[b * x.n + i] : 0.0;
+    }
+    __syncthreads();
+}
+
+// build_stack(mc, ::UnequalTimeStack) (:124-178)
+__device__ __noinline__ void ut_build(const Ctx& x, const UtView& s) {
+    DqmcChain& c = *x.c;
+    const int nr = c.nr, ms = x.nf * (int)x.nn;
+    mat_ident(x, utm(x, s.fu, 1));
+    set_ones(x, utv(x, s.fd, 1));
+    mat_ident(x, utm(x, s.ft, 1));
+    mat_ident(x, utm(x, s.bu, nr + 1));
+    set_ones(x, utv(x, s.bd, nr + 1));
+    mat_ident(x, utm(x, s.bt, nr + 1));
+    __syncthreads();
+    for (int idx = 1; idx <= nr; ++idx) {
+        copy(ms, c.currU, utm(x, s.fu, idx));
+        __syncthreads();
+        for (int sl = c.rfirst[idx - 1]; sl <= c.rlast[idx - 1]; ++sl) slice_left(x, sl, c.currU);
+        dright_blocks(x, c.tmp1, c.currU, utv(x, s.fd, idx));
+        udt_blocks(x, utm(x, s.fu, idx + 1), utv(x, s.fd, idx + 1), c.tmp1, true);
+        mm_blocks(x, utm(x, s.ft, idx + 1), c.tmp1, utm(x, s.ft, idx));
+    }
+    for (int idx = nr; idx >= 1; --idx) {
+        copy(ms, c.currU, utm(x, s.bu, idx + 1));
+        __syncthreads();
+        for (int sl = c.rlast[idx - 1]; sl >= c.rfirst[idx - 1]; --sl) slice_dagger_left(x, sl, c.currU);
+        dright_blocks(x, c.tmp1, c.currU, utv(x, s.bd, idx + 1));
+        udt_blocks(x, utm(x, s.bu, idx), utv(x, s.bd, idx), c.tmp1, true);
+        mm_blocks(x, utm(x, s.bt, idx), c.tmp1, utm(x, s.bt, idx + 1));
+    }
+    for (int idx = 1; idx <= nr; ++idx) {
+        double* it = utm(x, s.it, idx);
+        mat_ident(x, it);
+        __syncthreads();
+        for (int sl = c.rlast[idx - 1]; sl >= c.rfirst[idx - 1]; --sl) slice_inv_left(x, sl, it);
+        udt_blocks(x, utm(x, s.iu, idx), utv(x, s.id, idx), it, true);
+    }
+}
+
+// _find_range_with_value (:354-390): chunk (1-based) holding slice val
+__device__ int find_range(const Ctx& x, int val) {
+    const DqmcChain& c = *x.c;
+    if (val < 1) return 0;
+    if (val > c.rlast[c.nr - 1]) return c.nr + 1;
+    for (int i = 0; i < c.nr; ++i)
+        if (c.rfirst[i] <= val && val <= c.rlast[i]) return i + 1;
+    return c.nr + 1;
+}
+
+// compute_inverse_udt_block! (:400-463): U D T = B_{low+1}^-1 ... B_high^-1
+__device__ __noinline__ void ut_inverse_block(const Ctx& x, const UtView& s, int low, int high) {
+    DqmcChain& c = *x.c;
+    const int ms = x.nf * (int)x.nn;
+    const int lower = find_range(x, low) + 1, upper = find_range(x, high + 1) - 1;
+    mat_ident(x, s.U);
+    set_ones(x, s.D);
+    mat_ident(x, s.T);
+    __syncthreads();
+    for (int idx = lower; idx <= upper; ++idx) {
+        mm_blocks(x, c.tmp1, s.T, utm(x, s.iu, idx));
+        dleft_blocks(x, c.tmp2, s.D, c.tmp1);
+        dright_blocks(x, c.tmp1, c.tmp2, utv(x, s.id, idx));
+        udt_blocks(x, c.tmp2, s.D, c.tmp1, true);
+        mm_blocks(x, s.T, c.tmp1, utm(x, s.it, idx));
+        mm_blocks(x, c.tmp1, s.U, c.tmp2);
+        copy(ms, s.U, c.tmp1);
+        __syncthreads();
+    }
+    const int lower_slice = lower <= c.nr ? c.rfirst[lower - 1] : c.rlast[c.nr - 1] + 1;
+    const int upper_slice = upper > 0 ? c.rlast[upper - 1] : 0;
+    const int top = min(lower_slice - 1, high);
+    for (int sl = top; sl >= low + 1; --sl) slice_inv_left(x, sl, s.U);
+    if (top >= low + 1) {
+        dright_blocks(x, c.tmp1, s.U, s.D);
+        udt_blocks(x, s.U, s.D, c.tmp1, true);
+        mm_blocks(x, c.tmp2, c.tmp1, s.T);
+        copy(ms, s.T, c.tmp2);
+        __syncthreads();
+    }
+    for (int sl = max(upper_slice + 1, top + 1); sl <= high; ++sl) slice_inv_right(x, sl, s.T);
+}
+
+// compute_forward_udt_block! (:474-497): Ul Dl Tl = B_slice ... B_1
+__device__ __noinline__ void ut_forward_block(const Ctx& x, const UtView& s, int slice) {
+    DqmcChain& c = *x.c;
+    const int idx = max(0, find_range(x, slice) - 1);
+    copy(x.nf * (int)x.nn, c.Tl, utm(x, s.fu, idx + 1));
+    __syncthreads();
+    const int target = idx > 0 ? c.rlast[idx - 1] + 1 : 1;
+    for (int l = target; l <= slice; ++l) slice_left(x, l, c.Tl);
+    dright_blocks(x, c.tmp1, c.Tl, utv(x, s.fd, idx + 1));
+    udt_blocks(x, c.Ul, c.Dl, c.tmp1, true);
+    mm_blocks(x, c.Tl, c.tmp1, utm(x, s.ft, idx + 1));
+}
+
+// compute_backward_udt_block! (:509-533): (Ur Dr Tr)^T = B_M ... B_{slice+1}
+__device__ __noinline__ void ut_backward_block(const Ctx& x, const UtView& s, int slice) {
+    DqmcChain& c = *x.c;
+    const int idx = find_range(x, slice) + 1;
+    copy(x.nf * (int)x.nn, c.Ur, utm(x, s.bu, idx));
+    __syncthreads();
+    const int target = idx <= c.nr ? c.rfirst[idx - 1] - 1 : c.rlast[c.nr - 1];
+    for (int l = target; l >= slice + 1; --l) slice_dagger_left(x, l, c.Ur);
+    dright_blocks(x, c.tmp1, c.Ur, utv(x, s.bd, idx));
+    udt_blocks(x, c.Ur, c.Dr, c.tmp1, true);
+    mm_blocks(x, c.Tr, c.tmp1, utm(x, s.bt, idx));
+}
+
+// calculate_greens_full1! (:536-619), slice1 >= slice2
+__device__ __noinline__ void ut_full1(const Ctx& x, const UtView& s, int slice1, int slice2) {
+    DqmcChain& c = *x.c;
+    ut_inverse_block(x, s, slice2, slice1);
+    ut_forward_block(x, s, slice2);
+    ut_backward_block(x, s, slice1);
+    mm_nt_blocks(x, s.G, c.Tl, c.Tr);
+    dright_blocks(x, c.tmp1, s.G, c.Dr);
+    dleft_blocks(x, s.G, c.Dl, c.tmp1);
+    udt_blocks(x, c.Tr, c.Dr, s.G, false);
+    mm_blocks(x, c.Tl, c.Ul, c.Tr);
+    rdivp_blocks(x, c.Ur, s.G, c.Ul);
+    mm_tn_blocks(x, c.Tr, s.U, c.Tl);
+    vmaxinv_v(x, c.Dl, s.D);
+    dleft_blocks(x, c.tmp1, c.Dl, c.Tr);
+    vmin_v(x, c.Dl, c.Dr);
+    dright_blocks(x, c.Tr, c.tmp1, c.Dl);
+    mm_blocks(x, c.Tl, s.T, c.Ur);
+    vmin_v(x, c.Dl, s.D);
+    dleft_blocks(x, c.tmp1, c.Dl, c.Tl);
+    vmaxinv_v(x, c.Dl, c.Dr);
+    dright_blocks(x, c.Tl, c.tmp1, c.Dl);
+    mat_add(x, c.Tl, c.Tr);
+    udt_blocks(x, c.Tr, c.Dl, c.Tl, false);
+    vmaxinv_v(x, c.Dr, c.Dr);
+    mat_diag(x, c.Ul, c.Dr);
+    rdivp_blocks(x, c.Ul, c.Tl, c.tmp1);
+    vinv_v(x, c.Dl);
+    dright_blocks(x, c.tmp1, c.Ul, c.Dl);
+    mm_nt_blocks(x, c.Ul, c.tmp1, c.Tr);
+    vmaxinv_v(x, c.Dl, s.D);
+    dright_blocks(x, s.G, c.Ul, c.Dl);
+    mm_nt_blocks(x, c.Tr, s.G, s.U);
+    mm_blocks(x, s.G, c.Ur, c.Tr);
+}
+
+// calculate_greens_full2! (:621-697), slice1 < slice2
+__device__ __noinline__ void ut_full2(const Ctx& x, const UtView& s, int slice1, int slice2) {
+    DqmcChain& c = *x.c;
+    ut_inverse_block(x, s, slice1, slice2);
+    ut_forward_block(x, s, slice1);
+    ut_backward_block(x, s, slice2);
+    mm_nt_blocks(x, s.G, c.Tl, c.Tr);
+    dleft_blocks(x, c.tmp1, c.Dl, s.G);
+    dright_blocks(x, s.G, c.tmp1, c.Dr);
+    udt_blocks(x, c.Tr, c.Dr, s.G, false);
+    mm_blocks(x, c.Tl, c.Ul, c.Tr);
+    mm_tn_blocks(x, c.Ul, s.U, c.Tl);
+    vmaxinv_v(x, c.Dl, s.D);
+    dleft_blocks(x, s.U, c.Dl, c.Ul);
+    vmin_v(x, c.Dl, c.Dr);
+    dright_blocks(x, c.Ul, s.U, c.Dl);
+    mm_blocks(x, s.U, s.T, c.Ur);
+    rdivp_blocks(x, s.U, s.G, c.Ur);
+    vmin_v(x, c.Dl, s.D);
+    dleft_blocks(x, c.Ur, c.Dl, s.U);
+    vmaxinv_v(x, c.Dl, c.Dr);
+    dright_blocks(x, c.Tr, c.Ur, c.Dl);
+    mat_add(x, c.Tr, c.Ul);
+    udt_blocks(x, c.Ul, c.Dl, c.Tr, false);
+    vmin_v(x, c.Dr, c.Dr);
+    mat_diag(x, s.U, c.Dr);
+    rdivp_blocks(x, s.U, c.Tr, c.Ur);
+    vinv_v(x, c.Dl);
+    dright_blocks(x, c.Ur, s.U, c.Dl);
+    mm_nt_blocks(x, s.U, c.Ur, c.Ul);
+    vmin_v(x, s.D, s.D);
+    dright_blocks(x, c.Ur, s.U, s.D);
+    mm_blocks(x, c.Tr, c.Ur, s.T);
+    mm_blocks(x, s.G, c.Tl, c.Tr);
+    for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) s.G[e] = -s.G[e];
+    __syncthreads();
+}
+
+// OP_GREENS_KL: one stack build, then G(k, l) for each requested pair
+// (physical: the _greens! transform of the result, greens.jl:114-125)
+__device__ __noinline__ void greens_kl(const Ctx& x, int npairs, bool physical) {
+    const DqmcChain& c = *x.c;
+    const UtView s = ut_view(x);
+    ut_build(x, s);
+    const int ms = x.nf * (int)x.nn;
+    for (int p = 0; p < npairs; ++p) {
+        const int k = c.ut_pairs[2 * p], l = c.ut_pairs[2 * p + 1];
+        if (k >= l) ut_full1(x, s, k, l);
+        else ut_full2(x, s, k, l);
+        if (physical) {
+            greens_physical(x, s.G, c.ut_out + (size_t)p * ms);
+        } else {
+            copy(ms, c.ut_out + (size_t)p * ms, s.G);
+            __syncthreads();
+        }
+    }
+}
+
+}  // namespace
+}  // namespace dqmc

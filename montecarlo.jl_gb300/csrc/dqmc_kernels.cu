@@ -134,6 +134,10 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     case DQMC_OP_REPLICA_ACCEPT:
         if (s->c.partner >= 0) replica_accept(x, chains, (int)blockIdx.x);
         break;
+    case DQMC_OP_GREENS_KL:
+        if (s->c.ut && s->c.ut_pairs && s->c.ut_out) greens_kl(x, arg0, arg1 != 0);
+        else if (threadIdx.x == 0) s->c.status = 1;
+        break;
     default:
         break;
     }

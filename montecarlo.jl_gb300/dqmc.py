@@ -102,6 +102,11 @@ class DQMC:
         """greens(mc) (greens.jl:87): the physical equal-time G by default."""
         return self.handle.greens(0, physical=physical)
 
+    def greens_kl(self, k, l, physical=True):
+        """greens(mc, k, l) (unequal_time_stack.jl:309-324): the unequal-time
+        G(k dtau, l dtau); physical (the _greens! transform) by default."""
+        return self.handle.greens_kl(0, [(k, l)], physical=physical)[0]
+
     def calculate_greens(self, slice_, safe_mult=0):
         """calculate_greens(mc, slice) (stack.jl:525-583), effective G."""
         return self.handle.calculate_greens(0, slice_, safe_mult)

@@ -1010,3 +1010,236 @@ double oc_run_chains_threaded(OcChain** chains, int nchains, int nsweeps, int th
     free(th); free(wk);
     return (double)(t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec);
 }
+
+/* ------------------------------------------------- unequal-time Green's function
+ * calculate_greens(mc, k, l) through the UnequalTimeStack
+ * (unequal_time_stack.jl:124-178, 326-338, 354-697), the stacks rebuilt from
+ * the current configuration at every call (the reference rebuilds them when
+ * the configuration has changed since the last call). */
+
+typedef struct {
+    int nr;
+    double *fu, *fd, *ft;   /* forward  B_{n*k} ... B_1, nr+1 entries */
+    double *bu, *bd, *bt;   /* backward B_{n*k+1}^T ... B_M^T, nr+1 entries */
+    double *iu, *id, *it;   /* inverse chunks, nr entries */
+    double *U, *D, *T, *G;  /* s.U, s.D, s.T, s.greens */
+} OcUt;
+
+static OcUt ut_alloc(OcChain* c) {
+    OcUt s;
+    size_t ms = MATSZ(c), vs = (size_t)c->nf * c->n;
+    s.nr = c->nr;
+    s.fu = dalloc(ms * (c->nr + 1)); s.ft = dalloc(ms * (c->nr + 1)); s.fd = dalloc(vs * (c->nr + 1));
+    s.bu = dalloc(ms * (c->nr + 1)); s.bt = dalloc(ms * (c->nr + 1)); s.bd = dalloc(vs * (c->nr + 1));
+    s.iu = dalloc(ms * c->nr); s.it = dalloc(ms * c->nr); s.id = dalloc(vs * c->nr);
+    s.U = dalloc(ms); s.T = dalloc(ms); s.G = dalloc(ms); s.D = dalloc(vs);
+    return s;
+}
+static void ut_free(OcUt* s) {
+    free(s->fu); free(s->ft); free(s->fd); free(s->bu); free(s->bt); free(s->bd);
+    free(s->iu); free(s->it); free(s->id); free(s->U); free(s->T); free(s->G); free(s->D);
+}
+#define UTM(p, c, idx) ((p) + (size_t)((idx) - 1) * MATSZ(c))
+#define UTV(p, c, idx) ((p) + (size_t)((idx) - 1) * (size_t)(c)->nf * (c)->n)
+
+/* build_stack(mc, ::UnequalTimeStack), unequal_time_stack.jl:124-178 */
+static void ut_build(OcChain* c, OcUt* s) {
+    const int nr = c->nr;
+    mat_identity(c, UTM(s->fu, c, 1)); vec_ones(c, UTV(s->fd, c, 1)); mat_identity(c, UTM(s->ft, c, 1));
+    mat_identity(c, UTM(s->bu, c, nr + 1)); vec_ones(c, UTV(s->bd, c, nr + 1));
+    mat_identity(c, UTM(s->bt, c, nr + 1));
+    for (int idx = 1; idx <= nr; ++idx) {
+        mat_copy(c, c->curr_U, UTM(s->fu, c, idx));
+        for (int sl = c->rfirst[idx - 1]; sl <= c->rlast[idx - 1]; ++sl) mult_slice_left(c, sl, c->curr_U);
+        diag_right_blocks(c, c->tmp1, c->curr_U, UTV(s->fd, c, idx));
+        udt_blocks(c, UTM(s->fu, c, idx + 1), UTV(s->fd, c, idx + 1), c->tmp1, 1);
+        gemm_blocks(c, UTM(s->ft, c, idx + 1), c->tmp1, UTM(s->ft, c, idx));
+    }
+    for (int idx = nr; idx >= 1; --idx) {
+        mat_copy(c, c->curr_U, UTM(s->bu, c, idx + 1));
+        for (int sl = c->rlast[idx - 1]; sl >= c->rfirst[idx - 1]; --sl)
+            mult_daggered_slice_left(c, sl, c->curr_U);
+        diag_right_blocks(c, c->tmp1, c->curr_U, UTV(s->bd, c, idx + 1));
+        udt_blocks(c, UTM(s->bu, c, idx), UTV(s->bd, c, idx), c->tmp1, 1);
+        gemm_blocks(c, UTM(s->bt, c, idx), c->tmp1, UTM(s->bt, c, idx + 1));
+    }
+    for (int idx = 1; idx <= nr; ++idx) {
+        double* it = UTM(s->it, c, idx);
+        mat_identity(c, it);
+        for (int sl = c->rlast[idx - 1]; sl >= c->rfirst[idx - 1]; --sl) mult_slice_inv_left(c, sl, it);
+        udt_blocks(c, UTM(s->iu, c, idx), UTV(s->id, c, idx), it, 1);
+    }
+}
+
+/* _find_range_with_value, unequal_time_stack.jl:354-390: 1-based chunk
+ * holding slice val; 0 below, nr + 1 above */
+static int find_range(const OcChain* c, int val) {
+    if (val < 1) return 0;
+    if (val > c->rlast[c->nr - 1]) return c->nr + 1;
+    for (int i = 0; i < c->nr; ++i)
+        if (c->rfirst[i] <= val && val <= c->rlast[i]) return i + 1;
+    return c->nr + 1;
+}
+
+static void gemm_nt_blocks(OcChain* c, double* C, const double* A, const double* B) {
+    for (int b = 0; b < c->nf; ++b) gemm_nt(c->n, C + b * NN(c), A + b * NN(c), B + b * NN(c), c->scratch);
+}
+static void gemm_tn_blocks(OcChain* c, double* C, const double* A, const double* B) {
+    for (int b = 0; b < c->nf; ++b) gemm_tn(c->n, C + b * NN(c), A + b * NN(c), B + b * NN(c), c->scratch);
+}
+static void diag_left_blocks(OcChain* c, double* C, const double* d, const double* B) {
+    for (int b = 0; b < c->nf; ++b) diag_left(c->n, C + b * NN(c), d + b * c->n, B + b * NN(c));
+}
+static void rdivp_blocks(OcChain* c, double* A, const double* T, double* O) {
+    for (int b = 0; b < c->nf; ++b)
+        oc_rdivp(c->n, A + b * NN(c), T + b * NN(c), O + b * NN(c), c->pivot + b * c->n, c->nf > 1);
+}
+static void vmaxinv(OcChain* c, double* v, const double* w) {  /* real.jl:164-170 */
+    for (int i = 0; i < c->nf * c->n; ++i) v[i] = 1.0 / (w[i] > 1.0 ? w[i] : 1.0);
+}
+static void vmin1(OcChain* c, double* v, const double* w) {    /* real.jl:143-149 */
+    for (int i = 0; i < c->nf * c->n; ++i) v[i] = (w[i] < 1.0 ? w[i] : 1.0);
+}
+static void mat_add(OcChain* c, double* A, const double* B) {  /* rvadd!, real.jl:123-127 */
+    for (size_t e = 0; e < MATSZ(c); ++e) A[e] += B[e];
+}
+static void mat_diag(OcChain* c, double* A, const double* d) { /* copyto!(A, Diagonal(d)) */
+    memset(A, 0, MATSZ(c) * sizeof(double));
+    for (int b = 0; b < c->nf; ++b)
+        for (int i = 0; i < c->n; ++i) A[b * NN(c) + (size_t)i * c->n + i] = d[b * c->n + i];
+}
+
+/* compute_inverse_udt_block!, unequal_time_stack.jl:400-463:
+ * U D T = B_{low+1}^-1 ... B_high^-1 */
+static void ut_inverse_block(OcChain* c, OcUt* s, int low, int high) {
+    const int lower = find_range(c, low) + 1, upper = find_range(c, high + 1) - 1;
+    mat_identity(c, s->U); vec_ones(c, s->D); mat_identity(c, s->T);
+    for (int idx = lower; idx <= upper; ++idx) {
+        gemm_blocks(c, c->tmp1, s->T, UTM(s->iu, c, idx));
+        diag_left_blocks(c, c->tmp2, s->D, c->tmp1);
+        diag_right_blocks(c, c->tmp1, c->tmp2, UTV(s->id, c, idx));
+        udt_blocks(c, c->tmp2, s->D, c->tmp1, 1);
+        gemm_blocks(c, s->T, c->tmp1, UTM(s->it, c, idx));
+        gemm_blocks(c, c->tmp1, s->U, c->tmp2);
+        mat_copy(c, s->U, c->tmp1);
+    }
+    const int lower_slice = lower <= c->nr ? c->rfirst[lower - 1] : c->rlast[c->nr - 1] + 1;
+    const int upper_slice = upper > 0 ? c->rlast[upper - 1] : 0;
+    const int top = (lower_slice - 1 < high) ? lower_slice - 1 : high;
+    for (int sl = top; sl >= low + 1; --sl) mult_slice_inv_left(c, sl, s->U);
+    if (top >= low + 1) {
+        diag_right_blocks(c, c->tmp1, s->U, s->D);
+        udt_blocks(c, s->U, s->D, c->tmp1, 1);
+        gemm_blocks(c, c->tmp2, c->tmp1, s->T);
+        mat_copy(c, s->T, c->tmp2);
+    }
+    const int from = (upper_slice + 1 > top + 1) ? upper_slice + 1 : top + 1;
+    for (int sl = from; sl <= high; ++sl) mult_slice_inv_right(c, sl, s->T);
+}
+
+/* compute_forward_udt_block!, :474-497: Ul Dl Tl = B_slice ... B_1 */
+static void ut_forward_block(OcChain* c, OcUt* s, int slice) {
+    int idx = find_range(c, slice) - 1;
+    if (idx < 0) idx = 0;
+    mat_copy(c, c->Tl, UTM(s->fu, c, idx + 1));
+    const int target = idx > 0 ? c->rlast[idx - 1] + 1 : 1;
+    for (int l = target; l <= slice; ++l) mult_slice_left(c, l, c->Tl);
+    diag_right_blocks(c, c->tmp1, c->Tl, UTV(s->fd, c, idx + 1));
+    udt_blocks(c, c->Ul, c->Dl, c->tmp1, 1);
+    gemm_blocks(c, c->Tl, c->tmp1, UTM(s->ft, c, idx + 1));
+}
+
+/* compute_backward_udt_block!, :509-533: (Ur Dr Tr)^T = B_M ... B_{slice+1} */
+static void ut_backward_block(OcChain* c, OcUt* s, int slice) {
+    const int idx = find_range(c, slice) + 1;
+    mat_copy(c, c->Ur, UTM(s->bu, c, idx));
+    const int target = idx <= c->nr ? c->rfirst[idx - 1] - 1 : c->rlast[c->nr - 1];
+    for (int l = target; l >= slice + 1; --l) mult_daggered_slice_left(c, l, c->Ur);
+    diag_right_blocks(c, c->tmp1, c->Ur, UTV(s->bd, c, idx));
+    udt_blocks(c, c->Ur, c->Dr, c->tmp1, 1);
+    gemm_blocks(c, c->Tr, c->tmp1, UTM(s->bt, c, idx));
+}
+
+/* calculate_greens_full1!, :536-619 (slice1 >= slice2) */
+static void ut_full1(OcChain* c, OcUt* s, int slice1, int slice2) {
+    ut_inverse_block(c, s, slice2, slice1);
+    ut_forward_block(c, s, slice2);
+    ut_backward_block(c, s, slice1);
+    gemm_nt_blocks(c, s->G, c->Tl, c->Tr);
+    diag_right_blocks(c, c->tmp1, s->G, c->Dr);
+    diag_left_blocks(c, s->G, c->Dl, c->tmp1);
+    udt_blocks(c, c->Tr, c->Dr, s->G, 0);
+    gemm_blocks(c, c->Tl, c->Ul, c->Tr);
+    rdivp_blocks(c, c->Ur, s->G, c->Ul);
+    gemm_tn_blocks(c, c->Tr, s->U, c->Tl);
+    vmaxinv(c, c->Dl, s->D);
+    diag_left_blocks(c, c->tmp1, c->Dl, c->Tr);
+    vmin1(c, c->Dl, c->Dr);
+    diag_right_blocks(c, c->Tr, c->tmp1, c->Dl);
+    gemm_blocks(c, c->Tl, s->T, c->Ur);
+    vmin1(c, c->Dl, s->D);
+    diag_left_blocks(c, c->tmp1, c->Dl, c->Tl);
+    vmaxinv(c, c->Dl, c->Dr);
+    diag_right_blocks(c, c->Tl, c->tmp1, c->Dl);
+    mat_add(c, c->Tl, c->Tr);
+    udt_blocks(c, c->Tr, c->Dl, c->Tl, 0);
+    vmaxinv(c, c->Dr, c->Dr);
+    mat_diag(c, c->Ul, c->Dr);
+    rdivp_blocks(c, c->Ul, c->Tl, c->tmp1);
+    for (int i = 0; i < c->nf * c->n; ++i) c->Dl[i] = 1.0 / c->Dl[i];
+    diag_right_blocks(c, c->tmp1, c->Ul, c->Dl);
+    gemm_nt_blocks(c, c->Ul, c->tmp1, c->Tr);
+    vmaxinv(c, c->Dl, s->D);
+    diag_right_blocks(c, s->G, c->Ul, c->Dl);
+    gemm_nt_blocks(c, c->Tr, s->G, s->U);
+    gemm_blocks(c, s->G, c->Ur, c->Tr);
+}
+
+/* calculate_greens_full2!, :621-697 (slice1 < slice2) */
+static void ut_full2(OcChain* c, OcUt* s, int slice1, int slice2) {
+    ut_inverse_block(c, s, slice1, slice2);
+    ut_forward_block(c, s, slice1);
+    ut_backward_block(c, s, slice2);
+    gemm_nt_blocks(c, s->G, c->Tl, c->Tr);
+    diag_left_blocks(c, c->tmp1, c->Dl, s->G);
+    diag_right_blocks(c, s->G, c->tmp1, c->Dr);
+    udt_blocks(c, c->Tr, c->Dr, s->G, 0);
+    gemm_blocks(c, c->Tl, c->Ul, c->Tr);
+    gemm_tn_blocks(c, c->Ul, s->U, c->Tl);
+    vmaxinv(c, c->Dl, s->D);
+    diag_left_blocks(c, s->U, c->Dl, c->Ul);
+    vmin1(c, c->Dl, c->Dr);
+    diag_right_blocks(c, c->Ul, s->U, c->Dl);
+    gemm_blocks(c, s->U, s->T, c->Ur);
+    rdivp_blocks(c, s->U, s->G, c->Ur);
+    vmin1(c, c->Dl, s->D);
+    diag_left_blocks(c, c->Ur, c->Dl, s->U);
+    vmaxinv(c, c->Dl, c->Dr);
+    diag_right_blocks(c, c->Tr, c->Ur, c->Dl);
+    mat_add(c, c->Tr, c->Ul);
+    udt_blocks(c, c->Ul, c->Dl, c->Tr, 0);
+    vmin1(c, c->Dr, c->Dr);
+    mat_diag(c, s->U, c->Dr);
+    rdivp_blocks(c, s->U, c->Tr, c->Ur);
+    for (int i = 0; i < c->nf * c->n; ++i) c->Dl[i] = 1.0 / c->Dl[i];
+    diag_right_blocks(c, c->Ur, s->U, c->Dl);
+    gemm_nt_blocks(c, s->U, c->Ur, c->Ul);
+    vmin1(c, s->D, s->D);
+    diag_right_blocks(c, c->Ur, s->U, s->D);
+    gemm_blocks(c, c->Tr, c->Ur, s->T);
+    gemm_blocks(c, s->G, c->Tl, c->Tr);
+    for (size_t e = 0; e < MATSZ(c); ++e) s->G[e] = -s->G[e];
+}
+
+/* calculate_greens(mc, slice1, slice2), :326-338: the effective G(k, l) for
+ * npairs pairs (one stack build) */
+void oc_greens_kl(OcChain* c, const int* k, const int* l, int npairs, double* out) {
+    OcUt s = ut_alloc(c);
+    ut_build(c, &s);
+    for (int p = 0; p < npairs; ++p) {
+        if (k[p] >= l[p]) ut_full1(c, &s, k[p], l[p]);
+        else ut_full2(c, &s, k[p], l[p]);
+        memcpy(out + (size_t)p * MATSZ(c), s.G, MATSZ(c) * sizeof(double));
+    }
+    ut_free(&s);
+}

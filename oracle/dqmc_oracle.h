@@ -94,6 +94,11 @@ void oc_replica_accept(OcChain* c, const int8_t* partner_conf);
 double oc_local_move_to(OcChain* c, int i, int x_new);
 void oc_get_global_stats(const OcChain* c, long* accepted, long* proposals);
 
+/* calculate_greens(mc, k, l) (unequal_time_stack.jl:326-338, 536-697): the
+ * effective unequal-time G(k, l) for npairs (k, l) pairs, 0 <= k, l <= M,
+ * into out (npairs * nf*n*n) */
+void oc_greens_kl(OcChain* c, const int* k, const int* l, int npairs, double* out);
+
 /* stand-alone linalg kernels for unit tests */
 /* udt_AVX_pivot!, UDT.jl:216-309 (one n x n block) */
 void oc_udt_pivot(int n, double* U, double* D, double* input, int64_t* pivot,

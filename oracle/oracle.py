@@ -106,6 +106,7 @@ def lib():
         L.oc_local_move_to.argtypes = [P, C.c_int, C.c_int]
         L.oc_local_move_to.restype = C.c_double
         L.oc_get_global_stats.argtypes = [P, C.POINTER(C.c_long), C.POINTER(C.c_long)]
+        L.oc_greens_kl.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int, dp]
         L.oc_run_chains_threaded.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
         L.oc_run_chains_threaded.restype = C.c_double
         _lib = L
@@ -277,6 +278,16 @@ class OracleChain:
 
     def local_move_to(self, i, x_new):
         return lib().oc_local_move_to(self.h, int(i), int(x_new))
+
+    def greens_kl(self, pairs):
+        """Effective unequal-time G(k, l) for a list of (k, l) pairs."""
+        k = np.ascontiguousarray([p[0] for p in pairs], dtype=np.int32)
+        l = np.ascontiguousarray([p[1] for p in pairs], dtype=np.int32)
+        buf = np.zeros(len(pairs) * self.nf * self.n * self.n)
+        lib().oc_greens_kl(self.h, k.ctypes.data, l.ctypes.data, len(pairs), _dp(buf))
+        per = self.nf * self.n * self.n
+        return [self._buf_to_blocks(buf[i * per:(i + 1) * per], self.nf, self.n)
+                for i in range(len(pairs))]
 
     def global_stats(self):
         a, p = C.c_long(), C.c_long()

@@ -1,0 +1,61 @@
+"""Unequal-time Green's function G(k, l) (calculate_greens(mc, k, l) through
+the UnequalTimeStack) on the GPU against the oracle, FP64, 1e-10."""
+import numpy as np
+import pytest
+
+from _util import FIELD_U, chain_config, make_setup, maxdiff, oracle_chain
+
+pytestmark = pytest.mark.gpu
+
+TOL_G = 1e-10
+
+
+@pytest.mark.parametrize("L,field,beta,k", [(4, "DensityHirschField", 2.0, 5),
+                                            (4, "MagneticHirschField", 2.0, 5),
+                                            (8, "MagneticHirschField", 2.0, 10),
+                                            (3, "MagneticGHQField", 1.5, 4),
+                                            (10, "DensityHirschField", 1.0, 5)])
+def test_greens_kl_matches_oracle(pkg, lib, oracle, L, field, beta, k):
+    model, param, fld, exps = make_setup(pkg, L=L, U=FIELD_U[field], beta=beta, safe_mult=k,
+                                         field=getattr(pkg, field))
+    h = lib.Handle([chain_config(lib, model, param, fld, 17)])
+    h.set_hopping(-1, exps)
+    h.init_random_field(0)
+    h.initialize_run()
+    h.sweep(1)
+    o = oracle_chain(oracle, model, param, fld, exps, 17)
+    o.set_conf(h.get_field(0))
+    M = param.slices
+    pairs = [(0, 0), (M, M), (3, 0), (0, 3), (M - 1, 2), (2, M - 1), (M, 0), (0, M), (7, 7),
+             (M // 2, M // 3)]
+    g_gpu = h.greens_kl(0, pairs)
+    g_cpu = o.greens_kl(pairs)
+    for p, a, b in zip(pairs, g_gpu, g_cpu):
+        assert maxdiff(a, b) < TOL_G, (p, maxdiff(a, b))
+    # physical form and equal-time consistency on the GPU itself
+    gp = h.greens_kl(0, [(4, 4)], physical=True)[0]
+    eq = h.calculate_greens(0, 4)
+    assert maxdiff(h.greens_kl(0, [(4, 4)])[0], eq) < 1e-12
+    assert maxdiff(gp, o.greens_physical(o.calculate_greens_at(4))) < TOL_G
+
+
+def test_greens_kl_does_not_disturb_the_chain(pkg, lib, oracle):
+    """Sweeps after an unequal-time request replay the oracle exactly."""
+    model, param, fld, exps = make_setup(pkg, L=4, U=-4.0, beta=2.0, safe_mult=5,
+                                         field=pkg.MagneticHirschField)
+    h = lib.Handle([chain_config(lib, model, param, fld, 23)])
+    h.set_hopping(-1, exps)
+    h.init_random_field(0)
+    h.initialize_run()
+    o = oracle_chain(oracle, model, param, fld, exps, 23)
+    o.init_random_conf()
+    o.initialize_run()
+    h.sweep(1)
+    o.sweeps(1)
+    h.greens_kl(0, [(5, 1), (1, 5)])
+    h.sweep(1)
+    o.sweeps(1)
+    assert np.array_equal(h.get_field(0), o.get_conf())
+    assert maxdiff(h.greens(0), o.greens()) < TOL_G
+    with pytest.raises(lib.DQMCError):
+        h.greens_kl(0, [(param.slices + 1, 0)])

@@ -268,3 +268,56 @@ def test_global_flip_and_shuffle_keep_stack_consistent(oracle, pkg, field):
         o.sweeps(1)
     assert o.global_stats() == (n_acc, 12)
     assert o.analysis()["propagation_error_reported"] < 1e-6
+
+
+def _slice_B(exps, fld_kind, alpha, conf_col, nf, n):
+    """B_l = exp(-dtau T) exp(V_l) per flavour block (the slice matrix of
+    multiply_slice_matrix_left!, stack.jl:319-327)."""
+    eT2 = np.asarray(exps[0])
+    s = conf_col.astype(float)
+    if fld_kind in (0, 1):
+        v = [np.exp(alpha * s), np.exp(-alpha * s)]
+    else:
+        eta = np.array([-np.sqrt(6 + 2 * np.sqrt(6)), -np.sqrt(6 - 2 * np.sqrt(6)),
+                        np.sqrt(6 - 2 * np.sqrt(6)), np.sqrt(6 + 2 * np.sqrt(6))])
+        e = eta[conf_col.astype(int) - 1]
+        v = [np.exp(alpha * e), np.exp(-alpha * e)]
+    return [eT2 @ np.diag(v[b]) for b in range(nf)]
+
+
+@pytest.mark.parametrize("field", ["DensityHirschField", "MagneticHirschField", "MagneticGHQField"])
+def test_unequal_time_greens_known_answers(oracle, pkg, field):
+    """The reference's unequal-time checks (test/DQMC/unequal_time_stack.jl:84-103):
+    G(k, k) equals the equal-time G, G(k, 0) = -G(k, M); and the defining
+    relations G(k, l) = B_k...B_{l+1} G(l) (k > l), G(k, l) = -(1 - G(k))
+    (B_l...B_{k+1})^-1 (k < l) on a short chain."""
+    model, param, fld, exps = make_setup(pkg, L=2, U=FIELD_U[field], beta=1.2, safe_mult=4,
+                                         field=getattr(pkg, field))
+    o = oracle_chain(oracle, model, param, fld, exps, 12)
+    o.init_random_conf()
+    o.initialize_run()
+    M = param.slices
+    pairs = [(k, k) for k in range(M + 1)] + [(k, 0) for k in range(M)] + \
+            [(k, M) for k in range(M)] + [(7, 2), (2, 7), (11, 4), (3, 9), (M, 1), (0, M)]
+    G = dict(zip(pairs, o.greens_kl(pairs)))
+    eq = {k: o.calculate_greens_at(k) for k in range(M + 1)}
+    for k in range(M + 1):
+        assert maxdiff(G[(k, k)], eq[k]) < 1e-12, k
+    for k in range(M):
+        assert maxdiff(G[(k, 0)], -G[(k, M)]) < 1e-12, k
+    conf = o.get_conf()
+    nf, n = fld.unique_flavors, 4
+    Bs = [None] + [_slice_B(exps, fld.kind, fld.alpha, conf[:, t - 1], nf, n) for t in range(1, M + 1)]
+    for (k, l) in [(7, 2), (11, 4), (M, 1)]:
+        for b in range(nf):
+            P = np.eye(n)
+            for t in range(l + 1, k + 1):
+                P = Bs[t][b] @ P
+            assert maxdiff(G[(k, l)][b], P @ eq[l][b]) < 1e-10, (k, l)
+    for (k, l) in [(2, 7), (3, 9), (0, M)]:
+        for b in range(nf):
+            P = np.eye(n)
+            for t in range(k + 1, l + 1):
+                P = Bs[t][b] @ P
+            ref = -(np.eye(n) - eq[k][b]) @ np.linalg.inv(P)
+            assert maxdiff(G[(k, l)][b], ref) < 1e-10, (k, l)
