@@ -37,7 +37,7 @@
 extern "C" {
 #endif
 
-#define DQMC_GB300_ABI_VERSION 4
+#define DQMC_GB300_ABI_VERSION 5
 
 /* status codes */
 #define DQMC_OK 0
@@ -208,6 +208,21 @@ int dqmc_reset_measurements(dqmc_handle* h, int chain);
  * greens (n_flavors*n*n physical G, or NULL) receive the means of those. */
 int dqmc_get_measurements(dqmc_handle* h, int chain, dqmc_observables* out, double* occupation,
                           double* greens);
+
+/* ---- checkerboard decomposition -------------------------------------------------
+ * Replaces: DQMCParameters(checkerboard = true) (stack.jl:240-246,
+ * linalg/checkerboard.jl:14-473): the hopping exponentials as products of
+ * site-disjoint bond factors, applied in O(n^2) per factor instead of a dense
+ * O(n^3) product.  Factor m (0 exp(-dtau T), 1 exp(+dtau T), 2 exp(-dtau T/2),
+ * 3 exp(+dtau T/2)) is X = P_1 ... P_N D with N = n_parts; data holds, per
+ * factor, D[n] then per part c[n] (cosh of the bond or 1), s[n] (sinh or 0)
+ * and partner[n] (the bond's other site, -1: none).  The decomposition
+ * (build_checkerboard's bond groups) is the host's: the Python package
+ * builds it as the reference does.  n_parts < 0 returns to the dense
+ * exponentials; chain = -1: all chains (same n_sites).  A chain with
+ * checkerboard factors computes its slice products in FP64 on every
+ * precision. */
+int dqmc_set_checkerboard(dqmc_handle* h, int chain, int n_parts, const double* data);
 
 /* ---- global updates and replica exchange -------------------------------------
  * Replaces: update(::GlobalFlip / ::GlobalShuffle, mc, model, field)

@@ -70,7 +70,7 @@ EXPORTS = [
     "dqmc_pool_run", "dqmc_pool_slot", "dqmc_pool_free_bytes",
     "dqmc_set_measurements", "dqmc_reset_measurements", "dqmc_get_measurements",
     "dqmc_global_update", "dqmc_set_global_schedule", "dqmc_replica_exchange",
-    "dqmc_get_global_stats", "dqmc_calculate_greens_kl",
+    "dqmc_get_global_stats", "dqmc_calculate_greens_kl", "dqmc_set_checkerboard",
 ]
 
 GLOBAL_FLIP = 0
@@ -129,6 +129,7 @@ def load(path: str = LIB_PATH):
     L.dqmc_set_measurements.argtypes = [P, C.c_int, C.POINTER(MeasureConfig)]
     L.dqmc_reset_measurements.argtypes = [P, C.c_int]
     L.dqmc_global_update.argtypes = [P, C.c_int, C.c_void_p]
+    L.dqmc_set_checkerboard.argtypes = [P, C.c_int, C.c_int, dp]
     L.dqmc_calculate_greens_kl.argtypes = [P, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                            dp]
     L.dqmc_set_global_schedule.argtypes = [P, C.c_int, C.c_int]
@@ -320,6 +321,14 @@ class Handle:
             out[name] = (o.mean[k], o.error[k])
             out[name + "_level"] = o.error_level[k]
         return out
+
+    def set_checkerboard(self, chain, data=None, n_parts=-1):
+        """Checkerboard factors (model.checkerboard_pack); None: dense."""
+        if data is None:
+            check(load().dqmc_set_checkerboard(self.h, chain, -1, None))
+            return
+        buf = np.ascontiguousarray(data, dtype=np.float64)
+        check(load().dqmc_set_checkerboard(self.h, chain, int(n_parts), dptr(buf)))
 
     def greens_kl(self, chain, pairs, physical=False):
         """Unequal-time G(k, l) of the chain's configuration for (k, l) pairs."""

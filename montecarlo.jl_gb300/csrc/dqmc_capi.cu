@@ -2,6 +2,7 @@
 // device-memory management, host-side tables, launches and error reporting.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <cmath>
 #include <stdio.h>
 #include <string.h>
 
@@ -99,6 +100,7 @@ struct dqmc_handle {
     DqmcChain* pinned = nullptr;           // pinned mirror for graph replays
     int n_max = 0;                         // largest n_sites of a fixed handle's chains
     std::vector<double*> ut_mem;           // per-chain unequal-time workspaces (lazy)
+    std::vector<double*> cb_mem;           // per-chain checkerboard factors
     cudaGraphExec_t graph = nullptr;
     int graph_budget_us = -1;
 };
@@ -314,6 +316,8 @@ int dqmc_destroy(dqmc_handle* h) {
     if (h->stream) cudaStreamSynchronize(h->stream);
     if (h->arena) cudaFree(h->arena);
     for (double* p : h->ut_mem)
+        if (p) cudaFree(p);
+    for (double* p : h->cb_mem)
         if (p) cudaFree(p);
     if (h->d_chains) cudaFree(h->d_chains);
     if (h->graph) cudaGraphExecDestroy(h->graph);
@@ -697,6 +701,58 @@ int dqmc_get_measurements(dqmc_handle* h, int chain, dqmc_observables* out, doub
     return DQMC_OK;
 }
 
+/* ---- checkerboard decomposition ---------------------------------------------- */
+
+int dqmc_set_checkerboard(dqmc_handle* h, int chain, int n_parts, const double* data) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    int lo = chain, hi = chain + 1;
+    if (chain == -1) { lo = 0; hi = (int)h->cfg.size(); }
+    else if (int st = check_chain(h, chain)) return st;
+    if (n_parts > DQMC_CB_MAXPARTS)
+        return fail(DQMC_ERR_INVALID, "dqmc_set_checkerboard: more than 12 parts");
+    if (n_parts >= 0 && !data) return fail(DQMC_ERR_INVALID, "dqmc_set_checkerboard: null data");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    if (h->cb_mem.size() < h->host.size()) h->cb_mem.resize(h->host.size(), nullptr);
+    for (int i = lo; i < hi; ++i) {
+        DqmcChain& d = h->host[i];
+        if (!d.active) continue;
+        if (n_parts < 0) {  // back to the dense exponentials
+            d.cb = nullptr;
+            d.cb_np = 0;
+            continue;
+        }
+        const int n = d.n;
+        if (chain == -1 && n != h->host[lo].n)
+            return fail(DQMC_ERR_INVALID, "dqmc_set_checkerboard(-1): chains have different n_sites");
+        const size_t per = (size_t)n * (1 + 3 * (size_t)n_parts), cnt = 4 * per;
+        for (size_t m = 0; m < 4; ++m) {
+            const double* f = data + m * per;
+            for (size_t e = 0; e < per; ++e)
+                if (!std::isfinite(f[e]))
+                    return fail(DQMC_ERR_INVALID, "dqmc_set_checkerboard: non-finite entry");
+            for (int p = 0; p < n_parts; ++p) {
+                const double* pt = f + n + (size_t)p * 3 * n + 2 * n;
+                for (int k = 0; k < n; ++k) {
+                    const double q = pt[k];
+                    if (!(q == -1.0 || (q >= 0.0 && q < n && q == (double)(int)q)))
+                        return fail(DQMC_ERR_INVALID, "dqmc_set_checkerboard: partner out of range");
+                }
+            }
+        }
+        if (h->cb_mem[i]) { cudaFree(h->cb_mem[i]); h->cb_mem[i] = nullptr; }
+        CUDA_TRY(cudaMalloc((void**)&h->cb_mem[i], cnt * sizeof(double)), "allocate checkerboard factors");
+        CUDA_TRY(cudaMemcpyAsync(h->cb_mem[i], data, cnt * sizeof(double), cudaMemcpyHostToDevice,
+                                 h->stream),
+                 "upload checkerboard factors");
+        CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+        d.cb = h->cb_mem[i];
+        d.cb_np = n_parts;
+    }
+    h->host_dirty = true;
+    return DQMC_OK;
+}
+
 /* ---- unequal-time Green's function ------------------------------------------ */
 
 int dqmc_calculate_greens_kl(dqmc_handle* h, int chain, const int32_t* k, const int32_t* l,
@@ -930,6 +986,10 @@ int dqmc_pool_release(dqmc_handle* h, int slot) {
     if ((size_t)slot < h->ut_mem.size() && h->ut_mem[slot]) {
         cudaFree(h->ut_mem[slot]);
         h->ut_mem[slot] = nullptr;
+    }
+    if ((size_t)slot < h->cb_mem.size() && h->cb_mem[slot]) {
+        cudaFree(h->cb_mem[slot]);
+        h->cb_mem[slot] = nullptr;
     }
     memset(&h->host[slot], 0, sizeof(DqmcChain));
     h->cfg[slot] = dqmc_chain_config{};

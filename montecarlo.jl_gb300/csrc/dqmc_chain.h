@@ -86,7 +86,14 @@ struct DqmcChain {
     double* ut;
     const int* ut_pairs;
     double* ut_out;
+    // checkerboard = true (stack.jl:240-246, linalg/checkerboard.jl): parts
+    // per factor and the four factors exp(-dtau T), exp(+dtau T),
+    // exp(-dtau T/2), exp(+dtau T/2), each D[n] then per part c[n], s[n],
+    // partner[n] (-1: none); NULL: the dense exponentials
+    int cb_np, pad3;
+    const double* cb;
 };
+#define DQMC_CB_MAXPARTS 12
 
 // Measurement accumulators of one chain (doubles):
 //   [0] measurements taken, [1..3] unused

@@ -55,7 +55,7 @@ __device__ __forceinline__ bool g_resident_possible(const Ctx& x) {
 // entirely on the FP32 pipe; it is rounded back to FP64 whenever it leaves
 // shared memory.  (At n = 16 the split arithmetic costs more than it saves.)
 __device__ __forceinline__ bool df_mode(const Ctx& x) {
-    return x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 32;
+    return x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 32 && !x.c->cb;
 }
 __device__ __forceinline__ bool df_resident(const Ctx& x) { return df_mode(x) && x.s->gres; }
 __device__ __forceinline__ float2* arena_df(const Ctx& x) {
@@ -140,6 +140,62 @@ __device__ __forceinline__ void smm(const Ctx& x, bool wrap, double* C, const do
     }
 }
 
+// Checkerboard products (linalg/checkerboard.jl:272-473) on one flavour
+// block.  Factor m (0 exp(-dtau T), 1 exp(+dtau T), 2 exp(-dtau T/2),
+// 3 exp(+dtau T/2)) is X = P_1 ... P_N D; mode 0: out = X in, 1: out = in X,
+// 2: out = X^T in = D P_N ... P_1 in.  One pass per part: row (mode 1: column)
+// i becomes c_i times itself plus s_i times its partner's, D fused into the
+// first (mode 0) or last (modes 1, 2) pass.  Passes alternate between out and
+// scr so that the last lands in out; in must differ from out and scr.
+// O(n^2) per part instead of the dense product's O(n^3), FP64 on every chain.
+__device__ __noinline__ void cb_apply(const Ctx& x, int m, int mode, double* out,
+                                      const double* in, double* scr) {
+    const DqmcChain& c = *x.c;
+    const int n = x.n, np = c.cb_np;
+    const double* D = c.cb + (size_t)m * n * (1 + 3 * (size_t)np);
+    const double* P = D + n;
+    if (np == 0) {
+        for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
+            const int i = e % n, k = e / n;
+            out[e] = (mode == 1) ? in[e] * D[k] : D[i] * in[e];
+        }
+        __syncthreads();
+        return;
+    }
+    const double* src = in;
+    for (int step = 0; step < np; ++step) {
+        const int part = (mode == 0) ? np - 1 - step : step;
+        const double* cc = P + (size_t)part * 3 * n;
+        const double* ss = cc + n;
+        const double* pt = ss + n;
+        const bool first = (step == 0), last = (step == np - 1);
+        double* dst = ((np - 1 - step) & 1) ? scr : out;
+        for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
+            const int i = e % n, k = e / n;
+            double y;
+            if (mode == 1) {
+                const int q = (int)pt[k];
+                const double v = src[e];
+                y = (q >= 0) ? fma(src[i + (size_t)q * n], ss[k], v * cc[k]) : v;
+                if (last) y = y * D[k];
+            } else {
+                const int q = (int)pt[i];
+                double v = src[e];
+                double w = (q >= 0) ? src[q + (size_t)k * n] : 0.0;
+                if (mode == 0 && first) {
+                    v = D[i] * v;
+                    if (q >= 0) w = D[q] * w;
+                }
+                y = (q >= 0) ? fma(ss[i], w, cc[i] * v) : v;
+                if (mode == 2 && last) y = D[i] * y;
+            }
+            dst[e] = y;
+        }
+        __syncthreads();
+        src = dst;
+    }
+}
+
 // interaction_matrix_exp! (fields.jl:380-386, 429-438, 548-560, 618-624)
 // into shared memory: ev[b*n + i]
 __device__ __noinline__ void interaction_exp(const Ctx& x, int slice, bool inverse) {
@@ -160,7 +216,10 @@ __device__ __noinline__ void slice_left(const Ctx& x, int slice, double* M, bool
     for (int b = 0; b < x.nf; ++b) {
         dleft(x.n, blk(x.c->tmp1, x, b), x.s->ev + b * x.n, blk(M, x, b));
         __syncthreads();
-        smm<true, false>(x, wrap, blk(M, x, b), x.c->eT2, blk(x.c->tmp1, x, b));
+        if (x.c->cb)
+            cb_apply(x, 0, 0, blk(M, x, b), blk(x.c->tmp1, x, b), blk(x.c->tmp2, x, b));
+        else
+            smm<true, false>(x, wrap, blk(M, x, b), x.c->eT2, blk(x.c->tmp1, x, b));
         __syncthreads();
     }
 }
@@ -168,7 +227,10 @@ __device__ __noinline__ void slice_left(const Ctx& x, int slice, double* M, bool
 __device__ __noinline__ void slice_right(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, false);
     for (int b = 0; b < x.nf; ++b) {
-        smm<false, true>(x, wrap, blk(x.c->tmp1, x, b), blk(M, x, b), x.c->eT2);
+        if (x.c->cb)
+            cb_apply(x, 0, 1, blk(x.c->tmp1, x, b), blk(M, x, b), blk(x.c->tmp2, x, b));
+        else
+            smm<false, true>(x, wrap, blk(x.c->tmp1, x, b), blk(M, x, b), x.c->eT2);
         __syncthreads();
         dright(x.n, blk(M, x, b), blk(x.c->tmp1, x, b), x.s->ev + b * x.n);
         __syncthreads();
@@ -180,7 +242,10 @@ __device__ __noinline__ void slice_inv_right(const Ctx& x, int slice, double* M,
     for (int b = 0; b < x.nf; ++b) {
         dright(x.n, blk(x.c->tmp1, x, b), blk(M, x, b), x.s->ev + b * x.n);
         __syncthreads();
-        smm<false, true>(x, wrap, blk(M, x, b), blk(x.c->tmp1, x, b), x.c->eT2inv);
+        if (x.c->cb)
+            cb_apply(x, 1, 1, blk(M, x, b), blk(x.c->tmp1, x, b), blk(x.c->tmp2, x, b));
+        else
+            smm<false, true>(x, wrap, blk(M, x, b), blk(x.c->tmp1, x, b), x.c->eT2inv);
         __syncthreads();
     }
 }
@@ -188,7 +253,10 @@ __device__ __noinline__ void slice_inv_right(const Ctx& x, int slice, double* M,
 __device__ __noinline__ void slice_inv_left(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, true);
     for (int b = 0; b < x.nf; ++b) {
-        smm<true, false>(x, wrap, blk(x.c->tmp1, x, b), x.c->eT2inv, blk(M, x, b));
+        if (x.c->cb)
+            cb_apply(x, 1, 0, blk(x.c->tmp1, x, b), blk(M, x, b), blk(x.c->tmp2, x, b));
+        else
+            smm<true, false>(x, wrap, blk(x.c->tmp1, x, b), x.c->eT2inv, blk(M, x, b));
         __syncthreads();
         dleft(x.n, blk(M, x, b), x.s->ev + b * x.n, blk(x.c->tmp1, x, b));
         __syncthreads();
@@ -198,7 +266,10 @@ __device__ __noinline__ void slice_inv_left(const Ctx& x, int slice, double* M, 
 __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* M) {
     interaction_exp(x, slice, false);
     for (int b = 0; b < x.nf; ++b) {
-        smm<true, false>(x, false, blk(x.c->tmp1, x, b), x.c->eT2, blk(M, x, b));
+        if (x.c->cb)
+            cb_apply(x, 0, 2, blk(x.c->tmp1, x, b), blk(M, x, b), blk(x.c->tmp2, x, b));
+        else
+            smm<true, false>(x, false, blk(x.c->tmp1, x, b), x.c->eT2, blk(M, x, b));
         __syncthreads();
         dleft(x.n, blk(M, x, b), x.s->ev + b * x.n, blk(x.c->tmp1, x, b));
         __syncthreads();
@@ -1057,6 +1128,11 @@ __device__ __noinline__ void replica_accept(const Ctx& x, const DqmcChain* all, 
 __device__ __noinline__ void greens_physical(const Ctx& x, const double* src, double* out) {
     DqmcChain& c = *x.c;
     for (int b = 0; b < x.nf; ++b) {
+        if (c.cb) {
+            cb_apply(x, 2, 1, blk(c.tmp1, x, b), src + (size_t)b * x.nn, blk(c.tmp2, x, b));
+            cb_apply(x, 3, 0, blk(out, x, b), blk(c.tmp1, x, b), blk(c.tmp2, x, b));
+            continue;
+        }
         mm<false, true>(x.n, blk(c.tmp1, x, b), src + (size_t)b * x.nn, c.eTh, x.s->tiles);
         __syncthreads();
         mm<true, false>(x.n, blk(out, x, b), c.eThinv, blk(c.tmp1, x, b), x.s->tiles);

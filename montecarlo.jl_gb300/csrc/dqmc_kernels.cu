@@ -87,7 +87,10 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
             // SimpleScheduler(LocalSweep(), <global update>) (scheduler.jl:281-289):
             // every call after the first starts with the global update
             if (s->c.global_kind >= 0) {
-                if (s->c.sched_calls > 0) {
+                // every thread reads the call count before thread 0 bumps it
+                const bool global_first = s->c.sched_calls > 0;
+                __syncthreads();
+                if (global_first) {
                     if (res) g_to_global(x);
                     global_update(x, s->c.global_kind);
                     if (res) g_to_arena(x);

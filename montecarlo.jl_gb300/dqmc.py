@@ -68,6 +68,10 @@ class DQMC:
         self.handle = _lib.Handle([self.config], precision=prec, device=device)
         self.exps = hopping_exponentials(model.hopping_matrix(), p.delta_tau)
         self.handle.set_hopping(0, self.exps)
+        if p.checkerboard:  # init_hopping_matrices with checkerboard (stack.jl:240-246)
+            from .model import checkerboard_exponentials, checkerboard_pack
+            cbf = checkerboard_exponentials(model.hopping_matrix(), model.l, p.delta_tau)
+            self.handle.set_checkerboard(0, *checkerboard_pack(cbf))
         self.handle.init_random_field(0)  # rand!(field_data), DQMC.jl:50
         self.field.conf[:] = self.handle.get_field(0)
         self.initialized = False

@@ -96,8 +96,6 @@ class DQMCParameters:
     def make(cls, thermalization=100, sweeps=100, silent=False, check_sign_problem=True,
              check_propagation_error=True, safe_mult=10, measure_rate=10, warn_round=True,
              print_rate=None, checkerboard=False, **kw):
-        if checkerboard:
-            raise NotImplementedError("checkerboard hopping is not part of this library")
         if print_rate is None:
             print_rate = max(10, (thermalization + sweeps) // 100)
         keys = set(kw)
@@ -124,7 +122,8 @@ class DQMCParameters:
         else:
             raise ValueError(f"Invalid keyword arguments to DQMCParameters {kw}")
         return cls(thermalization, sweeps, silent, check_sign_problem, check_propagation_error,
-                   safe_mult, float(dt), float(beta), int(slices), measure_rate, print_rate, False)
+                   safe_mult, float(dt), float(beta), int(slices), measure_rate, print_rate,
+                   bool(checkerboard))
 
 
 def _round_half_even(x: float) -> int:
@@ -241,3 +240,122 @@ def generate_chunks(length: int, max_chunk: int):
     n = -(-length // max_chunk)
     step = length / n
     return [(_round_half_even((i - 1) * step) + 1, _round_half_even(i * step)) for i in range(1, n + 1)]
+
+
+# ---- checkerboard decomposition of the hopping exponentials ------------------
+
+def _is_reversal(b1, b2) -> bool:
+    """lattice.jl:48-51."""
+    return (b1.frm == b2.to and b1.to == b2.frm and
+            all(a == -b for a, b in zip(b1.uc_shift, b2.uc_shift)))
+
+
+def checkerboard_groups(lattice):
+    """build_checkerboard (linalg/checkerboard.jl:14-140): bond groups in
+    which every site occurs at most once, one bond direction per group, as
+    0-based (src, trg) pairs, in the reference's order.
+
+    Per directed unit-cell bond (the first of each reversal pair,
+    lattice.jl:126-134) the bonds of all Bravais cells form a base group
+    (duplicates and reversals within it dropped); a base group that chains
+    (some bond starts where the first one ends) is split greedily into up to
+    three site-disjoint groups.  The reference's filter of bonds repeated
+    across base groups compares tuples with pairs and so never removes any;
+    that is kept (no cross-group filter)."""
+    uc = lattice.unitcell
+    directed = []
+    for i, b in enumerate(uc.bonds):
+        if not any(_is_reversal(b, uc.bonds[j]) for j in directed):
+            directed.append(i)
+    nb = int(np.prod(lattice.Ls))
+    out = []
+    for j in directed:
+        group = [lattice._shift_bravais(src, uc.bonds[j]) for src in range(1, nb + 1)]
+        i = 0
+        while i < len(group) - 1:
+            s, t = group[i]
+            k = i + 1
+            while k < len(group):
+                if group[k] == (s, t) or group[k] == (t, s):
+                    del group[k]
+                else:
+                    k += 1
+            i += 1
+        s0, t0 = group[0]
+        if any(g[0] == t0 for g in group):
+            parts, used = [[], [], []], [set(), set(), set()]
+            for s, t in group:
+                for p in range(3):
+                    if s not in used[p] and t not in used[p]:
+                        parts[p].append((s, t))
+                        used[p].update((s, t))
+                        break
+                else:
+                    raise RuntimeError("Failed to distribute bonds into groups.")
+            groups = [g for g in parts if g]
+        else:
+            groups = [group]
+        out.extend([[(s - 1, t - 1) for s, t in g] for g in groups])
+    return out
+
+
+def checkerboard_factor(T: np.ndarray, groups, factor: float):
+    """CheckerboardDecomposed(T, lattice, factor) (checkerboard.jl:203-270)
+    of one flavour block: exp(factor T) ~ P_1 P_2 ... P_N D with
+    D = exp(factor diag(T)) and, per group, P = 1 + (cosh(v) - 1) on the
+    bond's two sites and sinh(v) between them (v = factor T[src, trg]); the
+    parts are reversed for factor > 0 (the inverse's order).  Returns
+    (D, [(c, s, partner), ...]) with per-site c (cosh or 1), s (sinh or 0)
+    and partner site (-1: none)."""
+    n = T.shape[0]
+    D = np.exp(factor * np.diag(T))
+    parts = []
+    for g in groups:
+        c, s, partner = np.ones(n), np.zeros(n), np.full(n, -1, dtype=np.int64)
+        for src, trg in g:
+            v = factor * T[src, trg]
+            c[src] = c[trg] = math.cosh(v)
+            s[src] = s[trg] = math.sinh(v)
+            partner[src], partner[trg] = trg, src
+        parts.append((c, s, partner))
+    if factor > 0.0:
+        parts.reverse()
+    return D, parts
+
+
+def checkerboard_matrix(D, parts) -> np.ndarray:
+    """Dense form P_1 ... P_N D of a checkerboard factor (for tests)."""
+    n = len(D)
+    X = np.diag(D)
+    for c, s, partner in reversed(parts):
+        P = np.diag(c)
+        for i in range(n):
+            if partner[i] >= 0:
+                P[i, partner[i]] = s[i]
+        X = P @ X
+    return X
+
+
+def checkerboard_exponentials(T: np.ndarray, lattice, delta_tau: float):
+    """The four hopping exponentials of init_hopping_matrices with
+    checkerboard = true (stack.jl:240-246): factors -dtau, +dtau, -dtau/2,
+    +dtau/2."""
+    groups = checkerboard_groups(lattice)
+    return [checkerboard_factor(T, groups, f)
+            for f in (-delta_tau, +delta_tau, -0.5 * delta_tau, +0.5 * delta_tau)]
+
+
+def checkerboard_pack(cb_factors):
+    """Flat FP64 layout of the four checkerboard factors, as
+    dqmc_set_checkerboard takes them: per factor D[n], then per part
+    c[n], s[n], partner[n] (-1: none).  Returns (data, parts per factor)."""
+    n_parts = len(cb_factors[0][1])
+    out = []
+    for D, parts in cb_factors:
+        if len(parts) != n_parts:
+            raise ValueError("all checkerboard factors need the same number of parts")
+        out.append(np.asarray(D, dtype=np.float64))
+        for c, s, partner in parts:
+            out += [np.asarray(c, dtype=np.float64), np.asarray(s, dtype=np.float64),
+                    np.asarray(partner, dtype=np.float64)]
+    return np.ascontiguousarray(np.concatenate(out)), n_parts

@@ -70,6 +70,9 @@ struct OcChain {
     int current_slice, current_range, direction;
     double prop_err_all, prop_err_reported;
     long n_prop_err, n_neg_p, accepted;
+    int cb_np;                    /* checkerboard parts per factor (0: dense exponentials) */
+    double* cb;                   /* 4 factors x (D[n], parts x (c[n], s[n], partner[n])) */
+    double *cbt0, *cbt1;          /* n x n scratch of the checkerboard products */
     int8_t* temp_conf;            /* temp_conf(field): the configuration before a global move */
     double* tempvf;               /* stack.tempvf: Dl of the current G during a global move */
     long g_accepted, g_proposals;
@@ -382,6 +385,7 @@ void oc_destroy(OcChain* c) {
     free(c->rfirst); free(c->rlast);
     free(c->eT2); free(c->eT2inv); free(c->eTh); free(c->eThinv); free(c->conf);
     free(c->temp_conf); free(c->tempvf);
+    free(c->cb); free(c->cbt0); free(c->cbt1);
     free(c->u_stack); free(c->t_stack); free(c->d_stack);
     free(c->Ul); free(c->Ur); free(c->Tl); free(c->Tr); free(c->Dl); free(c->Dr);
     free(c->greens); free(c->greens_temp); free(c->tmp1); free(c->tmp2); free(c->curr_U);
@@ -428,21 +432,85 @@ static void interaction_matrix_exp(OcChain* c, int slice, double power, double* 
     }
 }
 
+/* ---- checkerboard products (linalg/checkerboard.jl:272-473) ----------------
+ * Factor m (0 exp(-dtau T), 1 exp(+dtau T), 2 exp(-dtau T/2), 3 exp(+dtau T/2))
+ * is X = P_1 ... P_N D; mode 0: X A, 1: A X, 2: X^T A = D P_N ... P_1 A.  One
+ * pass per part: row (or column) i takes c_i times itself plus s_i times its
+ * partner's, D fused into the first (mode 0) or last (modes 1, 2) pass. */
+void oc_set_checkerboard(OcChain* c, int np, const double* data) {
+    size_t per = (size_t)c->n * (1 + 3 * (size_t)np);
+    free(c->cb);
+    c->cb_np = np;
+    c->cb = dalloc(4 * per);
+    memcpy(c->cb, data, 4 * per * sizeof(double));
+    if (!c->cbt0) { c->cbt0 = dalloc(NN(c)); c->cbt1 = dalloc(NN(c)); }
+}
+static void cb_apply(OcChain* c, int m, int mode, double* out, const double* in) {
+    const int n = c->n, np = c->cb_np;
+    const double* D = c->cb + (size_t)m * n * (1 + 3 * (size_t)np);
+    const double* P = D + n;
+    const double* src = in;
+    double* bufs[2] = {c->cbt0, c->cbt1};
+    if (np == 0) {
+        for (int k = 0; k < n; ++k)
+            for (int i = 0; i < n; ++i)
+                c->cbt0[i + (size_t)k * n] = (mode == 1) ? in[i + (size_t)k * n] * D[k]
+                                                         : D[i] * in[i + (size_t)k * n];
+        memcpy(out, c->cbt0, NN(c) * sizeof(double));
+        return;
+    }
+    for (int step = 0; step < np; ++step) {
+        /* mode 0 applies P_N first; modes 1, 2 apply P_1 first */
+        const int part = (mode == 0) ? np - 1 - step : step;
+        const double* cc = P + (size_t)part * 3 * n;
+        const double* ss = cc + n;
+        const double* pt = ss + n;
+        const int first = (step == 0), last = (step == np - 1);
+        double* dst = bufs[step & 1];
+        for (int k = 0; k < n; ++k)
+            for (int i = 0; i < n; ++i) {
+                double y;
+                if (mode == 1) {  /* columns */
+                    const int q = (int)pt[k];
+                    const double v = src[i + (size_t)k * n];
+                    y = (q >= 0) ? fma(src[i + (size_t)q * n], ss[k], v * cc[k]) : v;
+                    if (last) y = y * D[k];
+                } else {          /* rows */
+                    const int q = (int)pt[i];
+                    double v = src[i + (size_t)k * n];
+                    double w = (q >= 0) ? src[q + (size_t)k * n] : 0.0;
+                    if (mode == 0 && first) {
+                        v = D[i] * v;
+                        if (q >= 0) w = D[q] * w;
+                    }
+                    y = (q >= 0) ? fma(ss[i], w, cc[i] * v) : v;
+                    if (mode == 2 && last) y = D[i] * y;
+                }
+                dst[i + (size_t)k * n] = y;
+            }
+        src = dst;
+    }
+    memcpy(out, src, NN(c) * sizeof(double));
+}
+
 /* slice matrices, stack.jl:319-367 (hopping exponentials are Hermitian-wrapped,
- * so vmul! multiplies with the transposed data: fallbacks.jl:67-68) */
+ * so vmul! multiplies with the transposed data: fallbacks.jl:67-68); with a
+ * checkerboard decomposition the exponentials are applied as its products */
 static void mult_slice_left(OcChain* c, int slice, double* M) {
     int n = c->n; size_t nn = NN(c);
     interaction_matrix_exp(c, slice, 1.0, c->eV);
     for (int b = 0; b < c->nf; ++b) {
         diag_left(n, c->tmp1 + b * nn, c->eV + b * n, M + b * nn);
-        gemm_tn(n, M + b * nn, c->eT2, c->tmp1 + b * nn, c->scratch);
+        if (c->cb) cb_apply(c, 0, 0, M + b * nn, c->tmp1 + b * nn);
+        else gemm_tn(n, M + b * nn, c->eT2, c->tmp1 + b * nn, c->scratch);
     }
 }
 static void mult_slice_right(OcChain* c, int slice, double* M) {
     int n = c->n; size_t nn = NN(c);
     interaction_matrix_exp(c, slice, 1.0, c->eV);
     for (int b = 0; b < c->nf; ++b) {
-        gemm_nt(n, c->tmp1 + b * nn, M + b * nn, c->eT2, c->scratch);
+        if (c->cb) cb_apply(c, 0, 1, c->tmp1 + b * nn, M + b * nn);
+        else gemm_nt(n, c->tmp1 + b * nn, M + b * nn, c->eT2, c->scratch);
         diag_right(n, M + b * nn, c->tmp1 + b * nn, c->eV + b * n);
     }
 }
@@ -451,14 +519,16 @@ static void mult_slice_inv_right(OcChain* c, int slice, double* M) {
     interaction_matrix_exp(c, slice, -1.0, c->eV);
     for (int b = 0; b < c->nf; ++b) {
         diag_right(n, c->tmp1 + b * nn, M + b * nn, c->eV + b * n);
-        gemm_nt(n, M + b * nn, c->tmp1 + b * nn, c->eT2inv, c->scratch);
+        if (c->cb) cb_apply(c, 1, 1, M + b * nn, c->tmp1 + b * nn);
+        else gemm_nt(n, M + b * nn, c->tmp1 + b * nn, c->eT2inv, c->scratch);
     }
 }
 static void mult_slice_inv_left(OcChain* c, int slice, double* M) {
     int n = c->n; size_t nn = NN(c);
     interaction_matrix_exp(c, slice, -1.0, c->eV);
     for (int b = 0; b < c->nf; ++b) {
-        gemm_tn(n, c->tmp1 + b * nn, c->eT2inv, M + b * nn, c->scratch);
+        if (c->cb) cb_apply(c, 1, 0, c->tmp1 + b * nn, M + b * nn);
+        else gemm_tn(n, c->tmp1 + b * nn, c->eT2inv, M + b * nn, c->scratch);
         diag_left(n, M + b * nn, c->eV + b * n, c->tmp1 + b * nn);
     }
 }
@@ -466,7 +536,8 @@ static void mult_daggered_slice_left(OcChain* c, int slice, double* M) {
     int n = c->n; size_t nn = NN(c);
     interaction_matrix_exp(c, slice, 1.0, c->eV);
     for (int b = 0; b < c->nf; ++b) {
-        gemm_tn(n, c->tmp1 + b * nn, c->eT2, M + b * nn, c->scratch);
+        if (c->cb) cb_apply(c, 0, 2, c->tmp1 + b * nn, M + b * nn);
+        else gemm_tn(n, c->tmp1 + b * nn, c->eT2, M + b * nn, c->scratch);
         diag_left(n, M + b * nn, c->eV + b * n, c->tmp1 + b * nn);
     }
 }
@@ -950,8 +1021,13 @@ void oc_greens_physical(OcChain* c, const double* src, double* out) {
     size_t nn = NN(c);
     double* tmp = dalloc(nn);
     for (int b = 0; b < c->nf; ++b) {
-        gemm_nt(n, tmp, src + b * nn, c->eTh, c->scratch);
-        gemm_tn(n, out + b * nn, c->eThinv, tmp, c->scratch);
+        if (c->cb) {
+            cb_apply(c, 2, 1, tmp, src + b * nn);
+            cb_apply(c, 3, 0, out + b * nn, tmp);
+        } else {
+            gemm_nt(n, tmp, src + b * nn, c->eTh, c->scratch);
+            gemm_tn(n, out + b * nn, c->eThinv, tmp, c->scratch);
+        }
     }
     free(tmp);
 }

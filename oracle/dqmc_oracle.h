@@ -78,6 +78,12 @@ void oc_get_stack(const OcChain* c, int which, int idx, double* out);
  *            max reported (>1e-7), negative-p count, accepted total] */
 void oc_get_analysis(const OcChain* c, double* out5);
 
+/* checkerboard = true (stack.jl:240-246, linalg/checkerboard.jl): the four
+ * hopping factors as np parts each, data = 4 x (D[n], np x (cosh-or-1[n],
+ * sinh-or-0[n], partner[n] (-1: none))), factors in the order exp(-dtau T),
+ * exp(+dtau T), exp(-dtau T/2), exp(+dtau T/2) */
+void oc_set_checkerboard(OcChain* c, int np, const double* data);
+
 /* global updates (global_updates.jl), at current_slice 1, direction +1:
  * kind 0 GlobalFlip, 1 GlobalShuffle; returns 1 when accepted */
 int oc_global_update(OcChain* c, int kind);

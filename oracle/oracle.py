@@ -107,6 +107,7 @@ def lib():
         L.oc_local_move_to.restype = C.c_double
         L.oc_get_global_stats.argtypes = [P, C.POINTER(C.c_long), C.POINTER(C.c_long)]
         L.oc_greens_kl.argtypes = [P, C.c_void_p, C.c_void_p, C.c_int, dp]
+        L.oc_set_checkerboard.argtypes = [P, C.c_int, dp]
         L.oc_run_chains_threaded.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int]
         L.oc_run_chains_threaded.restype = C.c_double
         _lib = L
@@ -278,6 +279,11 @@ class OracleChain:
 
     def local_move_to(self, i, x_new):
         return lib().oc_local_move_to(self.h, int(i), int(x_new))
+
+    def set_checkerboard(self, data, n_parts):
+        """Checkerboard factors packed as oc_set_checkerboard expects."""
+        lib().oc_set_checkerboard(self.h, int(n_parts), _dp(np.ascontiguousarray(data,
+                                                                               dtype=np.float64)))
 
     def greens_kl(self, pairs):
         """Effective unequal-time G(k, l) for a list of (k, l) pairs."""

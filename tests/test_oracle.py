@@ -321,3 +321,62 @@ def test_unequal_time_greens_known_answers(oracle, pkg, field):
                 P = Bs[t][b] @ P
             ref = -(np.eye(n) - eq[k][b]) @ np.linalg.inv(P)
             assert maxdiff(G[(k, l)][b], ref) < 1e-10, (k, l)
+
+
+def test_checkerboard_groups_and_factors(pkg):
+    """build_checkerboard: site-disjoint groups that cover every bond once;
+    the factors invert each other exactly and approximate exp(f T) to the
+    Trotter order (exactly where the groups commute, as on 4x4)."""
+    from scipy.linalg import expm
+    from montecarlo_gb300 import model as M
+    for lat in (pkg.SquareLattice(4), pkg.SquareLattice(3), pkg.SquareLattice(8), pkg.Honeycomb(2),
+                pkg.Chain(6)):
+        T = pkg.HubbardModel(lat, U=1.0, mu=0.3).hopping_matrix()
+        groups = M.checkerboard_groups(lat)
+        seen = set()
+        for g in groups:
+            sites = [s for b in g for s in b]
+            assert len(sites) == len(set(sites))
+            for s, t in g:
+                seen.add((min(s, t), max(s, t)))
+        nz = {(i, j) for i in range(len(T)) for j in range(i + 1, len(T)) if T[i, j] != 0}
+        assert nz <= seen
+        X = [M.checkerboard_matrix(*f) for f in M.checkerboard_exponentials(T, lat, 0.1)]
+        assert np.abs(X[0] @ X[1] - np.eye(len(T))).max() < 1e-14
+        assert np.abs(X[2] @ X[3] - np.eye(len(T))).max() < 1e-14
+        assert np.abs(X[0] - expm(-0.1 * T)).max() < 0.02
+    T = pkg.HubbardModel(pkg.SquareLattice(4), U=1.0).hopping_matrix()
+    X0 = M.checkerboard_matrix(*M.checkerboard_exponentials(T, pkg.SquareLattice(4), 0.1)[0])
+    assert np.abs(X0 - expm(-0.1 * T)).max() < 1e-14
+
+
+@pytest.mark.parametrize("field", ["DensityHirschField", "MagneticHirschField"])
+def test_checkerboard_chain_vs_direct(oracle, pkg, field):
+    """With checkerboard = true the stack uses the factor products: G from the
+    oracle's stack equals the direct QR chain of the dense checkerboard slice
+    matrices (3x3: the groups do not commute, so this differs from the dense
+    exponential path)."""
+    from montecarlo_gb300 import model as M
+    model, param, fld, exps = make_setup(pkg, L=3, U=FIELD_U[field], beta=2.0, safe_mult=5,
+                                         field=getattr(pkg, field))
+    T = model.hopping_matrix()
+    cb = M.checkerboard_exponentials(T, model.l, param.delta_tau)
+    X = [M.checkerboard_matrix(*f) for f in cb]
+    cexps = [X[0], X[1], X[2], X[3]]
+    c = oracle_chain(oracle, model, param, fld, exps, 31)
+    c.set_checkerboard(*M.checkerboard_pack(cb))
+    c.init_random_conf()
+    conf = c.get_conf()
+    for sl in (0, 3, 10, param.slices):
+        G = c.calculate_greens_at(sl)
+        for b in range(fld.unique_flavors):
+            Bs = _dense_B(pkg, model, fld, cexps, conf, b)
+            Gd = oracle.direct_greens(Bs, sl, param.safe_mult)
+            assert maxdiff(G[b], Gd) < 1e-12 * max(1.0, np.abs(Gd).max()), (sl, b)
+    c.initialize_run()
+    c.sweeps(2)
+    assert c.analysis()["propagation_error_reported"] < 1e-8
+    Gp = c.greens_physical(c.greens())
+    for b in range(fld.unique_flavors):
+        ref = X[3] @ c.greens()[b] @ X[2]
+        assert maxdiff(Gp[b], ref) < 1e-13
