@@ -719,6 +719,7 @@ int dqmc_set_checkerboard(dqmc_handle* h, int chain, int n_parts, const double* 
         if (!d.active) continue;
         if (n_parts < 0) {  // back to the dense exponentials
             d.cb = nullptr;
+            d.cbp = nullptr;
             d.cb_np = 0;
             continue;
         }
@@ -740,13 +741,39 @@ int dqmc_set_checkerboard(dqmc_handle* h, int chain, int n_parts, const double* 
                 }
             }
         }
+        // device layout: per factor D[n] and per part c[n], s[n]; then the
+        // partners as int32, per factor and part
+        const size_t per_d = (size_t)n * (1 + 2 * (size_t)n_parts);
+        std::vector<double> dv(4 * per_d);
+        std::vector<int32_t> pv(4 * (size_t)n_parts * n);
+        for (size_t m = 0; m < 4; ++m) {
+            const double* f = data + m * per;
+            double* g = dv.data() + m * per_d;
+            for (int k = 0; k < n; ++k) g[k] = f[k];
+            for (int p = 0; p < n_parts; ++p) {
+                const double* fp = f + n + (size_t)p * 3 * n;
+                for (int k = 0; k < n; ++k) {
+                    g[n + (size_t)p * 2 * n + k] = fp[k];
+                    g[n + (size_t)p * 2 * n + n + k] = fp[n + k];
+                    pv[(m * n_parts + p) * (size_t)n + k] = (int32_t)fp[2 * n + k];
+                }
+            }
+        }
+        (void)cnt;
         if (h->cb_mem[i]) { cudaFree(h->cb_mem[i]); h->cb_mem[i] = nullptr; }
-        CUDA_TRY(cudaMalloc((void**)&h->cb_mem[i], cnt * sizeof(double)), "allocate checkerboard factors");
-        CUDA_TRY(cudaMemcpyAsync(h->cb_mem[i], data, cnt * sizeof(double), cudaMemcpyHostToDevice,
-                                 h->stream),
+        const size_t bytes = dv.size() * sizeof(double) + pv.size() * sizeof(int32_t);
+        CUDA_TRY(cudaMalloc((void**)&h->cb_mem[i], bytes), "allocate checkerboard factors");
+        CUDA_TRY(cudaMemcpyAsync(h->cb_mem[i], dv.data(), dv.size() * sizeof(double),
+                                 cudaMemcpyHostToDevice, h->stream),
                  "upload checkerboard factors");
+        int32_t* dp = reinterpret_cast<int32_t*>(h->cb_mem[i] + dv.size());
+        if (!pv.empty())
+            CUDA_TRY(cudaMemcpyAsync(dp, pv.data(), pv.size() * sizeof(int32_t),
+                                     cudaMemcpyHostToDevice, h->stream),
+                     "upload checkerboard partners");
         CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
         d.cb = h->cb_mem[i];
+        d.cbp = dp;
         d.cb_np = n_parts;
     }
     h->host_dirty = true;

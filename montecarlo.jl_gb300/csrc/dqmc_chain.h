@@ -87,11 +87,13 @@ struct DqmcChain {
     const int* ut_pairs;
     double* ut_out;
     // checkerboard = true (stack.jl:240-246, linalg/checkerboard.jl): parts
-    // per factor and the four factors exp(-dtau T), exp(+dtau T),
-    // exp(-dtau T/2), exp(+dtau T/2), each D[n] then per part c[n], s[n],
-    // partner[n] (-1: none); NULL: the dense exponentials
+    // per factor; the four factors exp(-dtau T), exp(+dtau T), exp(-dtau T/2),
+    // exp(+dtau T/2), each D[n] then per part c[n], s[n] (cb), and per factor
+    // and part the bond partner of each site (cbp, -1: none); NULL: the
+    // dense exponentials
     int cb_np, pad3;
     const double* cb;
+    const int* cbp;
 };
 #define DQMC_CB_MAXPARTS 12
 

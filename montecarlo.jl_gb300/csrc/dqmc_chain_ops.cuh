@@ -152,8 +152,9 @@ __device__ __noinline__ void cb_apply(const Ctx& x, int m, int mode, double* out
                                       const double* in, double* scr) {
     const DqmcChain& c = *x.c;
     const int n = x.n, np = c.cb_np;
-    const double* D = c.cb + (size_t)m * n * (1 + 3 * (size_t)np);
+    const double* D = c.cb + (size_t)m * n * (1 + 2 * (size_t)np);
     const double* P = D + n;
+    const int* PT = c.cbp + (size_t)m * np * n;
     if (np == 0) {
         for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
             const int i = e % n, k = e / n;
@@ -165,21 +166,21 @@ __device__ __noinline__ void cb_apply(const Ctx& x, int m, int mode, double* out
     const double* src = in;
     for (int step = 0; step < np; ++step) {
         const int part = (mode == 0) ? np - 1 - step : step;
-        const double* cc = P + (size_t)part * 3 * n;
+        const double* cc = P + (size_t)part * 2 * n;
         const double* ss = cc + n;
-        const double* pt = ss + n;
+        const int* pt = PT + (size_t)part * n;
         const bool first = (step == 0), last = (step == np - 1);
         double* dst = ((np - 1 - step) & 1) ? scr : out;
         for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
             const int i = e % n, k = e / n;
             double y;
             if (mode == 1) {
-                const int q = (int)pt[k];
+                const int q = pt[k];
                 const double v = src[e];
                 y = (q >= 0) ? fma(src[i + (size_t)q * n], ss[k], v * cc[k]) : v;
                 if (last) y = y * D[k];
             } else {
-                const int q = (int)pt[i];
+                const int q = pt[i];
                 double v = src[e];
                 double w = (q >= 0) ? src[q + (size_t)k * n] : 0.0;
                 if (mode == 0 && first) {

@@ -111,6 +111,27 @@ class DQMC:
         G(k dtau, l dtau); physical (the _greens! transform) by default."""
         return self.handle.greens_kl(0, [(k, l)], physical=physical)[0]
 
+    def spin_susceptibility(self, q=None):
+        """chi_z(q) of the current configuration (time-displaced spin-density
+        correlations integrated over tau, the reference's
+        spin_density_susceptibility with a TimeIntegral): the unequal-time
+        Green's functions G(0,0), G(l,l), G(0,l), G(l,0) for l = 0..M in one
+        device call, contracted on the host.  q defaults to (pi, pi, ...)."""
+        from .measurements import spin_susceptibility_z
+        M = self.parameters.slices
+        pairs = [(0, 0)]
+        for l in range(M + 1):
+            pairs += [(l, l), (0, l), (l, 0)]
+        Gs = self.handle.greens_kl(0, pairs, physical=True)
+        G00 = Gs[0]
+        by_l = [(G00, Gs[2 + 3 * l], Gs[3 + 3 * l], Gs[1 + 3 * l]) for l in range(M + 1)]
+        if q is None:
+            phases = self._q_phases
+        else:
+            ph = self.model.l.positions() @ np.asarray(q, dtype=float)
+            phases = (np.cos(ph), np.sin(ph))
+        return spin_susceptibility_z(by_l, phases, self.parameters.delta_tau)
+
     def calculate_greens(self, slice_, safe_mult=0):
         """calculate_greens(mc, slice) (stack.jl:525-583), effective G."""
         return self.handle.calculate_greens(0, slice_, safe_mult)

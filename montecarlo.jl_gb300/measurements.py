@@ -114,6 +114,36 @@ def structure_factor(corr, positions, q):
     return float(np.real(np.conj(ph) @ corr @ ph) / len(r))
 
 
+def time_displaced_sdc_z(G00, G0l, Gl0, Gll, at_zero):
+    """<m_z(i, tau) m_z(j, 0)> for all site pairs from the four Green's
+    functions G(0,0), G(0,l), G(l,0), G(l,l) (full_sdc_z_kernel,
+    spin_density.jl:182-227); ``at_zero``: l == 0 (the delta of the
+    time-ordered contraction)."""
+    n = G00.shape[1]
+    idm = np.eye(n) if at_zero else np.zeros((n, n))
+    if G00.shape[0] == 1:
+        return 2.0 * (idm - G0l[0].T) * Gl0[0]
+    ml = np.diag(Gll[1]) - np.diag(Gll[0])      # (1 - G1_ii) - (1 - G2_ii)
+    m0 = np.diag(G00[1]) - np.diag(G00[0])
+    exch = sum((idm - G0l[b].T) * Gl0[b] for b in range(2))
+    return np.outer(ml, m0) + exch
+
+
+def spin_susceptibility_z(greens_by_l, phases, delta_tau):
+    """chi_z(q) = (1/n) sum_l w_l sum_ij e^{i q (r_i - r_j)} <m_z(i, l dtau) m_z(j, 0)>
+    with the trapezoid weights of the reference's TimeIntegral
+    (generic.jl:337-366: 0.5 dtau at l = 0 and l = M, dtau otherwise) and real
+    phases (cos(q.r_i), sin(q.r_i)).  greens_by_l[l] = (G00, G0l, Gl0, Gll)."""
+    c, s = phases
+    M = len(greens_by_l) - 1
+    chi = 0.0
+    for l, (G00, G0l, Gl0, Gll) in enumerate(greens_by_l):
+        C = time_displaced_sdc_z(G00, G0l, Gl0, Gll, l == 0)
+        w = (0.5 if l in (0, M) else 1.0) * delta_tau
+        chi += w * float(c @ C @ c + s @ C @ s)
+    return chi / len(c)
+
+
 MEASUREMENTS = {
     "greens": greens_kernel,
     "occupation": occupation_kernel,

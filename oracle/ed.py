@@ -74,3 +74,15 @@ class HubbardED:
 
     def energy(self):
         return self.expect(self.H)
+
+    def susceptibility_z(self, phases):
+        """(1/n) int_0^beta dtau <M(tau) M(0)> with M = sum_i phases_i m_z(i)
+        (real phases, e.g. cos(q.r_i) at q = (pi, pi)), from the spectral
+        sum over eigenstates: sum_ab rho_a |M_ab|^2 (e^{beta (E_a - E_b)} - 1) / (E_b - E_a)."""
+        Mop = sum(phases[i] * (self.nop[i][0] - self.nop[i][1]) for i in range(self.n))
+        Mab = self.V.T @ Mop @ self.V
+        E = self.E
+        d = E[None, :] - E[:, None]          # E_b - E_a
+        with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
+            f = np.where(np.abs(d) < 1e-12, self.beta, (1.0 - np.exp(-self.beta * d)) / d)
+        return float(np.sum(self.rho_diag[:, None] * Mab ** 2 * f)) / self.n

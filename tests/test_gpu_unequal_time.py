@@ -59,3 +59,26 @@ def test_greens_kl_does_not_disturb_the_chain(pkg, lib, oracle):
     assert maxdiff(h.greens(0), o.greens()) < TOL_G
     with pytest.raises(lib.DQMCError):
         h.greens_kl(0, [(param.slices + 1, 0)])
+
+
+@pytest.mark.parametrize("U", [-1.0, 1.0])
+def test_spin_susceptibility_matches_ed_2x2(pkg, lib, U):
+    """chi_z(pi, pi) from the time-displaced Green's functions (TimeIntegral
+    of the z spin-density correlation) against exact diagonalisation on 2x2
+    at beta = 1, dtau = 0.1 (atol 3.05 dtau^2 as the reference's ED tests,
+    plus five binning errors)."""
+    import ed
+    DT = 0.1
+    model = pkg.HubbardModel(pkg.SquareLattice(2), U=U, mu=0.0)
+    E = ed.HubbardED(4, model.l.bonds(), 1.0, U, 0.0, 1.0)
+    pos = model.l.positions()
+    chi_ed = E.susceptibility_z(np.cos(pos @ np.array([np.pi, np.pi])))
+    mc = pkg.DQMC(model, beta=1.0, delta_tau=DT, safe_mult=10, seed=44, thermalization=200,
+                  sweeps=0, measure_rate=1)
+    pkg.run(mc)
+    b = pkg.LogBinner()
+    for _ in range(1500):
+        mc.handle.sweep(1)
+        b.push(mc.spin_susceptibility())
+    chi, err = float(b.mean()), float(b.std_error())
+    assert abs(chi - chi_ed) <= 3.05 * DT ** 2 + 5 * err, (chi, chi_ed, err)

@@ -109,3 +109,14 @@ def test_neighbour_partners(pkg):
     """Replica-exchange rounds pair neighbours, alternating even and odd pairs."""
     assert pkg.neighbour_partners(5, False).tolist() == [1, 0, 3, 2, -1]
     assert pkg.neighbour_partners(5, True).tolist() == [-1, 2, 1, 4, 3]
+
+
+def test_time_displaced_kernel_reduces_to_equal_time(pkg):
+    """With all four Green's functions equal to G and l = 0 the time-displaced
+    kernel is the equal-time one."""
+    rng = np.random.default_rng(4)
+    for nf in (1, 2):
+        G = rng.normal(size=(nf, 5, 5)) * 0.1 + 0.5 * np.eye(5)
+        C0 = pkg.time_displaced_sdc_z(G, G, G, G, True)
+        C1 = pkg.spin_density_correlation_z(G)
+        assert np.max(np.abs(C0 - C1)) < 1e-14
