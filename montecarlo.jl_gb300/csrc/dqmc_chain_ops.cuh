@@ -13,7 +13,7 @@ namespace {  // internal linkage: each translation unit gets its own copy
 
 struct Smem {
     union {                      // never live at the same time
-        double tiles[2 * 16 * 64];  // mm() / mm_df() staging
+        double tiles[2 * 16 * 64];  // mm() / mm_dfx() staging
         struct {
             double col[2][DQMC_NMAX];  // rank-1: (I - G)[:, i] per block
             double row[2][DQMC_NMAX];  // rank-1: (Delta/R) G[i, :] per block

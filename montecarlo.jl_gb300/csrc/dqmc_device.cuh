@@ -137,101 +137,6 @@ __device__ __noinline__ void mm(int n, double* __restrict__ C, const double* __r
     }
 }
 
-// Double-float product for the mixed path: C = op(A) * op(B) with FP64
-// inputs and output, computed on the FP32 pipe.  Each operand is split
-// X = Xh + Xl (Xh = fp32(X), Xl = fp32(X - Xh), on the fly while staging).
-// The main term sum_k Ah Bh is accumulated exactly-rounded in a pair of floats:
-// the product is split exactly with one fmaf (TwoProd) and added with TwoSum
-// (Knuth); the cross terms Ah Bl + Al Bh are accumulated in plain FP32 and
-// Al Bl is dropped.  Relative error ~1e-14 per product (FP32 alone: ~1e-7,
-// which the wraps' error amplification over ten slices turns into O(1)).
-// About 12 FP32 instructions per multiply-add, against one FP64 instruction
-// on a pipe ~57x narrower on GB300.  64 x 64 tiles, 4 x 4 per thread, k staged
-// 16 at a time (sm: 4 * 16 * 64 floats).  C must not alias A or B.
-template <bool TA, bool TB>
-__device__ __noinline__ void mm_df(int n, double* __restrict__ C, const double* __restrict__ A,
-                                   const double* __restrict__ B, double* smd) {
-    float* sAh = reinterpret_cast<float*>(smd);  // [16][64]: sAh[kk*64 + m]
-    float* sAl = sAh + 16 * 64;
-    float* sBh = sAl + 16 * 64;                   // [16][64]: sBh[kk*64 + j]
-    float* sBl = sBh + 16 * 64;
-    const int tid = threadIdx.x, tx = tid & 15, ty = tid >> 4;
-    for (int n0 = 0; n0 < n; n0 += 64) {
-        for (int m0 = 0; m0 < n; m0 += 64) {
-            float sh[4][4], sl[4][4], xx[4][4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) sh[r][q] = sl[r][q] = xx[r][q] = 0.f;
-            for (int k0 = 0; k0 < n; k0 += 16) {
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    int e = tid + t * DQMC_NT;
-                    int mm_, kk;
-                    if (!TA) { mm_ = e & 63; kk = e >> 6; } else { kk = e & 15; mm_ = e >> 4; }
-                    int gm = m0 + mm_, gk = k0 + kk;
-                    double v = 0.0;
-                    if (gm < n && gk < n) v = TA ? A[gk + (size_t)gm * n] : A[gm + (size_t)gk * n];
-                    float h = __double2float_rn(v);
-                    sAh[kk * 64 + mm_] = h;
-                    sAl[kk * 64 + mm_] = __double2float_rn(v - (double)h);
-                }
-#pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    int e = tid + t * DQMC_NT;
-                    int kk, jj;
-                    if (!TB) { kk = e & 15; jj = e >> 4; } else { jj = e & 63; kk = e >> 6; }
-                    int gk = k0 + kk, gj = n0 + jj;
-                    double v = 0.0;
-                    if (gk < n && gj < n) v = TB ? B[gj + (size_t)gk * n] : B[gk + (size_t)gj * n];
-                    float h = __double2float_rn(v);
-                    sBh[kk * 64 + jj] = h;
-                    sBl[kk * 64 + jj] = __double2float_rn(v - (double)h);
-                }
-                __syncthreads();
-#pragma unroll 4
-                for (int kk = 0; kk < 16; ++kk) {
-                    float ah[4], al[4], bh[4], bl[4];
-#pragma unroll
-                    for (int r = 0; r < 4; ++r) {
-                        ah[r] = sAh[kk * 64 + tx + 16 * r];
-                        al[r] = sAl[kk * 64 + tx + 16 * r];
-                    }
-#pragma unroll
-                    for (int q = 0; q < 4; ++q) {
-                        bh[q] = sBh[kk * 64 + ty + 16 * q];
-                        bl[q] = sBl[kk * 64 + ty + 16 * q];
-                    }
-#pragma unroll
-                    for (int r = 0; r < 4; ++r)
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) {
-                            const float p = __fmul_rn(ah[r], bh[q]);
-                            const float pe = __fmaf_rn(ah[r], bh[q], -p);  // exact: ah*bh = p + pe
-                            const float t = __fadd_rn(sh[r][q], p);       // TwoSum(sh, p)
-                            const float z = __fsub_rn(t, sh[r][q]);
-                            const float er = __fadd_rn(__fsub_rn(sh[r][q], __fsub_rn(t, z)),
-                                                       __fsub_rn(p, z));
-                            sh[r][q] = t;
-                            sl[r][q] = __fadd_rn(sl[r][q], __fadd_rn(er, pe));
-                            xx[r][q] = __fmaf_rn(ah[r], bl[q], __fmaf_rn(al[r], bh[q], xx[r][q]));
-                        }
-                }
-                __syncthreads();
-            }
-#pragma unroll
-            for (int r = 0; r < 4; ++r)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    int gm = m0 + tx + 16 * r, gj = n0 + ty + 16 * q;
-                    if (gm < n && gj < n)
-                        C[gm + (size_t)gj * n] =
-                            (double)sh[r][q] + ((double)sl[r][q] + (double)xx[r][q]);
-                }
-        }
-    }
-}
-
 // ---- double-float storage (the mixed path's shared-memory G) ----------------
 // A value is a float pair (hi, lo) with |lo| <= ulp(hi) / 2: ~48 significant
 // bits.
@@ -271,10 +176,19 @@ __device__ __forceinline__ void dright_df(int n, float2* __restrict__ C, const f
     for (int e = threadIdx.x; e < n * n; e += DQMC_NT) C[e] = df_mul(A[e], d[e / n]);
 }
 
-// mm_df without transposes, with each operand either FP64 or already split
-// (ADF / BDF: a float2 array) and the result FP64 or double-float (CDF).
-// The split hopping exponentials and the shared-memory G of the mixed path
-// enter without any FP64 instruction.  Same arithmetic as mm_df.
+// Double-float product for the mixed path: C = A * B on the FP32 pipe, each
+// operand either FP64 (split X = Xh + Xl, Xh = fp32(X), Xl = fp32(X - Xh),
+// while staging) or already split (ADF / BDF: a float2 array), the result
+// FP64 or double-float (CDF).  The main term sum_k Ah Bh is accumulated
+// exactly-rounded in a pair of floats: the product is split exactly with one
+// fmaf (TwoProd) and added with TwoSum (Knuth); the cross terms Ah Bl + Al Bh
+// are accumulated in plain FP32 and Al Bl is dropped.  Relative error ~1e-14
+// per product (FP32 alone: ~1e-7, which the wraps' error amplification over
+// ten slices turns into O(1)).  About 12 FP32 instructions per multiply-add,
+// against one FP64 instruction on a pipe ~60x narrower on GB300.  64 x 64
+// tiles, 4 x 4 per thread, k staged 16 at a time (sm: 4 * 16 * 64 floats).
+// C must not alias A or B.  The split hopping exponentials and the
+// shared-memory G of the mixed path enter without any FP64 instruction.
 template <bool ADF, bool BDF, bool CDF>
 __device__ __noinline__ void mm_dfx(int n, void* __restrict__ Cv, const void* __restrict__ Av,
                                     const void* __restrict__ Bv, double* smd) {
