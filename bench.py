@@ -213,7 +213,10 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, seed=3):
     out["thermalize_s"] = therm_s
     for name, prec in (("plain_fp64", _lib.PREC_FP64), ("mixed", _lib.PREC_MIXED)):
         t = time.perf_counter()
-        ks, errs = autotune.tune_safe_mult(specs, tol=1e-6, precision=prec, confs=confs)
+        # a 50x margin on the probes: the propagation error's tail over long
+        # runs is far above its value on a few probe sweeps
+        ks, errs = autotune.tune_safe_mult(specs, tol=1e-6, precision=prec, confs=confs,
+                                           safety=0.02)
         tune_s = time.perf_counter() - t
         ce = []
         for (model, fcls, beta, dt, s), k in zip(specs, ks):
@@ -411,8 +414,6 @@ def main():
         from montecarlo_gb300 import autotune
 
         specs2 = [(model, type(fld), param.beta, param.delta_tau, seed0 + j) for j in range(8)]
-        kk, _ = autotune.tune_safe_mult(specs2, tol=1e-6, precision=_lib.PREC_MIXED)
-        k_tuned = min(kk)
 
         def time_mixed(k):
             cfgs_m = [_lib.ChainConfig(n, nf, M, k, fld.kind, 1, fld.alpha, seed0 + j)
@@ -437,11 +438,19 @@ def main():
             hm.close()
             return v, mp
 
-        # the plain path's safe_mult (same stabilisation work), and the
-        # autotuner's choice for a propagation error <= 0.1 x 1e-6
+        # the plain path's safe_mult (same stabilisation work), and the largest
+        # safe_mult at which every chain's propagation error over the timed
+        # sweeps stays <= 1e-6 (the double-float wraps drift ~30-70x faster
+        # than FP64 ones between stabilisations)
         k_mixed = param.safe_mult
         mixed_v, mp = time_mixed(k_mixed)
-        tuned_v, tuned_mp = time_mixed(k_tuned) if k_tuned != k_mixed else (mixed_v, mp)
+        strict = None
+        for k_try in (k_mixed, 8, 6, 5, 4):
+            v_try, mp_try = (mixed_v, mp) if k_try == k_mixed else time_mixed(k_try)
+            if mp_try <= 1e-6:
+                strict = {"safe_mult": k_try, "value": v_try, "vs_plain_fp64": v_try / value,
+                          "max_propagation_error": mp_try}
+                break
         # |dG| of the mixed path against FP64 for the same field configurations:
         # thermalised configurations of 4 chains, G from scratch at every
         # stabilisation slice, mixed (double-float slice chains) vs FP64
@@ -461,8 +470,7 @@ def main():
         extras["mixed"] = {"value": mixed_v, "unit": "sweeps/s", "vs_plain_fp64": mixed_v / value,
                            "max_dG_vs_fp64_at_stabilisations": dG,
                            "max_propagation_error": mp, "safe_mult": k_mixed,
-                           "autotuned": {"safe_mult": k_tuned, "value": tuned_v,
-                                         "max_propagation_error": tuned_mp},
+                           "strict_propagation_error_1e-6": strict,
                            "note": "wraps and slice chains as double-float products on the FP32 "
                                    "pipe; UDT, reconstruction, ratios, rank-1 updates FP64"}
         # the reference's checkerboard = true on the same ensemble: the
