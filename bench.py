@@ -213,10 +213,11 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, seed=3):
     out["thermalize_s"] = therm_s
     for name, prec in (("plain_fp64", _lib.PREC_FP64), ("mixed", _lib.PREC_MIXED)):
         t = time.perf_counter()
-        # a 50x margin on the probes: the propagation error's tail over long
-        # runs is far above its value on a few probe sweeps
+        # a 200x margin on the probes: the propagation error's tail over long
+        # runs is far above its value on a few probe sweeps (a 50x margin left
+        # 4 of 256 FP64 chains at 1-2e-6 over the timed sweeps)
         ks, errs = autotune.tune_safe_mult(specs, tol=1e-6, precision=prec, confs=confs,
-                                           safety=0.02)
+                                           safety=0.005)
         tune_s = time.perf_counter() - t
         ce = []
         for (model, fcls, beta, dt, s), k in zip(specs, ks):
