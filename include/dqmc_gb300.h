@@ -27,6 +27,12 @@
  *     return at once and complete through dqmc_query / dqmc_synchronize.
  *   - The library has no CPU fallback: without a usable CUDA device every
  *     call that needs one returns DQMC_ERR_CUDA.
+ *   - Complex chains (alpha_imag != 0: a field whose Hubbard-Stratonovich
+ *     constant is complex because its kind does not match the sign of U, the
+ *     reference's ComplexF64 path, fields.jl:294, 372, 421, 530, 600) exchange
+ *     their Green's functions as complex n x n blocks, each entry two doubles
+ *     (re, im) -- Julia's Matrix{ComplexF64} memory layout -- so 2*nf*n*n
+ *     doubles per matrix.  Hopping matrices stay real n x n.
  */
 #ifndef DQMC_GB300_H
 #define DQMC_GB300_H
@@ -37,7 +43,7 @@
 extern "C" {
 #endif
 
-#define DQMC_GB300_ABI_VERSION 5
+#define DQMC_GB300_ABI_VERSION 6
 
 /* status codes */
 #define DQMC_OK 0
@@ -70,8 +76,11 @@ typedef struct {
     int32_t safe_mult;     /* parameters.safe_mult */
     int32_t field;         /* DQMC_FIELD_* */
     int32_t check_propagation_error; /* parameters.check_propagation_error */
-    double alpha;          /* field.alpha */
+    double alpha;          /* field.alpha (its real part for a complex alpha) */
     uint64_t seed;         /* key of the chain's Philox4x32-10 stream */
+    double alpha_imag;     /* imaginary part of field.alpha; nonzero: complex chain
+                              (FP64 only, n_sites <= 128; no device measurements,
+                              global updates, replica exchange or checkerboard) */
 } dqmc_chain_config;
 
 /* Per-chain counters (DQMCAnalysis, statistics.jl:45-51; AcceptanceStatistics,
@@ -84,6 +93,8 @@ typedef struct {
     double max_propagation_error; /* max over all stabilisations of max|dG| */
     double max_reported_error;    /* max of the errors counted above */
     int32_t current_slice, current_range, direction, status;
+    int64_t imaginary_probability; /* proposals with |imag(p)| > 1e-6 (complex chains) */
+    double max_imaginary_probability; /* max |imag(p)| of those */
 } dqmc_stats;
 
 /* ---- lifecycle ------------------------------------------------------------

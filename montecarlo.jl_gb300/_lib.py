@@ -31,7 +31,7 @@ class ChainConfig(C.Structure):
     _fields_ = [("n_sites", C.c_int32), ("n_flavors", C.c_int32), ("slices", C.c_int32),
                 ("safe_mult", C.c_int32), ("field", C.c_int32),
                 ("check_propagation_error", C.c_int32), ("alpha", C.c_double),
-                ("seed", C.c_uint64)]
+                ("seed", C.c_uint64), ("alpha_imag", C.c_double)]
 
 
 class Stats(C.Structure):
@@ -39,7 +39,9 @@ class Stats(C.Structure):
                 ("propagation_errors", C.c_int64), ("negative_probability", C.c_int64),
                 ("max_propagation_error", C.c_double), ("max_reported_error", C.c_double),
                 ("current_slice", C.c_int32), ("current_range", C.c_int32),
-                ("direction", C.c_int32), ("status", C.c_int32)]
+                ("direction", C.c_int32), ("status", C.c_int32),
+                ("imaginary_probability", C.c_int64),
+                ("max_imaginary_probability", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -167,6 +169,18 @@ def buf_to_blocks(buf: np.ndarray, nf: int, n: int) -> np.ndarray:
     return np.transpose(buf.reshape(nf, n, n), (0, 2, 1)).copy()
 
 
+def is_complex(cfg) -> bool:
+    """A chain with a complex field constant (the reference's ComplexF64 path):
+    its matrices cross the ABI as interleaved (re, im) doubles."""
+    return cfg.alpha_imag != 0.0
+
+
+def complex_blocks_to_buf(G: np.ndarray) -> np.ndarray:
+    """(nf, n, n) complex -> flat column-major-per-block (re, im) doubles."""
+    g = np.ascontiguousarray(np.transpose(np.asarray(G, dtype=np.complex128), (0, 2, 1))).ravel()
+    return g.view(np.float64)
+
+
 class Handle:
     """Owns one dqmc_handle (a batch of chains on one device)."""
 
@@ -268,27 +282,31 @@ class Handle:
 
     def _mat_buf(self, chain):
         cfg = self.cfg(chain)
-        return np.zeros(cfg.n_flavors * cfg.n_sites * cfg.n_sites)
+        return np.zeros(cfg.n_flavors * cfg.n_sites * cfg.n_sites * (2 if is_complex(cfg) else 1))
+
+    def _blocks(self, chain, buf):
+        cfg = self.cfg(chain)
+        if is_complex(cfg):
+            buf = buf.view(np.complex128)
+        return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
 
     def greens(self, chain, physical=False):
-        cfg = self.cfg(chain)
         buf = self._mat_buf(chain)
         check(load().dqmc_get_greens(self.h, chain, int(bool(physical)), dptr(buf)))
-        return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
+        return self._blocks(chain, buf)
 
     def greens_into(self, chain, buf, physical=False):
         """Download G into a preallocated flat float64 buffer (no reshaping)."""
         check(load().dqmc_get_greens(self.h, chain, int(bool(physical)), dptr(buf)))
 
     def set_greens(self, chain, G):
-        buf = blocks_to_buf(G)
+        buf = complex_blocks_to_buf(G) if is_complex(self.cfg(chain)) else blocks_to_buf(G)
         check(load().dqmc_set_greens(self.h, chain, dptr(buf)))
 
     def calculate_greens(self, chain, slice_, safe_mult=0):
-        cfg = self.cfg(chain)
         buf = self._mat_buf(chain)
         check(load().dqmc_calculate_greens(self.h, chain, int(slice_), int(safe_mult), dptr(buf)))
-        return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
+        return self._blocks(chain, buf)
 
     def set_measurements(self, chain=-1, enable=True, rate=1, greens=False, sweep=-1, U=0.0,
                          q=None):
@@ -335,12 +353,11 @@ class Handle:
         cfg = self.cfg(chain)
         k = np.ascontiguousarray([p[0] for p in pairs], dtype=np.int32)
         l = np.ascontiguousarray([p[1] for p in pairs], dtype=np.int32)
-        per = cfg.n_flavors * cfg.n_sites * cfg.n_sites
+        per = cfg.n_flavors * cfg.n_sites * cfg.n_sites * (2 if is_complex(cfg) else 1)
         buf = np.zeros(len(pairs) * per)
         check(load().dqmc_calculate_greens_kl(self.h, chain, k.ctypes.data, l.ctypes.data,
                                               len(pairs), int(bool(physical)), dptr(buf)))
-        return [buf_to_blocks(buf[i * per:(i + 1) * per], cfg.n_flavors, cfg.n_sites)
-                for i in range(len(pairs))]
+        return [self._blocks(chain, buf[i * per:(i + 1) * per]) for i in range(len(pairs))]
 
     def global_update(self, kind=GLOBAL_FLIP):
         """One global move of every chain; returns the accepted flags."""
@@ -366,14 +383,17 @@ class Handle:
         return a.value, p.value
 
     def stack(self, chain, which, idx):
+        """u/t/d_stack[idx]; a complex chain's are the factors of its real
+        2n x 2n representation."""
         cfg = self.cfg(chain)
+        n = cfg.n_sites * (2 if is_complex(cfg) else 1)
         if which == 2:
-            out = np.zeros(cfg.n_flavors * cfg.n_sites)
+            out = np.zeros(cfg.n_flavors * n)
             check(load().dqmc_get_stack(self.h, chain, 2, idx, dptr(out)))
-            return out.reshape(cfg.n_flavors, cfg.n_sites)
-        buf = self._mat_buf(chain)
+            return out.reshape(cfg.n_flavors, n)
+        buf = np.zeros(cfg.n_flavors * n * n)
         check(load().dqmc_get_stack(self.h, chain, which, idx, dptr(buf)))
-        return buf_to_blocks(buf, cfg.n_flavors, cfg.n_sites)
+        return buf_to_blocks(buf, cfg.n_flavors, n)
 
 
 DQMC_ERR_OOM = 3

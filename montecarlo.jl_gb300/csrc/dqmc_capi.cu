@@ -18,6 +18,7 @@
 #include "philox.h"
 
 using dqmc_host::fill_tables;
+using dqmc_host::fill_tables_complex;
 using dqmc_host::generate_chunks;
 
 namespace {
@@ -40,7 +41,55 @@ int cuda_fail(cudaError_t e, const char* what) {
         if (_e != cudaSuccess) return cuda_fail(_e, what); \
     } while (0)
 
-size_t mat_elems(const dqmc_chain_config& c) { return (size_t)c.n_flavors * c.n_sites * c.n_sites; }
+bool is_cplx(const dqmc_chain_config& c) { return c.alpha_imag != 0.0; }
+// matrix dimension on the device: a complex chain keeps the real 2n x 2n
+// representation [[Re, -Im], [Im, Re]] of its n x n complex matrices
+size_t mat_n(const dqmc_chain_config& c) {
+    return is_cplx(c) ? 2 * (size_t)c.n_sites : (size_t)c.n_sites;
+}
+size_t mat_elems(const dqmc_chain_config& c) { return (size_t)c.n_flavors * mat_n(c) * mat_n(c); }
+// doubles of one matrix as the caller passes it (complex: re, im per entry)
+size_t user_elems(const dqmc_chain_config& c) {
+    return (is_cplx(c) ? 2 : 1) * (size_t)c.n_flavors * c.n_sites * c.n_sites;
+}
+// representation -> interleaved complex (Julia's Matrix{ComplexF64} layout), nf blocks
+void rep_to_complex(const dqmc_chain_config& c, const double* E, double* out) {
+    const size_t n = c.n_sites, n2 = 2 * n;
+    for (size_t b = 0; b < (size_t)c.n_flavors; ++b) {
+        const double* Eb = E + b * n2 * n2;
+        double* ob = out + 2 * b * n * n;
+        for (size_t col = 0; col < n; ++col)
+            for (size_t r = 0; r < n; ++r) {
+                ob[2 * (col * n + r)] = Eb[col * n2 + r];
+                ob[2 * (col * n + r) + 1] = Eb[col * n2 + n + r];
+            }
+    }
+}
+void complex_to_rep(const dqmc_chain_config& c, const double* in, double* E) {
+    const size_t n = c.n_sites, n2 = 2 * n;
+    for (size_t b = 0; b < (size_t)c.n_flavors; ++b) {
+        double* Eb = E + b * n2 * n2;
+        const double* ib = in + 2 * b * n * n;
+        for (size_t col = 0; col < n; ++col)
+            for (size_t r = 0; r < n; ++r) {
+                const double re = ib[2 * (col * n + r)], im = ib[2 * (col * n + r) + 1];
+                Eb[col * n2 + r] = re;
+                Eb[col * n2 + n + r] = im;
+                Eb[(n + col) * n2 + r] = -im;
+                Eb[(n + col) * n2 + n + r] = re;
+            }
+    }
+}
+// a real n x n matrix as the representation of a complex one: diag(A, A)
+void real_to_rep(size_t n, const double* A, double* E) {
+    const size_t n2 = 2 * n;
+    for (size_t e = 0; e < n2 * n2; ++e) E[e] = 0.0;
+    for (size_t col = 0; col < n; ++col)
+        for (size_t r = 0; r < n; ++r) {
+            E[col * n2 + r] = A[col * n + r];
+            E[(n + col) * n2 + n + r] = A[col * n + r];
+        }
+}
 
 struct Layout {
     size_t bytes;
@@ -53,10 +102,11 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 Layout layout_of(const dqmc_chain_config& c, int prec) {
     Layout L;
-    const size_t n = c.n_sites, nf = c.n_flavors, ms = mat_elems(c) * sizeof(double);
+    const size_t n = mat_n(c), nf = c.n_flavors, ms = mat_elems(c) * sizeof(double);
+    const size_t nconf = (size_t)c.n_sites * c.slices;
     const int nr = (c.slices + c.safe_mult - 1) / c.safe_mult;
     size_t o = 0;
-    L.off_conf = o; o = align256(o + n * c.slices);
+    L.off_conf = o; o = align256(o + nconf);
     L.off_hop = o; o = align256(o + 4 * n * n * sizeof(double));
     size_t* mats[] = {&L.off_G, &L.off_Gtmp, &L.off_Ul, &L.off_Ur, &L.off_Tl, &L.off_Tr,
                       &L.off_tmp1, &L.off_tmp2, &L.off_currU, &L.off_out};
@@ -70,7 +120,7 @@ Layout layout_of(const dqmc_chain_config& c, int prec) {
     L.off_pivot = o; o = align256(o + nf * n * sizeof(int));
     L.off_meas = o; o = align256(o + DQMC_MEAS_DOUBLES(n, nf) * sizeof(double));
     L.off_qcs = o; o = align256(o + 2 * n * sizeof(double));
-    L.off_tconf = o; o = align256(o + n * c.slices);
+    L.off_tconf = o; o = align256(o + nconf);
     L.off_tempvf = o; o = align256(o + nf * n * sizeof(double));
     L.off_hopdf = o; o = align256(o + 2 * n * n * sizeof(float2));
     L.bytes = o;
@@ -173,7 +223,10 @@ int validate_config(const dqmc_chain_config& c, int i) {
         return fail(DQMC_ERR_INVALID, "n_flavors does not match the field kind");
     if ((c.slices + c.safe_mult - 1) / c.safe_mult > DQMC_MAX_CHUNKS)
         return fail(DQMC_ERR_INVALID, "too many stabilisation chunks (max 256)");
-    if (!(c.alpha == c.alpha)) return fail(DQMC_ERR_INVALID, "alpha is NaN");
+    if (!std::isfinite(c.alpha) || !std::isfinite(c.alpha_imag))
+        return fail(DQMC_ERR_INVALID, "alpha is not finite");
+    if (is_cplx(c) && c.n_sites > 128)
+        return fail(DQMC_ERR_INVALID, "complex chains (alpha_imag != 0) need n_sites <= 128");
     return DQMC_OK;
 }
 
@@ -181,12 +234,15 @@ int validate_config(const dqmc_chain_config& c, int i) {
 void fill_descriptor(DqmcChain& d, const dqmc_chain_config& c, char* b, const Layout& L,
                      int precision) {
     memset(&d, 0, sizeof(d));
-    d.n = c.n_sites; d.nf = c.n_flavors; d.M = c.slices; d.k = c.safe_mult; d.kind = c.field;
+    d.n = (int)mat_n(c); d.nf = c.n_flavors; d.M = c.slices; d.k = c.safe_mult; d.kind = c.field;
+    d.ns = c.n_sites;
+    d.cplx = is_cplx(c) ? 1 : 0;
     d.check_prop = c.check_propagation_error ? 1 : 0;
     d.prec = precision;
     d.nr = generate_chunks(c.slices, c.safe_mult, d.rfirst, d.rlast);
-    fill_tables(d, c.field, c.alpha);
-    const size_t nn = (size_t)c.n_sites * c.n_sites;
+    if (d.cplx) fill_tables_complex(d, c.field, c.alpha, c.alpha_imag);
+    else fill_tables(d, c.field, c.alpha);
+    const size_t nn = mat_n(c) * mat_n(c);
     double* hop = (double*)(b + L.off_hop);
     d.conf = (int8_t*)(b + L.off_conf);
     d.eT2 = hop; d.eT2inv = hop + nn; d.eTh = hop + 2 * nn; d.eThinv = hop + 3 * nn;
@@ -264,8 +320,11 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
     *out = nullptr;
     if (precision != DQMC_PREC_FP64 && precision != DQMC_PREC_MIXED)
         return fail(DQMC_ERR_INVALID, "dqmc_create: unknown precision");
-    for (int i = 0; i < n_chains; ++i)
+    for (int i = 0; i < n_chains; ++i) {
         if (int st = validate_config(chains[i], i)) return st;
+        if (is_cplx(chains[i]) && precision != DQMC_PREC_FP64)
+            return fail(DQMC_ERR_INVALID, "dqmc_create: complex chains run in FP64 only");
+    }
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev == 0)
@@ -276,7 +335,7 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
     h->device = device;
     h->precision = precision;
     h->cfg.assign(chains, chains + n_chains);
-    for (int i = 0; i < n_chains; ++i) h->n_max = std::max(h->n_max, (int)chains[i].n_sites);
+    for (int i = 0; i < n_chains; ++i) h->n_max = std::max(h->n_max, (int)mat_n(chains[i]));
     size_t total = 0;
     std::vector<size_t> base(n_chains);
     for (int i = 0; i < n_chains; ++i) {
@@ -344,10 +403,19 @@ int dqmc_set_hopping(dqmc_handle* h, int chain, const double* a, const double* b
     CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
     for (int i = lo; i < hi; ++i) {
         if (!h->host[i].active) continue;  // free pool slot
-        const size_t nn = (size_t)h->cfg[i].n_sites * h->cfg[i].n_sites;
+        const size_t nn = mat_n(h->cfg[i]) * mat_n(h->cfg[i]);
         if (chain == -1 && h->cfg[i].n_sites != h->cfg[lo].n_sites)
             return fail(DQMC_ERR_INVALID, "dqmc_set_hopping(-1): chains have different n_sites");
         const double* src[4] = {a, b, c, d};
+        std::vector<double> rep;
+        if (is_cplx(h->cfg[i])) {  // diag(A, A): the representation of the real matrix
+            const size_t ns = h->cfg[i].n_sites;
+            rep.resize(4 * nn);
+            for (int m = 0; m < 4; ++m) {
+                real_to_rep(ns, src[m], rep.data() + m * nn);
+                src[m] = rep.data() + m * nn;
+            }
+        }
         double* dst[4] = {(double*)h->host[i].eT2, (double*)h->host[i].eT2inv,
                           (double*)h->host[i].eTh, (double*)h->host[i].eThinv};
         for (int m = 0; m < 4; ++m)
@@ -466,6 +534,8 @@ static void fill_stats(const DqmcChain& d, dqmc_stats* s) {
     s->negative_probability = d.n_neg_p;
     s->max_propagation_error = d.prop_err_max;
     s->max_reported_error = d.prop_err_reported;
+    s->imaginary_probability = d.n_imag_p;
+    s->max_imaginary_probability = d.max_imag_p;
     s->current_slice = d.current_slice;
     s->current_range = d.current_range;
     s->direction = d.direction;
@@ -532,10 +602,23 @@ int dqmc_get_timers(dqmc_handle* h, int chain, uint64_t* out) {
     return DQMC_OK;
 }
 
-static int download_mat(dqmc_handle* h, int chain, const double* src, double* out) {
-    const size_t bytes = mat_elems(h->cfg[chain]) * sizeof(double);
-    CUDA_TRY(cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToHost, h->stream), "download matrix");
+// one matrix to the caller: as stored, or (complex chain, raw = false) as
+// interleaved complex blocks
+static int download_mat(dqmc_handle* h, int chain, const double* src, double* out,
+                        bool raw = false) {
+    const dqmc_chain_config& c = h->cfg[chain];
+    const size_t bytes = mat_elems(c) * sizeof(double);
+    if (raw || !is_cplx(c)) {
+        CUDA_TRY(cudaMemcpyAsync(out, src, bytes, cudaMemcpyDeviceToHost, h->stream),
+                 "download matrix");
+        CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+        return DQMC_OK;
+    }
+    std::vector<double> rep(mat_elems(c));
+    CUDA_TRY(cudaMemcpyAsync(rep.data(), src, bytes, cudaMemcpyDeviceToHost, h->stream),
+             "download matrix");
     CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    rep_to_complex(c, rep.data(), out);
     return DQMC_OK;
 }
 
@@ -545,7 +628,7 @@ static int launch_one(dqmc_handle* h, int chain, int op, int arg0, int arg1) {
     CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
     if (h->host_dirty) if (int st = push_descriptors(h)) return st;
     CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains + chain, 1, op, arg0, arg1, h->stream,
-                                      h->cfg[chain].n_sites),
+                                      (int)mat_n(h->cfg[chain])),
              "chain kernel launch");
     CUDA_TRY(cudaStreamSynchronize(h->stream), "chain kernel");
     return pull_descriptors(h);
@@ -568,6 +651,12 @@ int dqmc_set_greens(dqmc_handle* h, int chain, const double* in) {
     if (!in) return fail(DQMC_ERR_INVALID, "dqmc_set_greens: null in");
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    std::vector<double> rep;
+    if (is_cplx(h->cfg[chain])) {
+        rep.resize(mat_elems(h->cfg[chain]));
+        complex_to_rep(h->cfg[chain], in, rep.data());
+        in = rep.data();
+    }
     CUDA_TRY(cudaMemcpyAsync(h->host[chain].G, in, mat_elems(h->cfg[chain]) * sizeof(double),
                              cudaMemcpyHostToDevice, h->stream),
              "upload greens");
@@ -601,7 +690,7 @@ int dqmc_get_stack(dqmc_handle* h, int chain, int which, int idx, double* out) {
         return DQMC_OK;
     }
     const double* base = which == 0 ? d.ustack : d.tstack;
-    return download_mat(h, chain, base + (idx - 1) * ms, out);
+    return download_mat(h, chain, base + (idx - 1) * ms, out, true);
 }
 
 /* ---- equal-time measurements ---------------------------------------------- */
@@ -621,6 +710,9 @@ int dqmc_set_measurements(dqmc_handle* h, int chain, const dqmc_measure_config* 
         if (!d.active) continue;  // free pool slot
         if (cfg->q_cos && chain == -1 && h->cfg[i].n_sites != h->cfg[lo].n_sites)
             return fail(DQMC_ERR_INVALID, "dqmc_set_measurements(-1): chains have different n_sites");
+        if (cfg->enable && d.cplx)
+            return fail(DQMC_ERR_INVALID, "dqmc_set_measurements: no device measurements on a "
+                                          "complex chain (download its Green's function instead)");
         d.meas_enable = cfg->enable ? 1 : 0;
         if (cfg->measure_rate >= 1) d.meas_rate = cfg->measure_rate;
         d.meas_greens = cfg->greens_mean ? 1 : 0;
@@ -723,8 +815,8 @@ int dqmc_set_checkerboard(dqmc_handle* h, int chain, int n_parts, const double* 
             d.cb_np = 0;
             continue;
         }
-        const int n = d.n;
-        if (chain == -1 && n != h->host[lo].n)
+        const int n = d.ns;  // the caller's data: per site of the lattice
+        if (chain == -1 && n != h->host[lo].ns)
             return fail(DQMC_ERR_INVALID, "dqmc_set_checkerboard(-1): chains have different n_sites");
         const size_t per = (size_t)n * (1 + 3 * (size_t)n_parts), cnt = 4 * per;
         for (size_t m = 0; m < 4; ++m) {
@@ -741,22 +833,28 @@ int dqmc_set_checkerboard(dqmc_handle* h, int chain, int n_parts, const double* 
                 }
             }
         }
-        // device layout: per factor D[n] and per part c[n], s[n]; then the
-        // partners as int32, per factor and part
-        const size_t per_d = (size_t)n * (1 + 2 * (size_t)n_parts);
+        // device layout: per factor D[dn] and per part c[dn], s[dn]; then the
+        // partners as int32, per factor and part.  A complex chain's
+        // representation needs diag(X, X): every site entry twice, partners
+        // of the second copy shifted by n.
+        const int dn = d.n, reps = dn / n;
+        const size_t per_d = (size_t)dn * (1 + 2 * (size_t)n_parts);
         std::vector<double> dv(4 * per_d);
-        std::vector<int32_t> pv(4 * (size_t)n_parts * n);
+        std::vector<int32_t> pv(4 * (size_t)n_parts * dn);
         for (size_t m = 0; m < 4; ++m) {
             const double* f = data + m * per;
             double* g = dv.data() + m * per_d;
-            for (int k = 0; k < n; ++k) g[k] = f[k];
+            for (int r = 0; r < reps; ++r)
+                for (int k = 0; k < n; ++k) g[r * n + k] = f[k];
             for (int p = 0; p < n_parts; ++p) {
                 const double* fp = f + n + (size_t)p * 3 * n;
-                for (int k = 0; k < n; ++k) {
-                    g[n + (size_t)p * 2 * n + k] = fp[k];
-                    g[n + (size_t)p * 2 * n + n + k] = fp[n + k];
-                    pv[(m * n_parts + p) * (size_t)n + k] = (int32_t)fp[2 * n + k];
-                }
+                for (int r = 0; r < reps; ++r)
+                    for (int k = 0; k < n; ++k) {
+                        const int q = (int)fp[2 * n + k];
+                        g[dn + (size_t)p * 2 * dn + r * n + k] = fp[k];
+                        g[dn + (size_t)p * 2 * dn + dn + r * n + k] = fp[n + k];
+                        pv[(m * n_parts + p) * (size_t)dn + r * n + k] = q < 0 ? -1 : q + r * n;
+                    }
             }
         }
         (void)cnt;
@@ -823,10 +921,16 @@ int dqmc_calculate_greens_kl(dqmc_handle* h, int chain, const int32_t* k, const 
             st = fail(DQMC_ERR_NUMERICAL, "chain " + std::to_string(chain) + " reported status " +
                                               std::to_string(h->host[chain].status));
         if (st == DQMC_OK) {
-            e = cudaMemcpyAsync(out, d_out, ms * npairs * sizeof(double), cudaMemcpyDeviceToHost,
-                                h->stream);
+            const dqmc_chain_config& cc = h->cfg[chain];
+            std::vector<double> rep;
+            if (is_cplx(cc)) rep.resize(ms * npairs);
+            e = cudaMemcpyAsync(is_cplx(cc) ? rep.data() : out, d_out, ms * npairs * sizeof(double),
+                                cudaMemcpyDeviceToHost, h->stream);
             if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
             if (e != cudaSuccess) st = cuda_fail(e, "dqmc_calculate_greens_kl: download");
+            else if (is_cplx(cc))
+                for (int p = 0; p < npairs; ++p)
+                    rep_to_complex(cc, rep.data() + (size_t)p * ms, out + (size_t)p * user_elems(cc));
         }
         h->host[chain].ut_pairs = nullptr;
         h->host[chain].ut_out = nullptr;
@@ -850,6 +954,16 @@ static int check_between_sweeps(dqmc_handle* h) {
     return DQMC_OK;
 }
 
+// global updates and replica exchange need the determinant's phase, which
+// the real representation of a complex chain does not give
+static int check_no_complex(dqmc_handle* h, const char* what) {
+    for (size_t i = 0; i < h->host.size(); ++i)
+        if (h->host[i].active && h->host[i].cplx)
+            return fail(DQMC_ERR_INVALID, std::string(what) + ": chain " + std::to_string(i) +
+                                              " is complex (no global updates on complex chains)");
+    return DQMC_OK;
+}
+
 // sweeps with a scheduled global update must start between sweeps
 static int check_scheduled(dqmc_handle* h) {
     bool any = false;
@@ -865,6 +979,7 @@ int dqmc_global_update(dqmc_handle* h, int kind, int32_t* accepted) {
         return fail(DQMC_ERR_INVALID, "dqmc_global_update: unknown kind");
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     if (int st = check_between_sweeps(h)) return st;
+    if (int st = check_no_complex(h, "dqmc_global_update")) return st;
     std::vector<long long> before(h->host.size());
     for (size_t i = 0; i < h->host.size(); ++i) before[i] = h->host[i].g_accepted;
     if (int st = launch(h, DQMC_OP_GLOBAL, kind, 0, true)) return st;
@@ -884,6 +999,9 @@ int dqmc_set_global_schedule(dqmc_handle* h, int chain, int kind) {
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     for (int i = lo; i < hi; ++i) {
         if (!h->host[i].active) continue;
+        if (kind >= 0 && h->host[i].cplx)
+            return fail(DQMC_ERR_INVALID, "dqmc_set_global_schedule: no global updates on a "
+                                          "complex chain");
         h->host[i].global_kind = kind;
         h->host[i].sched_calls = 0;
     }
@@ -910,6 +1028,7 @@ int dqmc_replica_exchange(dqmc_handle* h, const int32_t* partner, int32_t* accep
                                           "n_sites, n_flavors, slices and field kind");
     }
     if (int st = check_between_sweeps(h)) return st;
+    if (int st = check_no_complex(h, "dqmc_replica_exchange")) return st;
     std::vector<long long> before(nc);
     for (int i = 0; i < nc; ++i) {
         before[i] = h->host[i].g_accepted;
@@ -982,6 +1101,8 @@ int dqmc_pool_create(int device, int max_slots, int64_t budget_bytes, int precis
 int dqmc_pool_admit(dqmc_handle* h, const dqmc_chain_config* cfg, int* slot) {
     if (!h || !h->pool || !cfg || !slot) return fail(DQMC_ERR_INVALID, "dqmc_pool_admit: bad arguments");
     if (int st = validate_config(*cfg, -1)) return st;
+    if (is_cplx(*cfg) && h->precision != DQMC_PREC_FP64)
+        return fail(DQMC_ERR_INVALID, "dqmc_pool_admit: complex chains run in FP64 only");
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     int free_slot = -1;
     for (size_t i = 0; i < h->host.size(); ++i)

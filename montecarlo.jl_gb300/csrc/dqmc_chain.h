@@ -94,6 +94,19 @@ struct DqmcChain {
     int cb_np, pad3;
     const double* cb;
     const int* cbp;
+    // complex chain (a complex field constant, the reference's ComplexF64
+    // path): every matrix is the real 2 ns x 2 ns representation
+    // [[Re, -Im], [Im, Re]] of the ns x ns complex one (n = 2 ns; the
+    // adjoint of a complex matrix is the transpose of its representation),
+    // ns = sites (= n on a real chain).  Imaginary parts of the proposal
+    // tables and interaction exponentials, and the sign-problem statistics of
+    // sweep_spatial (local_updates.jl:33-46): proposals with |imag(p)| > 1e-6
+    // and the largest such |imag(p)|.
+    int cplx, ns;
+    double delta0i[16], delta1i[16], wbosoni[16];
+    double evi[2][4], evinvi[2][4];
+    long long n_imag_p;
+    double max_imag_p;
 };
 #define DQMC_CB_MAXPARTS 12
 

@@ -55,7 +55,7 @@ __device__ __forceinline__ bool g_resident_possible(const Ctx& x) {
 // entirely on the FP32 pipe; it is rounded back to FP64 whenever it leaves
 // shared memory.  (At n = 16 the split arithmetic costs more than it saves.)
 __device__ __forceinline__ bool df_mode(const Ctx& x) {
-    return x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 32 && !x.c->cb;
+    return x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 32 && !x.c->cb && !x.c->cplx;
 }
 __device__ __forceinline__ bool df_resident(const Ctx& x) { return df_mode(x) && x.s->gres; }
 __device__ __forceinline__ float2* arena_df(const Ctx& x) {
@@ -198,24 +198,38 @@ __device__ __noinline__ void cb_apply(const Ctx& x, int m, int mode, double* out
 }
 
 // interaction_matrix_exp! (fields.jl:380-386, 429-438, 548-560, 618-624)
-// into shared memory: ev[b*n + i]
+// into shared memory: ev[b*n + i]; on a complex chain Re at ev[b*n + i] and
+// Im at ev[b*n + ns + i] (i < ns)
 __device__ __noinline__ void interaction_exp(const Ctx& x, int slice, bool inverse) {
     const DqmcChain& c = *x.c;
-    const int8_t* s = c.conf + (size_t)(slice - 1) * x.n;
+    const int ns = c.ns;
+    const int8_t* s = c.conf + (size_t)(slice - 1) * ns;
     const bool ghq = (c.kind >= 2);
-    for (int e = threadIdx.x; e < x.nf * x.n; e += DQMC_NT) {
-        int b = e / x.n, i = e % x.n;
+    for (int e = threadIdx.x; e < x.nf * ns; e += DQMC_NT) {
+        int b = e / ns, i = e % ns;
         int v = ghq ? (int)s[i] - 1 : (s[i] > 0 ? 1 : 0);
-        x.s->ev[e] = inverse ? c.evinv[b][v] : c.ev[b][v];
+        x.s->ev[b * x.n + i] = inverse ? c.evinv[b][v] : c.ev[b][v];
+        if (c.cplx) x.s->ev[b * x.n + ns + i] = inverse ? c.evinvi[b][v] : c.evi[b][v];
     }
     __syncthreads();
+}
+// Diagonal(eV) * B and A * Diagonal(eV) with the current slice's exponentials
+// (complex on a complex chain; conj: adjoint(eV))
+__device__ __forceinline__ void ev_left(const Ctx& x, double* C, const double* d, const double* B,
+                                        bool conj = false) {
+    if (x.c->cplx) dleft_c(x.n, C, d, B, conj);
+    else dleft(x.n, C, d, B);
+}
+__device__ __forceinline__ void ev_right(const Ctx& x, double* C, const double* A, const double* d) {
+    if (x.c->cplx) dright_c(x.n, C, A, d, false);
+    else dright(x.n, C, A, d);
 }
 
 // multiply_slice_matrix_left!: M <- eT2 * eV * M  (stack.jl:319-327)
 __device__ __noinline__ void slice_left(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, false);
     for (int b = 0; b < x.nf; ++b) {
-        dleft(x.n, blk(x.c->tmp1, x, b), x.s->ev + b * x.n, blk(M, x, b));
+        ev_left(x, blk(x.c->tmp1, x, b), x.s->ev + b * x.n, blk(M, x, b));
         __syncthreads();
         if (x.c->cb)
             cb_apply(x, 0, 0, blk(M, x, b), blk(x.c->tmp1, x, b), blk(x.c->tmp2, x, b));
@@ -233,7 +247,7 @@ __device__ __noinline__ void slice_right(const Ctx& x, int slice, double* M, boo
         else
             smm<false, true>(x, wrap, blk(x.c->tmp1, x, b), blk(M, x, b), x.c->eT2);
         __syncthreads();
-        dright(x.n, blk(M, x, b), blk(x.c->tmp1, x, b), x.s->ev + b * x.n);
+        ev_right(x, blk(M, x, b), blk(x.c->tmp1, x, b), x.s->ev + b * x.n);
         __syncthreads();
     }
 }
@@ -241,7 +255,7 @@ __device__ __noinline__ void slice_right(const Ctx& x, int slice, double* M, boo
 __device__ __noinline__ void slice_inv_right(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, true);
     for (int b = 0; b < x.nf; ++b) {
-        dright(x.n, blk(x.c->tmp1, x, b), blk(M, x, b), x.s->ev + b * x.n);
+        ev_right(x, blk(x.c->tmp1, x, b), blk(M, x, b), x.s->ev + b * x.n);
         __syncthreads();
         if (x.c->cb)
             cb_apply(x, 1, 1, blk(M, x, b), blk(x.c->tmp1, x, b), blk(x.c->tmp2, x, b));
@@ -259,7 +273,7 @@ __device__ __noinline__ void slice_inv_left(const Ctx& x, int slice, double* M, 
         else
             smm<true, false>(x, wrap, blk(x.c->tmp1, x, b), x.c->eT2inv, blk(M, x, b));
         __syncthreads();
-        dleft(x.n, blk(M, x, b), x.s->ev + b * x.n, blk(x.c->tmp1, x, b));
+        ev_left(x, blk(M, x, b), x.s->ev + b * x.n, blk(x.c->tmp1, x, b));
         __syncthreads();
     }
 }
@@ -272,7 +286,7 @@ __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* 
         else
             smm<true, false>(x, false, blk(x.c->tmp1, x, b), x.c->eT2, blk(M, x, b));
         __syncthreads();
-        dleft(x.n, blk(M, x, b), x.s->ev + b * x.n, blk(x.c->tmp1, x, b));
+        ev_left(x, blk(M, x, b), x.s->ev + b * x.n, blk(x.c->tmp1, x, b), true);
         __syncthreads();
     }
 }
@@ -558,14 +572,26 @@ __device__ __noinline__ void build_stack(const Ctx& x) {
     __syncthreads();
 }
 
-// max |Gtmp - G| (stack.jl:646, 701); NaN propagates
+// max |Gtmp - G| (stack.jl:646, 701); NaN propagates.  On a complex chain
+// the modulus of the complex difference, read from the representation's
+// left half (Re rows 0..ns-1, Im rows ns..2ns-1).
 __device__ __noinline__ void record_prop_error(const Ctx& x) {
     DqmcChain& c = *x.c;
-    const int cnt = x.nf * (int)x.nn;
     double m = 0.0;
-    for (int e = threadIdx.x; e < cnt; e += DQMC_NT) {
-        double d = fabs(c.Gtmp[e] - c.G[e]);
-        if (d > m || d != d) m = d;
+    if (c.cplx) {
+        const int ns = c.ns, cnt = x.nf * ns * ns;
+        for (int e = threadIdx.x; e < cnt; e += DQMC_NT) {
+            const int b = e / (ns * ns), r = e % ns, col = (e / ns) % ns;
+            const size_t at = (size_t)b * x.nn + (size_t)col * x.n + r;
+            double d = hypot(c.Gtmp[at] - c.G[at], c.Gtmp[at + ns] - c.G[at + ns]);
+            if (d > m || d != d) m = d;
+        }
+    } else {
+        const int cnt = x.nf * (int)x.nn;
+        for (int e = threadIdx.x; e < cnt; e += DQMC_NT) {
+            double d = fabs(c.Gtmp[e] - c.G[e]);
+            if (d > m || d != d) m = d;
+        }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -733,6 +759,215 @@ __device__ void flush_delayed(const Ctx& x, int p) {
     __syncthreads();
 }
 
+// sweep_spatial on a complex chain (local_updates.jl:23-60 with the complex
+// calculate_detratio! methods, fields.jl:63-66 and 128-140, vldiv22!,
+// fields.jl:215-227, and update_greens!, fields.jl:271-286) on the real
+// representation E of G (n = 2 ns).  An accepted move at site j updates
+// G -= (I - G)[:, j] (Delta/R) G[j, :]; on E that is the rank-2 update
+// E -= a1 b1^T + a2 b2^T with a1 = e_j - E[:, j], a2 = e_(ns+j) - E[:, ns+j],
+// b1 = wr E[j, :] - wi E[ns+j, :], b2 = wi E[j, :] + wr E[ns+j, :], w = Delta/R.
+// Thread 0 decides in the reference's complex operation order from a
+// shared-memory mirror of G_jj = (E[j, j], E[ns+j, j]); the update vectors are
+// formed from E (plus the pending updates when E is in global memory) and
+// applied as in sweep_spatial.
+__device__ __noinline__ long long sweep_spatial_cplx(const Ctx& x) {
+    DqmcChain& c = *x.c;
+    const int n = x.n, nf = x.nf, m = c.ns;
+    const int slice = c.current_slice;
+    int8_t* s = c.conf + (size_t)(slice - 1) * m;
+    const bool ghq = (c.kind >= 2);
+    const bool twoflv = (nf == 2);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    double* diag = x.s->ev;  // [b*n + k]: Re G_b[k, k]; [b*n + m + k]: Im G_b[k, k]
+    for (int e = tid; e < nf * m; e += DQMC_NT) {
+        const int b = e / m, k = e % m;
+        const size_t at = (size_t)b * x.nn + (size_t)k * n + k;
+        diag[b * n + k] = c.G[at];
+        diag[b * n + m + k] = c.G[at + m];
+    }
+    __syncthreads();
+    // per block b: a1, a2, b1, b2 at vec + (4 b + q) n (4 nf n <= 2048 doubles)
+    double* vec = &x.s->r1.col[0][0];
+    long long acc_count = 0;
+    int i = 0, round = 0;
+    const bool delayed = !x.s->gres;
+    const int kcap = n < DQMC_DELAY ? n : DQMC_DELAY;  // even: two columns per accepted move
+    int pending = 0;
+    while (true) {
+        if (tid == 0) {
+            int j = i;
+            for (; j < m; ++j) {
+                int t;
+                int xnew = 0;
+                double gr = 1.0, gq = 1.0;
+                if (ghq) {
+                    const int xold = s[j];
+                    const uint64_t w = dqmc_philox_word(c.key, c.ctr);
+                    c.ctr += 1;
+                    const int r = dqmc_word_to_choice3(w);
+                    xnew = r + (r + 1 >= xold ? 2 : 1);  // choices[x_old, r+1] (fields.jl:534)
+                    t = (xold - 1) * 4 + (xnew - 1);
+                    gr = c.gam[xnew - 1];
+                    gq = c.gam[xold - 1];
+                } else {
+                    t = s[j] > 0 ? 1 : 0;
+                }
+                const double dre[2] = {c.delta0[t], c.delta1[t]};
+                const double dim[2] = {c.delta0i[t], c.delta1i[t]};
+                double Rr[2] = {0.0, 0.0}, Ri[2] = {0.0, 0.0};
+                double detr, deti;
+                if (!twoflv) {
+                    // R = 1.0 + Delta * (1.0 - G[i, i]); detratio = R * R
+                    const double o_r = __dsub_rn(1.0, diag[j]), o_i = -diag[m + j];
+                    const double pr = __dsub_rn(__dmul_rn(dre[0], o_r), __dmul_rn(dim[0], o_i));
+                    const double pi = __dadd_rn(__dmul_rn(dre[0], o_i), __dmul_rn(dim[0], o_r));
+                    Rr[0] = __dadd_rn(1.0, pr);
+                    Ri[0] = pi;
+                    detr = __dsub_rn(__dmul_rn(Rr[0], Rr[0]), __dmul_rn(Ri[0], Ri[0]));
+                    deti = __dadd_rn(__dmul_rn(Rr[0], Ri[0]), __dmul_rn(Ri[0], Rr[0]));
+                } else {
+                    // R.re = 1 + Dr (1 - G.re) + Di G.im; R.im = Di (1 - G.re) - Dr G.im;
+                    // detratio = prod(R)
+                    for (int b = 0; b < 2; ++b) {
+                        const double omg = __dsub_rn(1.0, diag[b * n + j]);
+                        const double gim = diag[b * n + m + j];
+                        Rr[b] = __dadd_rn(__dadd_rn(1.0, __dmul_rn(dre[b], omg)),
+                                          __dmul_rn(dim[b], gim));
+                        Ri[b] = __dsub_rn(__dmul_rn(dim[b], omg), __dmul_rn(dre[b], gim));
+                    }
+                    detr = __dsub_rn(__dmul_rn(Rr[0], Rr[1]), __dmul_rn(Ri[0], Ri[1]));
+                    deti = __dadd_rn(__dmul_rn(Rr[0], Ri[1]), __dmul_rn(Ri[0], Rr[1]));
+                }
+                if (ghq) {  // detratio * gamma[x_new] / gamma[x_old]
+                    detr = __ddiv_rn(__dmul_rn(detr, gr), gq);
+                    deti = __ddiv_rn(__dmul_rn(deti, gr), gq);
+                }
+                // p = exp(-dE_boson) * detratio
+                const double wr = c.wboson[t], wi = c.wbosoni[t];
+                const double p = __dsub_rn(__dmul_rn(wr, detr), __dmul_rn(wi, deti));
+                const double pim = __dadd_rn(__dmul_rn(wr, deti), __dmul_rn(wi, detr));
+                if (fabs(pim) > 1e-6) {
+                    c.n_imag_p += 1;
+                    if (fabs(pim) > c.max_imag_p) c.max_imag_p = fabs(pim);
+                }
+                if (p < 0.0) c.n_neg_p += 1;
+                int accept;
+                if (p > 1.0) {
+                    accept = 1;
+                } else {
+                    const uint64_t w = dqmc_philox_word(c.key, c.ctr);
+                    c.ctr += 1;
+                    accept = dqmc_word_to_uniform(w) < p;
+                }
+                c.proposals += 1;
+                if (accept) {
+                    // invRDelta_b = Delta_b / R_b = f (Delta conj(R)), f = 1 / |R|^2
+                    for (int b = 0; b < nf; ++b) {
+                        const double f =
+                            1.0 / (Rr[b] * Rr[b] + Ri[b] * Ri[b]);
+                        x.s->sxd[2 * b] = f * (dre[b] * Rr[b] + dim[b] * Ri[b]);
+                        x.s->sxd[2 * b + 1] = f * (dim[b] * Rr[b] - dre[b] * Ri[b]);
+                    }
+                    s[j] = ghq ? (int8_t)xnew : (int8_t)(-s[j]);
+                    c.accepted += 1;
+                    break;
+                }
+            }
+            x.s->sxi[2 + (round & 1)] = j;
+        }
+        __syncthreads();  // also: the previous round's update is complete
+        const int j = x.s->sxi[2 + (round & 1)];
+        ++round;
+        if (j >= m) {
+            if (pending > 0) flush_delayed(x, pending);
+            break;
+        }
+        acc_count += 1;
+        for (int e = tid; e < nf * n; e += DQMC_NT) {
+            const int b = e / n, k = e % n;
+            const double* g = c.G + (size_t)b * x.nn;
+            double cj = g[(size_t)j * n + k];        // E[k, j]
+            double cJ = g[(size_t)(m + j) * n + k];  // E[k, m + j]
+            double rj = g[(size_t)k * n + j];        // E[j, k]
+            double rJ = g[(size_t)k * n + m + j];    // E[m + j, k]
+            if (delayed) {
+                const double* U = c.tmp2 + (size_t)b * x.nn;
+                const double* W = c.currU + (size_t)b * x.nn;
+                for (int q = 0; q < pending; ++q) {
+                    const double* u = U + (size_t)q * n;
+                    const double* w = W + (size_t)q * n;
+                    cj = fma(-u[k], w[j], cj);
+                    cJ = fma(-u[k], w[m + j], cJ);
+                    rj = fma(-u[j], w[k], rj);
+                    rJ = fma(-u[m + j], w[k], rJ);
+                }
+            }
+            double a1 = -cj, a2 = -cJ;
+            if (k == j) a1 += 1.0;
+            if (k == m + j) a2 += 1.0;
+            const double wr = x.s->sxd[2 * b], wi = x.s->sxd[2 * b + 1];
+            const double b1 = wr * rj - wi * rJ;
+            const double b2 = wi * rj + wr * rJ;
+            double* v = vec + (size_t)4 * b * n;
+            v[k] = a1;
+            v[n + k] = a2;
+            v[2 * n + k] = b1;
+            v[3 * n + k] = b2;
+            if (delayed) {
+                double* U = c.tmp2 + (size_t)b * x.nn + (size_t)pending * n;
+                double* W = c.currU + (size_t)b * x.nn + (size_t)pending * n;
+                U[k] = a1;
+                U[n + k] = a2;
+                W[k] = b1;
+                W[n + k] = b2;
+            }
+        }
+        __syncthreads();
+        if (warp == 0) {  // the mirrored diagonal, with the same fused operations as E
+            for (int e = lane; e < nf * m; e += 32) {
+                const int b = e / m, k = e % m;
+                const double* v = vec + (size_t)4 * b * n;
+                double re = diag[b * n + k], im = diag[b * n + m + k];
+                re = fma(-v[k], v[2 * n + k], re);
+                re = fma(-v[n + k], v[3 * n + k], re);
+                im = fma(-v[m + k], v[2 * n + k], im);
+                im = fma(-v[n + m + k], v[3 * n + k], im);
+                diag[b * n + k] = re;
+                diag[b * n + m + k] = im;
+            }
+            __syncwarp();
+        }
+        if (delayed) {
+            pending += 2;
+            if (pending == kcap) {
+                __syncthreads();
+                flush_delayed(x, pending);
+                pending = 0;
+            }
+            i = j + 1;
+            continue;
+        }
+        if (warp != 0) {
+            const int w = tid - 32, nw = DQMC_NT / 32 - 1;
+            for (int b = 0; b < nf; ++b) {
+                double* g = c.G + (size_t)b * x.nn;
+                const double* v = vec + (size_t)4 * b * n;
+                for (int k = w & 31; k < n; k += 32) {
+                    const double na1 = -v[k], na2 = -v[n + k];
+                    for (int l = w >> 5; l < n; l += nw) {
+                        double y = g[k + (size_t)l * n];
+                        y = fma(na1, v[2 * n + l], y);
+                        y = fma(na2, v[3 * n + l], y);
+                        g[k + (size_t)l * n] = y;
+                    }
+                }
+            }
+        }
+        i = j + 1;
+    }
+    return acc_count;
+}
+
 // sweep_spatial (local_updates.jl:23-60) with propose_local / accept_local!
 // (fields.jl:58-84, 176-209, 271-286, 340-344, 388-393, 440-449, 497-503,
 // 563-573, 627-637).  Thread 0 makes the sequential decisions with the
@@ -743,6 +978,7 @@ __device__ void flush_delayed(const Ctx& x, int p) {
 // and thread 0 goes on deciding from it: the next decisions overlap the update
 // and read bit-identical diagonal values.
 __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
+    if (x.c->cplx) return sweep_spatial_cplx(x);
     DqmcChain& c = *x.c;
     const int n = x.n, nf = x.nf;
     const int slice = c.current_slice;

@@ -48,6 +48,35 @@ __device__ __forceinline__ void dright(int n, double* __restrict__ C, const doub
     for (int e = threadIdx.x; e < n * n; e += DQMC_NT) C[e] = A[e] * d[e / n];
 }
 
+// Complex diagonal scalings on the real 2m x 2m representation
+// [[Re, -Im], [Im, Re]] of m x m complex matrices (n = 2m; complex.jl:190-223,
+// 257-277): d holds Re d_i at d[i] and Im d_i at d[m + i]; conj scales by the
+// conjugate diagonal (adjoint(eV), stack.jl:359-367).
+// C = Diagonal(d) * B: rows i and m + i mix.
+__device__ __forceinline__ void dleft_c(int n, double* __restrict__ C, const double* __restrict__ d,
+                                        const double* __restrict__ B, bool conj) {
+    const int m = n >> 1;
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
+        const int r = e % n, base = e - r;
+        const int i = r < m ? r : r - m;
+        const double dr = d[i], di = conj ? -d[m + i] : d[m + i];
+        const double b0 = B[base + i], b1 = B[base + m + i];
+        C[e] = r < m ? dr * b0 - di * b1 : di * b0 + dr * b1;
+    }
+}
+// C = A * Diagonal(d): columns i and m + i mix.
+__device__ __forceinline__ void dright_c(int n, double* __restrict__ C, const double* __restrict__ A,
+                                         const double* __restrict__ d, bool conj) {
+    const int m = n >> 1;
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
+        const int r = e % n, col = e / n;
+        const int i = col < m ? col : col - m;
+        const double dr = d[i], di = conj ? -d[m + i] : d[m + i];
+        const double a0 = A[r + (size_t)i * n], a1 = A[r + (size_t)(m + i) * n];
+        C[e] = col < m ? a0 * dr + a1 * di : a1 * dr - a0 * di;
+    }
+}
+
 // C = op(A) * op(B), op = transpose when TA / TB, on the FP64 FMA pipe (on
 // GB300 measured at 1.16 TFLOP/s for 64 x 64 blocks, above the DMMA tensor
 // path at 1.04).  64 x 64 output tiles,

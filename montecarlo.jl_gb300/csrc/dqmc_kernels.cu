@@ -156,6 +156,8 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
         g.prop_err_reported = s->c.prop_err_reported;
         g.n_prop_err = s->c.n_prop_err;
         g.n_neg_p = s->c.n_neg_p;
+        g.n_imag_p = s->c.n_imag_p;
+        g.max_imag_p = s->c.max_imag_p;
         g.accepted = s->c.accepted;
         g.proposals = s->c.proposals;
         for (int p = 0; p < 8; ++p) g.timers[p] = s->c.timers[p];

@@ -97,6 +97,9 @@ extern "C" int dqmc_calculate_greens_noalloc(const dqmc_chain_config* cfg,
     if (slice < 0 || slice > c.slices)
         return dqmc_report_error(DQMC_ERR_INVALID,
                                  "dqmc_calculate_greens_noalloc: slice out of range 0..M");
+    if (c.alpha_imag != 0.0)
+        return dqmc_report_error(DQMC_ERR_INVALID,
+                                 "dqmc_calculate_greens_noalloc: real chains only (alpha_imag != 0)");
     if (safe_mult <= 0) safe_mult = c.safe_mult;
     if (safe_mult <= 0)
         return dqmc_report_error(DQMC_ERR_INVALID, "dqmc_calculate_greens_noalloc: safe_mult <= 0");
@@ -135,6 +138,7 @@ extern "C" int dqmc_calculate_greens_noalloc(const dqmc_chain_config* cfg,
     DqmcChain d;
     memset(&d, 0, sizeof(d));
     d.n = c.n_sites; d.nf = c.n_flavors; d.M = c.slices; d.k = safe_mult; d.kind = c.field;
+    d.ns = c.n_sites;
     d.check_prop = 0;
     d.prec = DQMC_PREC_FP64;
     d.nr = 0;

@@ -61,9 +61,13 @@ class DQMC:
         self.precision = precision
         p = self.parameters
         self.n = len(model.l)
+        a = complex(self.field.alpha)
         self.config = _lib.ChainConfig(self.n, self.field.unique_flavors, p.slices, p.safe_mult,
                                        self.field.kind, int(p.check_propagation_error),
-                                       self.field.alpha, self.seed)
+                                       a.real, self.seed, a.imag)
+        if self.field.is_complex:
+            # complex Green's functions: measured on the host from the download
+            device_measurements = False
         prec = _lib.PREC_MIXED if precision == "mixed" else _lib.PREC_FP64
         self.handle = _lib.Handle([self.config], precision=prec, device=device)
         self.exps = hopping_exponentials(model.hopping_matrix(), p.delta_tau)
@@ -180,6 +184,8 @@ class DQMC:
             propagation_errors=st["propagation_errors"],
             max_propagation_error=st["max_propagation_error"],
             negative_probability=st["negative_probability"],
+            imaginary_probability=(st["imaginary_probability"],
+                                   st["max_imaginary_probability"]),
             runtime=time.time() - t0)
         self.field.conf[:] = self.handle.get_field(0)
         if min_acceptance is not None and self.analysis["acceptance"] < min_acceptance:

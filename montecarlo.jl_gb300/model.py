@@ -7,6 +7,7 @@ repulsive (MagneticHirschField) -- HubbardModel.jl:15-16, 83.
 """
 from __future__ import annotations
 
+import cmath
 import math
 import warnings
 from dataclasses import dataclass
@@ -143,17 +144,50 @@ class _Field:
         self.conf = np.zeros((self.n, self.slices), dtype=np.int8, order="F")
 
     @staticmethod
-    def _real(x: complex, what: str) -> float:
+    def _real(x: complex, what: str = ""):
+        """maybe_to_float (fields.jl:294): real when the imaginary part is
+        below 10 eps of the real part, else the complex value (the
+        reference's ComplexF64 field path)."""
         if isinstance(x, complex):
             if abs(x.imag) < 10 * np.spacing(abs(x.real)):
                 return x.real
-            raise NotImplementedError(
-                f"{what}: complex alpha (field / sign(U) mismatch) is the reference's complex path, "
-                "which this library does not implement")
+            return x
         return float(x)
+
+    @property
+    def is_complex(self) -> bool:
+        return isinstance(self.alpha, complex)
 
     def energy_boson(self, conf=None):
         return 0.0
+
+
+def _acosh_complex(z: complex) -> complex:
+    """acosh of a complex number with Kahan's formula (W. Kahan, "Branch cuts
+    for complex elementary functions", 1987), the one Julia's acosh(::Complex)
+    uses: the sign of a zero imaginary part selects the branch."""
+    zm1 = cmath.sqrt(complex(z.real - 1.0, z.imag))
+    zp1 = cmath.sqrt(complex(z.real + 1.0, z.imag))
+    xi = math.asinh((zm1.conjugate() * zp1).real)
+    eta = 2.0 * math.atan2(zm1.imag, zp1.real)
+    return complex(xi, eta)
+
+
+def _hirsch_alpha(c: float, U: float):
+    """acosh(exp(c * ComplexF64(U))) with the signed zero of c * (U + 0im)."""
+    x = math.exp(c * U)
+    if x >= 1.0:
+        return math.acosh(x)
+    z = cmath.exp(complex(c * U, c * 0.0))
+    return _Field._real(_acosh_complex(complex(z.real, math.copysign(0.0, c))))
+
+
+def _ghq_alpha(c: float, U: float):
+    """sqrt(c * ComplexF64(U)) with the signed zero of c * (U + 0im)."""
+    x = c * U
+    if x >= 0:
+        return math.sqrt(x)
+    return _Field._real(cmath.sqrt(complex(x, c * 0.0)))
 
 
 class DensityHirschField(_Field):
@@ -162,10 +196,7 @@ class DensityHirschField(_Field):
     kind = DENSITY_HIRSCH
 
     def _alpha(self, dt, U):
-        x = math.exp(0.5 * dt * U)
-        if x < 1.0:
-            return self._real(complex(0, math.acos(x)), "DensityHirschField")
-        return math.acosh(x)
+        return _hirsch_alpha(0.5 * dt, U)
 
     def energy_boson(self, conf=None):
         conf = self.conf if conf is None else conf
@@ -179,10 +210,7 @@ class MagneticHirschField(_Field):
     unique_flavors = 2
 
     def _alpha(self, dt, U):
-        x = math.exp(-0.5 * dt * U)
-        if x < 1.0:
-            return self._real(complex(0, math.acos(x)), "MagneticHirschField")
-        return math.acosh(x)
+        return _hirsch_alpha(-0.5 * dt, U)
 
 
 class DensityGHQField(_Field):
@@ -192,10 +220,7 @@ class DensityGHQField(_Field):
     ghq = True
 
     def _alpha(self, dt, U):
-        x = 0.5 * dt * U
-        if x < 0:
-            return self._real(complex(0, math.sqrt(-x)), "DensityGHQField")
-        return math.sqrt(x)
+        return _ghq_alpha(0.5 * dt, U)
 
 
 class MagneticGHQField(_Field):
@@ -206,10 +231,7 @@ class MagneticGHQField(_Field):
     ghq = True
 
     def _alpha(self, dt, U):
-        x = -0.5 * dt * U
-        if x < 0:
-            return self._real(complex(0, math.sqrt(-x)), "MagneticGHQField")
-        return math.sqrt(x)
+        return _ghq_alpha(-0.5 * dt, U)
 
 
 def hopping_exponentials(T: np.ndarray, delta_tau: float):

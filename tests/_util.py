@@ -21,8 +21,9 @@ def make_setup(pkg, L=4, lattice="square", U=4.0, mu=0.0, beta=2.0, delta_tau=0.
 
 
 def chain_config(lib, model, param, fld, seed, check_prop=1):
+    a = complex(fld.alpha)
     return lib.ChainConfig(len(model.l), fld.unique_flavors, param.slices, param.safe_mult,
-                           fld.kind, check_prop, fld.alpha, seed)
+                           fld.kind, check_prop, a.real, seed, a.imag)
 
 
 def oracle_chain(oracle, model, param, fld, exps, seed, check_prop=True):

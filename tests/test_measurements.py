@@ -86,8 +86,9 @@ def test_field_alpha_and_flavours(pkg):
     assert pkg.DensityGHQField(p, att).alpha == math.sqrt(0.2)
     assert pkg.MagneticGHQField(p, rep).alpha == math.sqrt(0.2)
     assert pkg.MagneticHirschField(p, rep).unique_flavors == 2
-    with pytest.raises(NotImplementedError):
-        pkg.DensityHirschField(p, rep)  # field/U mismatch: complex path
+    # field/U mismatch: the complex path, alpha = i acos(exp(-0.2))
+    assert pkg.DensityHirschField(p, rep).alpha == complex(0.0, 2 * math.atan2(
+        math.sqrt(1 - math.exp(-0.2)), math.sqrt(1 + math.exp(-0.2))))
 
 
 def test_config_recorder_roundtrip(pkg):
