@@ -66,3 +66,31 @@ def test_invalid_config_rejected(pkg):
     code = L.dqmc_create(0, C.byref(cfg), 1, 0, C.byref(h))
     assert code == 1
     assert b"n_flavors" in L.dqmc_last_error()
+
+
+def test_ctypes_structs_match_the_header(pkg, tmp_path):
+    """The ctypes mirrors of the ABI structs have the header's sizes and offsets."""
+    import shutil
+    import subprocess
+    from montecarlo_gb300 import _lib
+    if shutil.which("gcc") is None:  # pragma: no cover
+        pytest.skip("gcc unavailable")
+    structs = {"dqmc_chain_config": _lib.ChainConfig, "dqmc_stats": _lib.Stats,
+               "dqmc_measure_config": _lib.MeasureConfig, "dqmc_observables": _lib.Observables}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "dqmc_gb300.h"', "int main(void){"]
+    for cname, py in structs.items():
+        lines.append(f'printf("{cname} %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines.append("return 0;}")
+    src = tmp_path / "sizes.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "sizes"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)],
+                   check=True)
+    got = dict(l.split() for l in subprocess.run([str(exe)], check=True, capture_output=True,
+                                                  text=True).stdout.splitlines())
+    for cname, py in structs.items():
+        assert int(got[cname]) == C.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
