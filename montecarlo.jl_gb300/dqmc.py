@@ -136,6 +136,26 @@ class DQMC:
             phases = (np.cos(ph), np.sin(ph))
         return spin_susceptibility_z(by_l, phases, self.parameters.delta_tau)
 
+    def susceptibilities(self, q=None):
+        """The time-integrated susceptibilities of the current configuration
+        (charge, spin x / y / z at q, on-site s-wave pairing; the reference's
+        charge_density_susceptibility, spin_density_susceptibility and
+        pairing_susceptibility with TimeIntegral) from one device call for
+        the Green's functions G(0,0), G(l,l), G(0,l), G(l,0), l = 0..M."""
+        from .measurements import susceptibilities
+        M = self.parameters.slices
+        pairs = [(0, 0)]
+        for l in range(M + 1):
+            pairs += [(l, l), (0, l), (l, 0)]
+        Gs = self.handle.greens_kl(0, pairs, physical=True)
+        by_l = [(Gs[0], Gs[2 + 3 * l], Gs[3 + 3 * l], Gs[1 + 3 * l]) for l in range(M + 1)]
+        if q is None:
+            phases = self._q_phases
+        else:
+            ph = self.model.l.positions() @ np.asarray(q, dtype=float)
+            phases = (np.cos(ph), np.sin(ph))
+        return susceptibilities(by_l, phases, self.parameters.delta_tau)
+
     def calculate_greens(self, slice_, safe_mult=0):
         """calculate_greens(mc, slice) (stack.jl:525-583), effective G."""
         return self.handle.calculate_greens(0, slice_, safe_mult)

@@ -129,6 +129,68 @@ def time_displaced_sdc_z(G00, G0l, Gl0, Gll, at_zero):
     return np.outer(ml, m0) + exch
 
 
+CORRELATIONS = ("charge", "spin_x", "spin_y", "spin_z", "pairing")
+
+
+def time_displaced_correlations(G00, G0l, Gl0, Gll, at_zero):
+    """<A_i(l dtau) B_j(0)> for all site pairs, from G(0,0), G(0,l), G(l,0),
+    G(l,l), for the Wick-expanded kernels of the reference (BlockDiagonal
+    spin blocks, or one block repeated for both spins):
+
+    * "charge": full_cdc_kernel (charge_density.jl:65-112), n = n_up + n_dn;
+    * "spin_x", "spin_y": full_sdc_x/y_kernel (spin_density.jl:100-169);
+    * "spin_z": full_sdc_z_kernel (spin_density.jl:182-227);
+    * "pairing": pc_combined_kernel (pairing.jl:95-161) on site
+      (Delta_i = c_i,up c_i,dn): <Delta_i(tau) Delta_j^+(0)> + <Delta_i^+(tau) Delta_j(0)>.
+
+    ``at_zero``: l == 0 (the delta of the time-ordered contraction)."""
+    n = G00.shape[1]
+    idm = np.eye(n) if at_zero else np.zeros((n, n))
+    out = {}
+    if G00.shape[0] == 1:
+        g00, g0l, gl0, gll = G00[0], G0l[0], Gl0[0], Gll[0]
+        ex = (idm - g0l.T) * gl0
+        out["charge"] = 4.0 * np.outer(1.0 - np.diag(gll), 1.0 - np.diag(g00)) + 2.0 * ex
+        out["spin_x"] = out["spin_y"] = out["spin_z"] = 2.0 * ex
+        out["pairing"] = gl0 * gl0 + (idm - g0l.T) * (idm - g0l.T)
+        return out
+    occ_l = [1.0 - np.diag(Gll[b]) for b in range(2)]
+    occ_0 = [1.0 - np.diag(G00[b]) for b in range(2)]
+    ex = [(idm - G0l[b].T) * Gl0[b] for b in range(2)]
+    out["charge"] = sum(np.outer(occ_l[a], occ_0[b]) for a in range(2) for b in range(2)) + \
+        ex[0] + ex[1]
+    out["spin_x"] = out["spin_y"] = (idm - G0l[0].T) * Gl0[1] + (idm - G0l[1].T) * Gl0[0]
+    ml = occ_l[0] - occ_l[1]
+    m0 = occ_0[0] - occ_0[1]
+    out["spin_z"] = np.outer(ml, m0) + ex[0] + ex[1]
+    out["pairing"] = Gl0[0] * Gl0[1] + (idm - G0l[1].T) * (idm - G0l[0].T)
+    return out
+
+
+def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS):
+    """chi_K(q) = (1/n) sum_l w_l sum_ij e^{i q (r_i - r_j)} C_K(i, j; l dtau)
+    for the correlations K of ``time_displaced_correlations``, with the
+    TimeIntegral's trapezoid weights (generic.jl:337-366) and real phases
+    (cos(q.r_i), sin(q.r_i)); the pairing susceptibility is summed without
+    phases (the q = 0 on-site s-wave channel).  The reference's
+    charge_density_susceptibility, spin_density_susceptibility(:x/:y/:z)
+    and pairing_susceptibility with an on-site lattice iterator."""
+    c, s = phases
+    n = len(c)
+    ones = np.ones(n)
+    M = len(greens_by_l) - 1
+    chi = {k: 0.0 for k in kinds}
+    for l, (G00, G0l, Gl0, Gll) in enumerate(greens_by_l):
+        C = time_displaced_correlations(G00, G0l, Gl0, Gll, l == 0)
+        w = (0.5 if l in (0, M) else 1.0) * delta_tau
+        for k in kinds:
+            if k == "pairing":
+                chi[k] += w * float(np.real(ones @ C[k] @ ones))
+            else:
+                chi[k] += w * float(np.real(c @ C[k] @ c + s @ C[k] @ s))
+    return {k: v / n for k, v in chi.items()}
+
+
 def spin_susceptibility_z(greens_by_l, phases, delta_tau):
     """chi_z(q) = (1/n) sum_l w_l sum_ij e^{i q (r_i - r_j)} <m_z(i, l dtau) m_z(j, 0)>
     with the trapezoid weights of the reference's TimeIntegral

@@ -86,3 +86,50 @@ class HubbardED:
         with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
             f = np.where(np.abs(d) < 1e-12, self.beta, (1.0 - np.exp(-self.beta * d)) / d)
         return float(np.sum(self.rho_diag[:, None] * Mab ** 2 * f)) / self.n
+
+    # ---- time-displaced correlations of the susceptibility measurements ----
+    def operators(self, kind, phases):
+        """(A, B) with C(tau) = <A(tau) B(0)>: the q-summed charge or spin
+        density (phases_i weights) or the on-site pair field."""
+        n, c = self.n, self.c
+        if kind == "charge":
+            O = [self.nop[i][0] + self.nop[i][1] for i in range(n)]
+        elif kind == "spin_z":
+            O = [self.nop[i][0] - self.nop[i][1] for i in range(n)]
+        elif kind == "spin_x":
+            O = [c[2 * i].T @ c[2 * i + 1] + c[2 * i + 1].T @ c[2 * i] for i in range(n)]
+        elif kind == "spin_y":
+            O = [-1j * (c[2 * i].T @ c[2 * i + 1] - c[2 * i + 1].T @ c[2 * i]) for i in range(n)]
+        elif kind == "pairing":
+            D = sum(c[2 * i] @ c[2 * i + 1] for i in range(n))   # sum_i c_i,up c_i,dn
+            return D, D.conj().T
+        else:
+            raise ValueError(kind)
+        A = sum(phases[i] * O[i] for i in range(n))
+        return A, A.conj().T
+
+    def correlation(self, A, B, tau):
+        """<A(tau) B(0)> = sum_ab rho_a A_ab B_ba e^{tau (E_a - E_b)}."""
+        Aab = self.V.T @ A @ self.V
+        Bba = (self.V.T @ B @ self.V).T
+        E = self.E
+        return complex(np.sum(self.rho_diag[:, None] * Aab * Bba *
+                              np.exp(tau * (E[:, None] - E[None, :]))))
+
+    def susceptibility(self, kind, phases):
+        """(1/n) int_0^beta <A(tau) B(0)> dtau (pairing: plus the Delta^+ Delta
+        term), by the spectral sum with (e^{beta (E_a - E_b)} - 1) / (E_a - E_b)."""
+        E = self.E
+        d = E[None, :] - E[:, None]          # E_b - E_a
+        with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
+            f = np.where(np.abs(d) < 1e-12, self.beta, (1.0 - np.exp(-self.beta * d)) / d)
+        terms = [self.operators(kind, phases)]
+        if kind == "pairing":
+            A, B = terms[0]
+            terms.append((B, A))
+        tot = 0.0
+        for A, B in terms:
+            Aab = self.V.T @ A @ self.V
+            Bba = (self.V.T @ B @ self.V).T
+            tot += np.sum(self.rho_diag[:, None] * Aab * Bba * f)
+        return float(np.real(tot)) / self.n

@@ -82,3 +82,30 @@ def test_spin_susceptibility_matches_ed_2x2(pkg, lib, U):
         b.push(mc.spin_susceptibility())
     chi, err = float(b.mean()), float(b.std_error())
     assert abs(chi - chi_ed) <= 3.05 * DT ** 2 + 5 * err, (chi, chi_ed, err)
+
+
+@pytest.mark.parametrize("U,mu", [(-1.0, 0.0), (1.0, 0.2)])
+def test_all_susceptibilities_match_ed_2x2(pkg, lib, U, mu):
+    """Charge and spin x / y / z susceptibilities at (pi, pi) and the on-site
+    s-wave pairing susceptibility, all from the same time-displaced Green's
+    functions of each sweep, against exact diagonalisation (2x2, beta = 1,
+    dtau = 0.1; repulsive at half filling, attractive at mu = 0.2: no sign
+    problem; atol 3.05 dtau^2 plus five binning errors)."""
+    import ed
+    DT = 0.1
+    model = pkg.HubbardModel(pkg.SquareLattice(2), U=U, mu=mu)
+    E = ed.HubbardED(4, model.l.bonds(), 1.0, U, mu, 1.0)
+    pos = model.l.positions()
+    phases = np.cos(pos @ np.array([np.pi, np.pi]))
+    want = {k: E.susceptibility(k, phases) for k in pkg.CORRELATIONS}
+    mc = pkg.DQMC(model, beta=1.0, delta_tau=DT, safe_mult=10, seed=45, thermalization=200,
+                  sweeps=0, measure_rate=1)
+    pkg.run(mc)
+    bins = {k: pkg.LogBinner() for k in pkg.CORRELATIONS}
+    for _ in range(1200):
+        mc.handle.sweep(1)
+        for k, v in mc.susceptibilities().items():
+            bins[k].push(v)
+    for k in pkg.CORRELATIONS:
+        chi, err = float(bins[k].mean()), float(bins[k].std_error())
+        assert abs(chi - want[k]) <= 3.05 * DT ** 2 + 5 * err, (k, chi, want[k], err)

@@ -1,0 +1,44 @@
+"""The time-displaced correlation kernels of the susceptibility measurements
+(charge, spin x / y / z, on-site pairing: the reference's full_cdc_kernel,
+full_sdc_x/y/z_kernel, pc_combined_kernel) pinned exactly on the CPU.
+
+At U = 0 the slice matrices have no Trotter error and no field, so the
+oracle's unequal-time Green's functions G(k, l) are the free ones and every
+Wick contraction must equal exact diagonalisation's <A(l dtau) B(0)> to
+rounding, at every l."""
+import numpy as np
+import pytest
+
+from _util import make_setup, oracle_chain
+
+
+@pytest.mark.parametrize("field", ["DensityHirschField", "MagneticHirschField"])
+@pytest.mark.parametrize("mu", [0.0, 0.3])
+def test_time_displaced_correlations_exact_at_u0(pkg, oracle, field, mu):
+    import ed
+    from montecarlo_gb300.measurements import CORRELATIONS, time_displaced_correlations
+    model, param, fld, exps = make_setup(pkg, L=2, U=0.0, mu=mu, beta=1.0, safe_mult=5,
+                                         field=getattr(pkg, field))
+    o = oracle_chain(oracle, model, param, fld, exps, 3)
+    o.init_random_conf()
+    E = ed.HubbardED(4, model.l.bonds(), 1.0, 0.0, mu, param.beta)
+    pos = model.l.positions()
+    phases = np.cos(pos @ np.array([np.pi, np.pi]))
+    M = param.slices
+    pairs = [(0, 0)]
+    for l in range(M + 1):
+        pairs += [(l, l), (0, l), (l, 0)]
+    Gs = [o.greens_physical(g) for g in o.greens_kl(pairs)]
+    for l in range(M + 1):
+        C = time_displaced_correlations(Gs[0], Gs[2 + 3 * l], Gs[3 + 3 * l], Gs[1 + 3 * l], l == 0)
+        tau = l * param.delta_tau
+        for kind in CORRELATIONS:
+            A, B = E.operators(kind, phases)
+            if kind == "pairing":
+                want = E.correlation(A, B, tau) + E.correlation(B, A, tau)
+                got = C[kind].sum()
+            else:
+                want = E.correlation(A, B, tau)
+                got = phases @ C[kind] @ phases
+            assert abs(got - want) < 1e-10, (kind, l, got, want)
+
