@@ -138,3 +138,28 @@ def test_dqmc_run_with_complex_field(pkg):
     n_imag, max_imag = mc.analysis["imaginary_probability"]
     assert n_imag >= 0 and max_imag >= 0.0
     assert mc.analysis["max_propagation_error"] < 1e-6
+
+
+def test_complex_chain_in_a_pool_equals_plain_sweeps(pkg, lib):
+    """A complex chain admitted to a pool beside a real one, time-sliced with
+    graph replays, ends where a plain handle's sweeps end (bit-for-bit)."""
+    h, c, model, param, fld = _pair(pkg, lib, "DensityHirschField", L=4, seed=88)
+    h.initialize_run()
+    h.sweep(2)
+    cfg = chain_config(lib, model, param, fld, 88)
+    rmodel = pkg.HubbardModel(pkg.SquareLattice(4), U=-4.0)
+    rfld = pkg.MagneticHirschField(param, rmodel)
+    rcfg = chain_config(lib, rmodel, param, rfld, 89)
+    hop = pkg.hopping_exponentials(model.hopping_matrix(), param.delta_tau)
+    pool = lib.Pool(2, lib.chain_bytes(cfg) + lib.chain_bytes(rcfg) + 8192)
+    slots = [pool.admit(cfg), pool.admit(rcfg)]
+    for s in slots:
+        pool.set_hopping(s, hop)
+        pool.init_random_field(s)
+        pool.set_quota(s, 2)
+    while any(pool.slot(s)[1] > 0 for s in slots):
+        pool.run(300, True)
+    assert np.array_equal(pool.get_field(slots[0]), h.get_field(0))
+    assert np.array_equal(pool.greens(slots[0]), h.greens(0))
+    assert pool.get_rng(slots[0]) == h.get_rng(0)
+    pool.close()
