@@ -503,6 +503,48 @@ def main():
                                   "note": "checkerboard = true (FP64): exp(-dtau T) as products of "
                                           "site-disjoint bond factors; Trotter-split physics as in "
                                           "the reference's checkerboard path"}
+        # complex chains (the reference's ComplexF64 path): the same lattice,
+        # U and chains with the density-channel field, whose alpha is then
+        # imaginary; FP64 on the real 2n x 2n representation of G
+        cfld = pkg.DensityHirschField(param, model)
+        ca = complex(cfld.alpha)
+        hcx = _lib.Handle([_lib.ChainConfig(n, 1, M, param.safe_mult, cfld.kind, 1, ca.real,
+                                            seed0 + j, ca.imag) for j in range(B_chains)],
+                          precision=_lib.PREC_FP64)
+        hcx.set_hopping(-1, exps)
+        hcx.init_random_field(-1)
+        hcx.set_stream(stream.cuda_stream)
+        hcx.initialize_run()
+        for _ in range(args.warmup):
+            hcx.sweep_async(1)
+        hcx.synchronize()
+        cs0 = [hcx.stats(i) for i in range(B_chains)]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(args.steps):
+            hcx.sweep_async(1)
+        e1.record(stream)
+        hcx.synchronize()
+        torch.cuda.synchronize()
+        cx_t = e0.elapsed_time(e1) / 1e3
+        cs1 = [hcx.stats(i) for i in range(B_chains)]
+        hcx.close()
+        props = sum(b["proposals"] - a["proposals"] for a, b in zip(cs0, cs1))
+        cx_acc = sum(b["accepted"] - a["accepted"] for a, b in zip(cs0, cs1)) / max(1, props)
+        cx_tf = B_chains * args.steps * sweep_flops(2 * n, 1, M, nr, cx_acc) / cx_t / 1e12
+        extras["complex"] = {
+            "value": B_chains * args.steps / cx_t, "unit": "sweeps/s",
+            "vs_plain_fp64": B_chains * args.steps / cx_t / value,
+            "representation_tflops": cx_tf, "frac_of_measured_dgemm": cx_tf / fp64_peak,
+            "acceptance": cx_acc,
+            "imaginary_probability_fraction": sum(
+                b["imaginary_probability"] - a["imaginary_probability"]
+                for a, b in zip(cs0, cs1)) / max(1, props),
+            "max_propagation_error": max(s["max_propagation_error"] for s in cs1),
+            "note": "DensityHirschField at repulsive U (complex alpha, the reference's "
+                    "ComplexF64 path), same 8x8 lattice, chains and safe_mult; one flavour "
+                    "block of the real 2n x 2n representation (n = 128): 4x the plain "
+                    "chain's flops per sweep"}
         extras["batched"] = ensemble_c3(pkg, _lib, 256, args.extra_seconds)
         extras["served"] = served_c5(pkg, _lib, 48, 5 * args.extra_seconds)
 

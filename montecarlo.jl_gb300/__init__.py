@@ -16,7 +16,8 @@ from .model import (DENSITY_GHQ, DENSITY_HIRSCH, MAGNETIC_GHQ, MAGNETIC_HIRSCH, 
 from .measurements import (LogBinner, double_occupancy as double_occupancy_kernel,  # noqa: F401
                            interaction_energy, occupation_kernel, spin_density_correlation_z,
                            spin_susceptibility_z, structure_factor, time_displaced_sdc_z,
-                           susceptibilities, time_displaced_correlations, CORRELATIONS)
+                           susceptibilities, time_displaced_correlations, CORRELATIONS,
+                           current_operator, bilinear_correlation)
 from .dqmc import (DQMC, ExitCode, Measurement, double_occupancy, greens_measurement,  # noqa: F401
                    occupation, spin_density_correlation)
 

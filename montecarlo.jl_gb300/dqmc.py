@@ -136,13 +136,16 @@ class DQMC:
             phases = (np.cos(ph), np.sin(ph))
         return spin_susceptibility_z(by_l, phases, self.parameters.delta_tau)
 
-    def susceptibilities(self, q=None):
+    def susceptibilities(self, q=None, current_direction=None):
         """The time-integrated susceptibilities of the current configuration
-        (charge, spin x / y / z at q, on-site s-wave pairing; the reference's
-        charge_density_susceptibility, spin_density_susceptibility and
-        pairing_susceptibility with TimeIntegral) from one device call for
-        the Green's functions G(0,0), G(l,l), G(0,l), G(l,0), l = 0..M."""
-        from .measurements import susceptibilities
+        (charge, spin x / y / z at q, on-site s-wave pairing, and the uniform
+        current-current one along ``current_direction`` (default: the first
+        lattice vector); the reference's charge_density_susceptibility,
+        spin_density_susceptibility, pairing_susceptibility and
+        current_current_susceptibility with TimeIntegral) from one device
+        call for the Green's functions G(0,0), G(l,l), G(0,l), G(l,0),
+        l = 0..M."""
+        from .measurements import current_operator, susceptibilities
         M = self.parameters.slices
         pairs = [(0, 0)]
         for l in range(M + 1):
@@ -154,7 +157,8 @@ class DQMC:
         else:
             ph = self.model.l.positions() @ np.asarray(q, dtype=float)
             phases = (np.cos(ph), np.sin(ph))
-        return susceptibilities(by_l, phases, self.parameters.delta_tau)
+        J = current_operator(self.model.hopping_matrix(), self.model.l, current_direction)
+        return susceptibilities(by_l, phases, self.parameters.delta_tau, current=J)
 
     def calculate_greens(self, slice_, safe_mult=0):
         """calculate_greens(mc, slice) (stack.jl:525-583), effective G."""

@@ -167,19 +167,63 @@ def time_displaced_correlations(G00, G0l, Gl0, Gll, at_zero):
     return out
 
 
-def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS):
+def current_operator(T, lattice, direction=None):
+    """Single-particle matrix A of the paramagnetic current J = sum_sigma
+    sum_ab A_ab c^+_a c_b along ``direction`` (default: the first lattice
+    vector): the sum over directed bonds (s -> t) whose displacement points
+    along +direction of the reference's bond current
+    j(s, t) = i T[s, t] c^+_t c_s - i T[t, s] c^+_s c_t (cc_kernel,
+    current_current.jl:44-61) with T the hopping matrix."""
+    uc = lattice.unitcell
+    vecs = np.asarray(uc.lattice_vectors, dtype=float)
+    sites = np.asarray(uc.sites, dtype=float)
+    e = vecs[0] if direction is None else np.asarray(direction, dtype=float)
+    nbu = len(uc.bonds)
+    n = T.shape[0]
+    A = np.zeros((n, n), dtype=np.complex128)
+    for k, (s, t) in enumerate(lattice.bonds()):
+        b = uc.bonds[k % nbu]
+        disp = sites[b.to - 1] - sites[b.frm - 1] + np.asarray(b.uc_shift, dtype=float) @ vecs
+        if disp @ e > 1e-12:
+            A[t, s] += 1j * T[s, t]
+            A[s, t] += -1j * T[t, s]
+    return A
+
+
+def bilinear_correlation(A, B, G00, G0l, Gl0, Gll, at_zero):
+    """<O_A(l dtau) O_B(0)> for spin-summed bilinears O_A = sum_sigma sum_ab
+    A_ab c^+_a c_b (Wick's theorem with G(0,0), G(0,l), G(l,0), G(l,l); one
+    block counts for both spins): tr[A (I - Gll)] tr[B (I - G00)] +
+    tr[A Gl0 B (id - G0l)], summed over spin blocks."""
+    n = G00.shape[1]
+    eye = np.eye(n)
+    rep = 2.0 if G00.shape[0] == 1 else 1.0
+    nb = G00.shape[0]
+    t1 = rep * sum(np.trace(A @ (eye - Gll[b])) for b in range(nb))
+    t2 = rep * sum(np.trace(B @ (eye - G00[b])) for b in range(nb))
+    idm = eye if at_zero else 0.0 * eye
+    ex = rep * sum(np.trace(A @ Gl0[b] @ B @ (idm - G0l[b])) for b in range(nb))
+    return t1 * t2 + ex
+
+
+def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS, current=None):
     """chi_K(q) = (1/n) sum_l w_l sum_ij e^{i q (r_i - r_j)} C_K(i, j; l dtau)
     for the correlations K of ``time_displaced_correlations``, with the
     TimeIntegral's trapezoid weights (generic.jl:337-366) and real phases
     (cos(q.r_i), sin(q.r_i)); the pairing susceptibility is summed without
     phases (the q = 0 on-site s-wave channel).  The reference's
     charge_density_susceptibility, spin_density_susceptibility(:x/:y/:z)
-    and pairing_susceptibility with an on-site lattice iterator."""
+    and pairing_susceptibility with an on-site lattice iterator.  With
+    ``current`` (a ``current_operator`` matrix) also "current": the uniform
+    current-current susceptibility (1/n) int <J(tau) J(0)> dtau, the q = 0
+    sum of the reference's current_current_susceptibility."""
     c, s = phases
     n = len(c)
     ones = np.ones(n)
     M = len(greens_by_l) - 1
     chi = {k: 0.0 for k in kinds}
+    if current is not None:
+        chi["current"] = 0.0
     for l, (G00, G0l, Gl0, Gll) in enumerate(greens_by_l):
         C = time_displaced_correlations(G00, G0l, Gl0, Gll, l == 0)
         w = (0.5 if l in (0, M) else 1.0) * delta_tau
@@ -188,6 +232,9 @@ def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS):
                 chi[k] += w * float(np.real(ones @ C[k] @ ones))
             else:
                 chi[k] += w * float(np.real(c @ C[k] @ c + s @ C[k] @ s))
+        if current is not None:
+            chi["current"] += w * float(np.real(
+                bilinear_correlation(current, current, G00, G0l, Gl0, Gll, l == 0)))
     return {k: v / n for k, v in chi.items()}
 
 

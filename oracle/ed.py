@@ -100,6 +100,10 @@ class HubbardED:
             O = [c[2 * i].T @ c[2 * i + 1] + c[2 * i + 1].T @ c[2 * i] for i in range(n)]
         elif kind == "spin_y":
             O = [-1j * (c[2 * i].T @ c[2 * i + 1] - c[2 * i + 1].T @ c[2 * i]) for i in range(n)]
+        elif kind == "bilinear":   # phases is then the single-particle matrix A
+            A = sum(phases[a, b] * c[2 * a + sg].T @ c[2 * b + sg]
+                    for a in range(n) for b in range(n) for sg in range(2) if phases[a, b] != 0)
+            return A, A.conj().T
         elif kind == "pairing":
             D = sum(c[2 * i] @ c[2 * i + 1] for i in range(n))   # sum_i c_i,up c_i,dn
             return D, D.conj().T
@@ -123,7 +127,7 @@ class HubbardED:
         d = E[None, :] - E[:, None]          # E_b - E_a
         with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
             f = np.where(np.abs(d) < 1e-12, self.beta, (1.0 - np.exp(-self.beta * d)) / d)
-        terms = [self.operators(kind, phases)]
+        terms = [self.operators("bilinear" if kind == "current" else kind, phases)]
         if kind == "pairing":
             A, B = terms[0]
             terms.append((B, A))

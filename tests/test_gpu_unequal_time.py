@@ -109,3 +109,29 @@ def test_all_susceptibilities_match_ed_2x2(pkg, lib, U, mu):
     for k in pkg.CORRELATIONS:
         chi, err = float(bins[k].mean()), float(bins[k].std_error())
         assert abs(chi - want[k]) <= 3.05 * DT ** 2 + 5 * err, (k, chi, want[k], err)
+
+
+@pytest.mark.parametrize("U,mu", [(-2.0, 0.0), (2.0, 0.3)])
+def test_current_susceptibility_matches_ed_chain4(pkg, lib, U, mu):
+    """Uniform current-current susceptibility (bond currents of cc_kernel)
+    and the others on a 4-site chain against exact diagonalisation
+    (beta = 1, dtau = 0.1; atol 3.05 dtau^2 plus five binning errors)."""
+    import ed
+    DT = 0.1
+    model = pkg.HubbardModel(pkg.Chain(4), U=U, mu=mu)
+    E = ed.HubbardED(4, model.l.bonds(), 1.0, U, mu, 1.0)
+    J = pkg.current_operator(model.hopping_matrix(), model.l)
+    phases = np.cos(np.pi * model.l.positions()[:, 0])
+    want = {k: E.susceptibility(k, phases) for k in pkg.CORRELATIONS}
+    want["current"] = E.susceptibility("current", J)
+    mc = pkg.DQMC(model, beta=1.0, delta_tau=DT, safe_mult=10, seed=46, thermalization=200,
+                  sweeps=0, measure_rate=1, structure_factor_q=[np.pi])
+    pkg.run(mc)
+    bins = {k: pkg.LogBinner() for k in want}
+    for _ in range(1200):
+        mc.handle.sweep(1)
+        for k, v in mc.susceptibilities().items():
+            bins[k].push(v)
+    for k in want:
+        chi, err = float(bins[k].mean()), float(bins[k].std_error())
+        assert abs(chi - want[k]) <= 3.05 * DT ** 2 + 5 * err, (k, chi, want[k], err)

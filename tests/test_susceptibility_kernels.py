@@ -42,3 +42,40 @@ def test_time_displaced_correlations_exact_at_u0(pkg, oracle, field, mu):
                 got = phases @ C[kind] @ phases
             assert abs(got - want) < 1e-10, (kind, l, got, want)
 
+
+
+@pytest.mark.parametrize("field", ["DensityHirschField", "MagneticHirschField"])
+def test_current_and_bilinear_correlations_exact_at_u0(pkg, oracle, field):
+    """The uniform current J_x (bond currents of cc_kernel) and a generic
+    bilinear through bilinear_correlation equal ED at every tau (4-site
+    chain, U = 0), and the bilinear form reproduces the charge kernel."""
+    import ed
+    from montecarlo_gb300.measurements import (bilinear_correlation, current_operator,
+                                               time_displaced_correlations)
+    model, param, fld, exps = make_setup(pkg, L=4, lattice="chain", U=0.0, mu=0.3, beta=1.0,
+                                         safe_mult=5, field=getattr(pkg, field))
+    o = oracle_chain(oracle, model, param, fld, exps, 3)
+    o.init_random_conf()
+    E = ed.HubbardED(4, model.l.bonds(), 1.0, 0.0, 0.3, param.beta)
+    J = current_operator(model.hopping_matrix(), model.l)
+    assert np.abs(J).max() > 0.5 and np.allclose(J, J.conj().T)
+    Jop = E.operators("bilinear", J)
+    rng = np.random.default_rng(1)
+    Bm = rng.standard_normal((4, 4))
+    Bop = E.operators("bilinear", Bm)
+    ph = np.cos(np.pi * model.l.positions()[:, 0])
+    M = param.slices
+    pairs = [(0, 0)]
+    for l in range(M + 1):
+        pairs += [(l, l), (0, l), (l, 0)]
+    Gs = [o.greens_physical(g) for g in o.greens_kl(pairs)]
+    for l in range(M + 1):
+        q = (Gs[0], Gs[2 + 3 * l], Gs[3 + 3 * l], Gs[1 + 3 * l])
+        tau = l * param.delta_tau
+        got = bilinear_correlation(J, J, *q, l == 0)
+        assert abs(got - E.correlation(*Jop, tau)) < 1e-10, (l, got)
+        got = bilinear_correlation(Bm, Bm.T, *q, l == 0)
+        assert abs(got - E.correlation(Bop[0], Bop[1], tau)) < 1e-10, l
+        C = time_displaced_correlations(*q, l == 0)["charge"]
+        D = np.diag(ph)
+        assert abs(ph @ C @ ph - bilinear_correlation(D, D, *q, l == 0)) < 1e-12
