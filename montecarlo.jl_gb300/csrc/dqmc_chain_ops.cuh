@@ -342,6 +342,26 @@ __device__ __noinline__ void wrap_greens_df(const Ctx& x, int curr_slice, int di
 }
 
 // wrap_greens! (stack.jl:594-603)
+// A complex chain's G projected back onto the representation subspace
+// [[X, -Y], [Y, X]] (each pair of copies replaced by its mean).  Rounding in
+// the wraps and rank-2 updates leaves a component outside the subspace,
+// which the next wraps carry along; the projection removes it.
+__device__ void rep_project(const Ctx& x, double* gf) {
+    const int n = x.n, m = n >> 1;
+    for (int e = threadIdx.x; e < x.nf * m * m; e += DQMC_NT) {
+        const int b = e / (m * m), r = e % m, col = (e / m) % m;
+        double* g = gf + (size_t)b * x.nn;
+        const size_t tl = (size_t)col * n + r, br = (size_t)(m + col) * n + m + r;
+        const size_t bl = (size_t)col * n + m + r, tr = (size_t)(m + col) * n + r;
+        const double xa = 0.5 * (g[tl] + g[br]), ya = 0.5 * (g[bl] - g[tr]);
+        g[tl] = xa;
+        g[br] = xa;
+        g[bl] = ya;
+        g[tr] = -ya;
+    }
+    __syncthreads();
+}
+
 __device__ void wrap_greens(const Ctx& x, double* gf, int curr_slice, int direction) {
     if (df_resident(x) && gf == x.c->G) {
         wrap_greens_df(x, curr_slice, direction);
@@ -354,6 +374,7 @@ __device__ void wrap_greens(const Ctx& x, double* gf, int curr_slice, int direct
         slice_left(x, curr_slice, gf, true);
         slice_inv_right(x, curr_slice, gf, true);
     }
+    if (x.c->cplx) rep_project(x, gf);
 }
 
 __device__ __forceinline__ double* ustk(const Ctx& x, int idx) {
