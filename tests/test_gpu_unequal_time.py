@@ -104,8 +104,9 @@ def test_all_susceptibilities_match_ed_2x2(pkg, lib, U, mu):
     bins = {k: pkg.LogBinner() for k in pkg.CORRELATIONS}
     for _ in range(1200):
         mc.handle.sweep(1)
-        for k, v in mc.susceptibilities().items():
-            bins[k].push(v)
+        chi = mc.susceptibilities()
+        for k in pkg.CORRELATIONS:
+            bins[k].push(chi[k])
     for k in pkg.CORRELATIONS:
         chi, err = float(bins[k].mean()), float(bins[k].std_error())
         assert abs(chi - want[k]) <= 3.05 * DT ** 2 + 5 * err, (k, chi, want[k], err)
