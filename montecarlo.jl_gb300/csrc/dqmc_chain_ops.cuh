@@ -498,9 +498,11 @@ __device__ __noinline__ void calculate_greens_pair(const Ctx& x, double* Gout, b
 // calculate_greens_AVX! (stack.jl:442-496), per flavour block.  finish =
 // false stops after the second UDT: calculate_inv_greens_udt
 // (global_updates.jl:26-49), leaving det(G) = 1 / prod(Dr) up to phases.
+// A complex chain's result is projected onto the representation subspace.
 __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout, bool finish = true) {
     if (paired(x)) {
         calculate_greens_pair(x, Gout, finish);
+        if (finish && x.c->cplx) rep_project(x, Gout);
         return;
     }
     DqmcChain& c = *x.c;
@@ -537,6 +539,7 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout, bool f
         mm<false, true>(n, g, ul, tr, x.s->tiles);
         __syncthreads();
     }
+    if (finish && x.c->cplx) rep_project(x, Gout);
 }
 
 __device__ void set_ones(const Ctx& x, double* d) {
@@ -784,9 +787,10 @@ __device__ void flush_delayed(const Ctx& x, int p) {
 // calculate_detratio! methods, fields.jl:63-66 and 128-140, vldiv22!,
 // fields.jl:215-227, and update_greens!, fields.jl:271-286) on the real
 // representation E of G (n = 2 ns).  An accepted move at site j updates
-// G -= (I - G)[:, j] (Delta/R) G[j, :]; on E that is the rank-2 update
-// E -= a1 b1^T + a2 b2^T with a1 = e_j - E[:, j], a2 = e_(ns+j) - E[:, ns+j],
-// b1 = wr E[j, :] - wi E[ns+j, :], b2 = wi E[j, :] + wr E[ns+j, :], w = Delta/R.
+// G -= u v^T with u = (I - G)[:, j], v = (Delta/R) G[j, :]; on E that is the
+// rank-2 update E -= a1 b1^T + a2 b2^T with a1 = [Re u; Im u],
+// a2 = [-Im u; Re u], b1 = [Re v, -Im v], b2 = [Im v, Re v], all formed from
+// the left half [X; Y] of E.
 // Thread 0 decides in the reference's complex operation order from a
 // shared-memory mirror of G_jj = (E[j, j], E[ns+j, j]); the update vectors are
 // formed from E (plus the pending updates when E is in global memory) and
@@ -904,43 +908,53 @@ __device__ __noinline__ long long sweep_spatial_cplx(const Ctx& x) {
             break;
         }
         acc_count += 1;
-        for (int e = tid; e < nf * n; e += DQMC_NT) {
-            const int b = e / n, k = e % n;
+        // every vector from the left half [X; Y] of E only (column j and
+        // rows j, m + j of its first m columns): the increment is then the
+        // representation of the complex update even where rounding has left
+        // E slightly off the subspace, so no such component is amplified
+        for (int e = tid; e < nf * m; e += DQMC_NT) {
+            const int b = e / m, k = e % m;
             const double* g = c.G + (size_t)b * x.nn;
-            double cj = g[(size_t)j * n + k];        // E[k, j]
-            double cJ = g[(size_t)(m + j) * n + k];  // E[k, m + j]
-            double rj = g[(size_t)k * n + j];        // E[j, k]
-            double rJ = g[(size_t)k * n + m + j];    // E[m + j, k]
+            double xc = g[(size_t)j * n + k];      // X[k, j] = E[k, j]
+            double yc = g[(size_t)j * n + m + k];  // Y[k, j] = E[m + k, j]
+            double xr = g[(size_t)k * n + j];      // X[j, k] = E[j, k]
+            double yr = g[(size_t)k * n + m + j];  // Y[j, k] = E[m + j, k]
             if (delayed) {
                 const double* U = c.tmp2 + (size_t)b * x.nn;
                 const double* W = c.currU + (size_t)b * x.nn;
                 for (int q = 0; q < pending; ++q) {
                     const double* u = U + (size_t)q * n;
                     const double* w = W + (size_t)q * n;
-                    cj = fma(-u[k], w[j], cj);
-                    cJ = fma(-u[k], w[m + j], cJ);
-                    rj = fma(-u[j], w[k], rj);
-                    rJ = fma(-u[m + j], w[k], rJ);
+                    xc = fma(-u[k], w[j], xc);
+                    yc = fma(-u[m + k], w[j], yc);
+                    xr = fma(-u[j], w[k], xr);
+                    yr = fma(-u[m + j], w[k], yr);
                 }
             }
-            double a1 = -cj, a2 = -cJ;
-            if (k == j) a1 += 1.0;
-            if (k == m + j) a2 += 1.0;
+            // u = e_j - G[:, j]; v = w G[j, :]
+            const double ur = (k == j ? 1.0 : 0.0) - xc, ui = -yc;
             const double wr = x.s->sxd[2 * b], wi = x.s->sxd[2 * b + 1];
-            const double b1 = wr * rj - wi * rJ;
-            const double b2 = wi * rj + wr * rJ;
+            const double vr = wr * xr - wi * yr, vi = wr * yr + wi * xr;
             double* v = vec + (size_t)4 * b * n;
-            v[k] = a1;
-            v[n + k] = a2;
-            v[2 * n + k] = b1;
-            v[3 * n + k] = b2;
+            v[k] = ur;           // a1 = [ur; ui]
+            v[m + k] = ui;
+            v[n + k] = -ui;      // a2 = [-ui; ur]
+            v[n + m + k] = ur;
+            v[2 * n + k] = vr;   // b1 = [vr, -vi]
+            v[2 * n + m + k] = -vi;
+            v[3 * n + k] = vi;   // b2 = [vi, vr]
+            v[3 * n + m + k] = vr;
             if (delayed) {
                 double* U = c.tmp2 + (size_t)b * x.nn + (size_t)pending * n;
                 double* W = c.currU + (size_t)b * x.nn + (size_t)pending * n;
-                U[k] = a1;
-                U[n + k] = a2;
-                W[k] = b1;
-                W[n + k] = b2;
+                U[k] = ur;
+                U[m + k] = ui;
+                U[n + k] = -ui;
+                U[n + m + k] = ur;
+                W[k] = vr;
+                W[m + k] = -vi;
+                W[n + k] = vi;
+                W[n + m + k] = vr;
             }
         }
         __syncthreads();
