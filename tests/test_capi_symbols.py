@@ -66,6 +66,23 @@ def test_invalid_config_rejected(pkg):
     code = L.dqmc_create(0, C.byref(cfg), 1, 0, C.byref(h))
     assert code == 1
     assert b"n_flavors" in L.dqmc_last_error()
+    # size limits and non-finite constants (checked before any device call)
+    for bad, what in (((513, 2, 10, 5, 1, 1, 0.5, 1, 0.0), b"n_sites"),
+                      ((0, 1, 10, 5, 0, 1, 0.5, 1, 0.0), b"n_sites"),
+                      ((16, 1, 0, 5, 0, 1, 0.5, 1, 0.0), b"slices"),
+                      ((16, 1, 10, 0, 0, 1, 0.5, 1, 0.0), b"safe_mult"),
+                      ((16, 1, 10, 5, 4, 1, 0.5, 1, 0.0), b"field"),
+                      ((16, 1, 3000, 5, 0, 1, 0.5, 1, 0.0), b"chunks"),
+                      ((129, 1, 10, 5, 0, 1, 0.0, 1, 0.6), b"complex"),
+                      ((16, 1, 10, 5, 0, 1, float("nan"), 1, 0.0), b"alpha"),
+                      ((16, 1, 10, 5, 0, 1, 0.5, 1, float("inf")), b"alpha")):
+        cfg = _lib.ChainConfig(*bad)
+        assert L.dqmc_create(0, C.byref(cfg), 1, 0, C.byref(h)) == 1, bad
+        assert what in L.dqmc_last_error(), (bad, L.dqmc_last_error())
+    # a complex chain at the largest size is valid, but not in mixed precision
+    cfg = _lib.ChainConfig(128, 1, 10, 5, 0, 1, 0.0, 1, 0.6)
+    assert L.dqmc_create(0, C.byref(cfg), 1, 1, C.byref(h)) == 1
+    assert b"FP64" in L.dqmc_last_error()
 
 
 def test_ctypes_structs_match_the_header(pkg, tmp_path):

@@ -189,3 +189,21 @@ def test_complex_propagation_error_at_oracle_level_8x8(pkg, lib):
     assert st[0]["max_propagation_error"] <= 10 * c.prop_err_max + 1e-13
     assert max(s["max_propagation_error"] for s in st) < 1e-9
     assert all(s["imaginary_probability"] == 0 for s in st)   # real weights at half filling
+
+
+def test_complex_max_size_128_sites(pkg, lib):
+    """The largest complex chain (n_sites = 128, the honeycomb L = 8;
+    representation 256, G in global memory): G from scratch and one sweep
+    replayed against the complex oracle."""
+    h, c, model, param, fld = _pair(pkg, lib, "DensityHirschField", L=8, lattice="honeycomb",
+                                    beta=0.5, k=5, seed=13)
+    assert len(model.l) == 128
+    for sl in (0, 3, param.slices):
+        assert _rel(h.calculate_greens(0, sl), c.calculate_greens_at(sl)) < TOL_G, sl
+    h.initialize_run()
+    c.initialize_run()
+    st = h.sweep(1)[0]
+    c.sweeps(1)
+    assert np.array_equal(h.get_field(0), c.conf)
+    assert st["accepted"] == c.accepted
+    assert _rel(h.greens(0), c.G) < 1e-9

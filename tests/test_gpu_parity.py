@@ -203,3 +203,24 @@ def test_max_size_16x16_two_flavours(pkg, lib, oracle):
     assert np.array_equal(h.get_field(0), oc.get_conf())
     assert h.get_rng(0)[1] == oc.rng_counter()
     assert maxdiff(h.greens(0), oc.greens()) < TOL_G
+
+
+def test_max_size_honeycomb_512_sites(pkg, lib, oracle):
+    """The largest chain the library takes (n_sites = 512: the honeycomb
+    L = 16 of the served stream), two flavours, short beta: G from scratch
+    and one sweep replayed bit-exactly against the oracle."""
+    h, oc, model, param, fld = _pair(pkg, lib, oracle, "MagneticHirschField", L=16,
+                                     lattice="honeycomb", beta=0.5, safe_mult=5, seed=12)
+    assert len(model.l) == 512
+    h.init_random_field(0)
+    oc.init_random_conf()
+    for sl in (0, 3, param.slices):
+        g = h.calculate_greens(0, sl)
+        assert maxdiff(g, oc.calculate_greens_at(sl)) < TOL_G, sl
+    h.initialize_run()
+    oc.initialize_run()
+    h.sweep(1)
+    oc.sweeps(1)
+    assert np.array_equal(h.get_field(0), oc.get_conf())
+    assert h.get_rng(0)[1] == oc.rng_counter()
+    assert maxdiff(h.greens(0), oc.greens()) < TOL_G
