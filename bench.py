@@ -473,7 +473,8 @@ def main():
                            "max_propagation_error": mp, "safe_mult": k_mixed,
                            "strict_propagation_error_1e-6": strict,
                            "note": "wraps and slice chains as double-float products on the FP32 "
-                                   "pipe; UDT, reconstruction, ratios, rank-1 updates FP64"}
+                                   "pipe, and so are the reconstruction's products; UDT, "
+                                   "triangular solves, ratios, rank-1 updates FP64"}
         # the reference's checkerboard = true on the same ensemble: the
         # hopping exponentials as bond-factor products (O(n^2) per factor)
         from montecarlo_gb300 import model as _M

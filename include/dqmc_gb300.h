@@ -61,9 +61,10 @@ extern "C" {
 
 /* arithmetic of the wraps and slice-matrix chains */
 #define DQMC_PREC_FP64 0  /* everything FP64 (parity path) */
-#define DQMC_PREC_MIXED 1 /* wraps and slice-matrix chains as double-float products
-                             on the FP32 pipe; UDT, reconstruction, determinant
-                             ratios and rank-1 updates in FP64 */
+#define DQMC_PREC_MIXED 1 /* wraps, slice-matrix chains and the products of the Green's
+                             reconstruction as double-float products on the FP32 pipe;
+                             UDT factorisations, triangular solves, determinant ratios
+                             and rank-1 updates in FP64 */
 
 typedef struct dqmc_handle dqmc_handle;
 

@@ -116,9 +116,10 @@ __device__ __forceinline__ void phase_stop(const Ctx& x, int phase, long long t0
 }
 
 // Slice-matrix products (wraps and slice chains): FP64, or on a
-// mixed-precision chain the double-float product on the FP32 pipe.  The UDT,
-// the Green's reconstruction, the T updates, the determinant ratios and the
-// rank-1 updates stay FP64 on every chain.
+// mixed-precision chain the double-float product on the FP32 pipe (so are
+// the products of the Green's reconstruction, rmm below).  The UDT
+// factorisations, the triangular solves, the T updates, the determinant ratios
+// and the rank-1 updates stay FP64 on every chain.
 // Every transposed left operand (TA) of these products is a hopping
 // exponential, which is symmetric, so the double-float product reads it
 // untransposed (identical sums; the untransposed staging needs fewer
@@ -462,21 +463,32 @@ __device__ __noinline__ void add_slice_sequence_right(const Ctx& x, int idx) {
 // independent; each sees exactly the per-block sequence below), so that the
 // two QR factorisations and the two triangular solves of each step run
 // together.
+// Products of the Green's reconstruction: FP64, or on a mixed-precision
+// chain with n >= 48 the double-float product on the FP32 pipe (FP64
+// operands split while staged; ~1e-14 relative per product).  The UDT
+// factorisations and triangular solves between them stay FP64.
+template <bool TA, bool TB>
+__device__ __forceinline__ void rmm(const Ctx& x, double* C, const double* A, const double* B) {
+    if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48 && !x.c->cplx)
+        mm_dfx<false, false, false, TA, TB>(x.n, C, A, B, x.s->tiles);
+    else
+        mm<TA, TB>(x.n, C, A, B, x.s->tiles);
+}
+
 __device__ __noinline__ void calculate_greens_pair(const Ctx& x, double* Gout, bool finish) {
     DqmcChain& c = *x.c;
     const int n = x.n;
-    double* sm = x.s->tiles;
-    for (int b = 0; b < 2; ++b) mm<false, true>(n, blk(Gout, x, b), blk(c.Tl, x, b), blk(c.Tr, x, b), sm);
+    for (int b = 0; b < 2; ++b) rmm<false, true>(x, blk(Gout, x, b), blk(c.Tl, x, b), blk(c.Tr, x, b));
     __syncthreads();
     for (int b = 0; b < 2; ++b) dright(n, blk(c.Tr, x, b), blk(Gout, x, b), c.Dr + b * n);
     __syncthreads();
     for (int b = 0; b < 2; ++b) dleft(n, blk(Gout, x, b), c.Dl + b * n, blk(c.Tr, x, b));
     __syncthreads();
     udt_pair(x, c.Tr, c.Dr, Gout, false);
-    for (int b = 0; b < 2; ++b) mm<false, false>(n, blk(c.Tl, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b), sm);
+    for (int b = 0; b < 2; ++b) rmm<false, false>(x, blk(c.Tl, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b));
     __syncthreads();
     rdivp_pair(x, c.Ur, Gout, c.Ul);
-    for (int b = 0; b < 2; ++b) mm<true, false>(n, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ur, x, b), sm);
+    for (int b = 0; b < 2; ++b) rmm<true, false>(x, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ur, x, b));
     __syncthreads();
     for (int e = threadIdx.x; e < 2 * n; e += DQMC_NT) {
         const int b = e / n, i = e % n;
@@ -486,12 +498,12 @@ __device__ __noinline__ void calculate_greens_pair(const Ctx& x, double* Gout, b
     udt_pair(x, c.Ul, c.Dr, c.Tr, false);
     if (!finish) return;
     rdivp_pair(x, c.Ur, c.Tr, Gout);
-    for (int b = 0; b < 2; ++b) mm<false, false>(n, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ul, x, b), sm);
+    for (int b = 0; b < 2; ++b) rmm<false, false>(x, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ul, x, b));
     for (int e = threadIdx.x; e < 2 * n; e += DQMC_NT) c.Dl[e] = 1.0 / c.Dr[e];
     __syncthreads();
     for (int b = 0; b < 2; ++b) dright(n, blk(c.Ul, x, b), blk(c.Ur, x, b), c.Dl + b * n);
     __syncthreads();
-    for (int b = 0; b < 2; ++b) mm<false, true>(n, blk(Gout, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b), sm);
+    for (int b = 0; b < 2; ++b) rmm<false, true>(x, blk(Gout, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b));
     __syncthreads();
 }
 
@@ -514,29 +526,29 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout, bool f
         double *dl = c.Dl + b * n, *dr = c.Dr + b * n;
         int* pv = c.pivot + b * n;
         double* tv = c.tempv + b * n;
-        mm<false, true>(n, g, tl, tr, x.s->tiles);
+        rmm<false, true>(x, g, tl, tr);
         __syncthreads();
         dright(n, tr, g, dr);
         __syncthreads();
         dleft(n, g, dl, tr);
         __syncthreads();
         udt_one(x, tr, dr, g, b, false);
-        mm<false, false>(n, tl, ul, tr, x.s->tiles);
+        rmm<false, false>(x, tl, ul, tr);
         __syncthreads();
         rdivp(n, ur, g, ul, pv, bf, x.s->sv);
-        mm<true, false>(n, tr, tl, ur, x.s->tiles);
+        rmm<true, false>(x, tr, tl, ur);
         __syncthreads();
         for (int i = threadIdx.x; i < n; i += DQMC_NT) tr[(size_t)i * n + i] += dr[i];
         __syncthreads();
         udt_one(x, ul, dr, tr, b, false);
         if (!finish) continue;
         rdivp(n, ur, tr, g, pv, bf, x.s->sv);
-        mm<false, false>(n, tr, tl, ul, x.s->tiles);
+        rmm<false, false>(x, tr, tl, ul);
         for (int i = threadIdx.x; i < n; i += DQMC_NT) dl[i] = 1.0 / dr[i];
         __syncthreads();
         dright(n, ul, ur, dl);
         __syncthreads();
-        mm<false, true>(n, g, ul, tr, x.s->tiles);
+        rmm<false, true>(x, g, ul, tr);
         __syncthreads();
     }
     if (finish && x.c->cplx) rep_project(x, Gout);

@@ -218,9 +218,11 @@ __device__ __forceinline__ void dright_df(int n, float2* __restrict__ C, const f
 // tiles, 4 x 4 per thread, k staged 16 at a time (sm: 4 * 16 * 64 floats).
 // C must not alias A or B.  The split hopping exponentials and the
 // shared-memory G of the mixed path enter without any FP64 instruction.
-template <bool ADF, bool BDF, bool CDF>
+// TA / TB: the FP64 operand is read transposed (not for split operands).
+template <bool ADF, bool BDF, bool CDF, bool TA = false, bool TB = false>
 __device__ __noinline__ void mm_dfx(int n, void* __restrict__ Cv, const void* __restrict__ Av,
                                     const void* __restrict__ Bv, double* smd) {
+    static_assert(!(ADF && TA) && !(BDF && TB), "split operands are read untransposed");
     float* sAh = reinterpret_cast<float*>(smd);  // [16][64]: sAh[kk*64 + m]
     float* sAl = sAh + 16 * 64;
     float* sBh = sAl + 16 * 64;                   // [16][64]: sBh[kk*64 + j]
@@ -237,11 +239,11 @@ __device__ __noinline__ void mm_dfx(int n, void* __restrict__ Cv, const void* __
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const int e = tid + t * DQMC_NT;
-                    const int mm_ = e & 63, kk = e >> 6;
+                    const int mm_ = TA ? e >> 4 : e & 63, kk = TA ? e & 15 : e >> 6;
                     const int gm = m0 + mm_, gk = k0 + kk;
                     float2 v = make_float2(0.f, 0.f);
                     if (gm < n && gk < n) {
-                        const size_t at = gm + (size_t)gk * n;
+                        const size_t at = TA ? gk + (size_t)gm * n : gm + (size_t)gk * n;
                         v = ADF ? static_cast<const float2*>(Av)[at]
                                 : d_to_df(static_cast<const double*>(Av)[at]);
                     }
@@ -251,11 +253,11 @@ __device__ __noinline__ void mm_dfx(int n, void* __restrict__ Cv, const void* __
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const int e = tid + t * DQMC_NT;
-                    const int kk = e & 15, jj = e >> 4;
+                    const int kk = TB ? e >> 6 : e & 15, jj = TB ? e & 63 : e >> 4;
                     const int gk = k0 + kk, gj = n0 + jj;
                     float2 v = make_float2(0.f, 0.f);
                     if (gk < n && gj < n) {
-                        const size_t at = gk + (size_t)gj * n;
+                        const size_t at = TB ? gj + (size_t)gk * n : gk + (size_t)gj * n;
                         v = BDF ? static_cast<const float2*>(Bv)[at]
                                 : d_to_df(static_cast<const double*>(Bv)[at]);
                     }

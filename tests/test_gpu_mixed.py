@@ -1,5 +1,6 @@
-"""Mixed-precision path: wraps and slice-matrix chains in split FP32, UDT,
-reconstruction, determinant ratios and rank-1 updates in FP64.  Every result is
+"""Mixed-precision path: wraps, slice-matrix chains and the reconstruction's
+products in split FP32; UDT factorisations, triangular solves, determinant
+ratios and rank-1 updates in FP64.  Every result is
 compared with the FP64 oracle; the target is max |dG| <= 1e-6."""
 import numpy as np
 import pytest
