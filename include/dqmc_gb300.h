@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define DQMC_GB300_ABI_VERSION 6
+#define DQMC_GB300_ABI_VERSION 7
 
 /* status codes */
 #define DQMC_OK 0
@@ -96,6 +96,13 @@ typedef struct {
     int32_t current_slice, current_range, direction, status;
     int64_t imaginary_probability; /* proposals with |imag(p)| > 1e-6 (complex chains) */
     double max_imaginary_probability; /* max |imag(p)| of those */
+    /* the rest of DQMCAnalysis' MagnitudeStats (statistics.jl:9-36): min and the
+     * geometric mean (10^mean log10|v|) of the recorded propagation errors
+     * (> 1e-7), of |p| of the negative probabilities (with their max) and of the
+     * imaginary parts; 0 when nothing was recorded */
+    double min_reported_error, mean_reported_error;
+    double min_negative_probability, mean_negative_probability, max_negative_probability;
+    double min_imaginary_probability, mean_imaginary_probability;
 } dqmc_stats;
 
 /* ---- lifecycle ------------------------------------------------------------

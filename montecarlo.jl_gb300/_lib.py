@@ -41,7 +41,13 @@ class Stats(C.Structure):
                 ("current_slice", C.c_int32), ("current_range", C.c_int32),
                 ("direction", C.c_int32), ("status", C.c_int32),
                 ("imaginary_probability", C.c_int64),
-                ("max_imaginary_probability", C.c_double)]
+                ("max_imaginary_probability", C.c_double),
+                ("min_reported_error", C.c_double), ("mean_reported_error", C.c_double),
+                ("min_negative_probability", C.c_double),
+                ("mean_negative_probability", C.c_double),
+                ("max_negative_probability", C.c_double),
+                ("min_imaginary_probability", C.c_double),
+                ("mean_imaginary_probability", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

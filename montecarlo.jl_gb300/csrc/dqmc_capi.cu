@@ -266,6 +266,11 @@ void fill_descriptor(DqmcChain& d, const dqmc_chain_config& c, char* b, const La
     d.alpha_field = c.alpha;
     d.partner = -1;
     d.global_kind = -1;
+    for (double* ms : {d.ms_prop, d.ms_neg, d.ms_imag}) {  // MagnitudeStats() (statistics.jl:16)
+        ms[0] = -INFINITY;
+        ms[1] = INFINITY;
+        ms[2] = 0.0;
+    }
     d.key = c.seed; d.ctr = 0;
     d.current_slice = 0; d.current_range = 1; d.direction = 1;
     d.active = 1;
@@ -536,6 +541,17 @@ static void fill_stats(const DqmcChain& d, dqmc_stats* s) {
     s->max_reported_error = d.prop_err_reported;
     s->imaginary_probability = d.n_imag_p;
     s->max_imaginary_probability = d.max_imag_p;
+    // MagnitudeStats min / mean / max (statistics.jl:26-28): 10^(log10 stats), 0 when empty
+    auto mag = [](const double* ms, long long cnt, double* mn, double* mean, double* mx) {
+        *mn = cnt > 0 ? pow(10.0, ms[1]) : 0.0;
+        *mean = cnt > 0 ? pow(10.0, ms[2] / (double)cnt) : 0.0;
+        if (mx) *mx = cnt > 0 ? pow(10.0, ms[0]) : 0.0;
+    };
+    mag(d.ms_prop, d.n_prop_err, &s->min_reported_error, &s->mean_reported_error, nullptr);
+    mag(d.ms_neg, d.n_neg_p, &s->min_negative_probability, &s->mean_negative_probability,
+        &s->max_negative_probability);
+    mag(d.ms_imag, d.n_imag_p, &s->min_imaginary_probability, &s->mean_imaginary_probability,
+        nullptr);
     s->current_slice = d.current_slice;
     s->current_range = d.current_range;
     s->direction = d.direction;

@@ -107,7 +107,18 @@ struct DqmcChain {
     double evi[2][4], evinvi[2][4];
     long long n_imag_p;
     double max_imag_p;
+    // MagnitudeStats (statistics.jl:9-36) of the recorded propagation errors
+    // (> 1e-7), negative probabilities and imaginary probabilities: max, min
+    // and sum of log10 |value| each (counts: n_prop_err, n_neg_p, n_imag_p)
+    double ms_prop[3], ms_neg[3], ms_imag[3];
 };
+#define DQMC_MS_PUSH(ms, v)                               \
+    do {                                                  \
+        const double l_ = log10(fabs(v));                 \
+        if (l_ > (ms)[0]) (ms)[0] = l_;                   \
+        if (l_ < (ms)[1]) (ms)[1] = l_;                   \
+        (ms)[2] += l_;                                    \
+    } while (0)
 #define DQMC_CB_MAXPARTS 12
 
 // Measurement accumulators of one chain (doubles):

@@ -649,6 +649,7 @@ __device__ __noinline__ void record_prop_error(const Ctx& x) {
         if (mx > 1e-7) {
             c.n_prop_err += 1;
             if (mx > c.prop_err_reported) c.prop_err_reported = mx;
+            DQMC_MS_PUSH(c.ms_prop, mx);
         }
     }
     __syncthreads();
@@ -886,8 +887,12 @@ __device__ __noinline__ long long sweep_spatial_cplx(const Ctx& x) {
                 if (fabs(pim) > 1e-6) {
                     c.n_imag_p += 1;
                     if (fabs(pim) > c.max_imag_p) c.max_imag_p = fabs(pim);
+                    DQMC_MS_PUSH(c.ms_imag, pim);
                 }
-                if (p < 0.0) c.n_neg_p += 1;
+                if (p < 0.0) {
+                    c.n_neg_p += 1;
+                    DQMC_MS_PUSH(c.ms_neg, p);
+                }
                 int accept;
                 if (p > 1.0) {
                     accept = 1;
@@ -1085,7 +1090,10 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 }
                 if (ghq) detratio = __ddiv_rn(__dmul_rn(detratio, gr), gq);
                 const double p = __dmul_rn(c.wboson[t], detratio);
-                if (p < 0.0) c.n_neg_p += 1;
+                if (p < 0.0) {
+                    c.n_neg_p += 1;
+                    DQMC_MS_PUSH(c.ms_neg, p);
+                }
                 int accept;
                 if (p > 1.0) {
                     accept = 1;

@@ -158,6 +158,11 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
         g.n_neg_p = s->c.n_neg_p;
         g.n_imag_p = s->c.n_imag_p;
         g.max_imag_p = s->c.max_imag_p;
+        for (int q = 0; q < 3; ++q) {
+            g.ms_prop[q] = s->c.ms_prop[q];
+            g.ms_neg[q] = s->c.ms_neg[q];
+            g.ms_imag[q] = s->c.ms_imag[q];
+        }
         g.accepted = s->c.accepted;
         g.proposals = s->c.proposals;
         for (int p = 0; p < 8; ++p) g.timers[p] = s->c.timers[p];

@@ -210,6 +210,20 @@ class DQMC:
             negative_probability=st["negative_probability"],
             imaginary_probability=(st["imaginary_probability"],
                                    st["max_imaginary_probability"]),
+            # DQMCAnalysis' MagnitudeStats (statistics.jl:9-51), since creation
+            magnitude_stats={
+                "propagation_error": dict(count=st["propagation_errors"],
+                                          min=st["min_reported_error"],
+                                          mean=st["mean_reported_error"],
+                                          max=st["max_reported_error"]),
+                "negative_probability": dict(count=st["negative_probability"],
+                                             min=st["min_negative_probability"],
+                                             mean=st["mean_negative_probability"],
+                                             max=st["max_negative_probability"]),
+                "imaginary_probability": dict(count=st["imaginary_probability"],
+                                              min=st["min_imaginary_probability"],
+                                              mean=st["mean_imaginary_probability"],
+                                              max=st["max_imaginary_probability"])},
             runtime=time.time() - t0)
         self.field.conf[:] = self.handle.get_field(0)
         if min_acceptance is not None and self.analysis["acceptance"] < min_acceptance:

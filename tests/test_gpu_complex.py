@@ -207,3 +207,23 @@ def test_complex_max_size_128_sites(pkg, lib):
     assert np.array_equal(h.get_field(0), c.conf)
     assert st["accepted"] == c.accepted
     assert _rel(h.greens(0), c.G) < 1e-9
+
+
+def test_magnitude_stats_of_the_sign_problem(pkg, lib):
+    """DQMCAnalysis' MagnitudeStats on the device: counts equal the oracle's,
+    max equals the oracle's max, and min <= geometric mean <= max."""
+    h, c, model, param, fld = _pair(pkg, lib, "DensityHirschField", L=4, mu=0.5, seed=3)
+    h.initialize_run()
+    c.initialize_run()
+    st = h.sweep(2)[0]
+    c.sweeps(2)
+    assert st["imaginary_probability"] == c.n_imag_p > 0
+    assert abs(st["max_imaginary_probability"] - c.max_imag_p) <= 1e-9 * c.max_imag_p
+    assert 0 < st["min_imaginary_probability"] <= st["mean_imaginary_probability"] \
+        <= st["max_imaginary_probability"] * (1 + 1e-12)
+    if st["negative_probability"] > 0:
+        assert 0 < st["min_negative_probability"] <= st["mean_negative_probability"] \
+            <= st["max_negative_probability"] * (1 + 1e-12)
+    else:
+        assert st["max_negative_probability"] == 0.0
+    assert st["propagation_errors"] == 0 and st["mean_reported_error"] == 0.0

@@ -224,3 +224,26 @@ def test_max_size_honeycomb_512_sites(pkg, lib, oracle):
     assert np.array_equal(h.get_field(0), oc.get_conf())
     assert h.get_rng(0)[1] == oc.rng_counter()
     assert maxdiff(h.greens(0), oc.greens()) < TOL_G
+
+
+def test_negative_probability_magnitude_stats(pkg, lib, oracle):
+    """A sign problem (repulsive U away from half filling): the device counts
+    the same negative probabilities as the oracle and reports the
+    MagnitudeStats min <= geometric mean <= max of |p| (statistics.jl:9-36)."""
+    from _util import chain_config, make_setup, oracle_chain
+    model, param, fld, exps = make_setup(pkg, L=4, U=-4.0, mu=0.6, beta=2.0, safe_mult=5,
+                                         field=pkg.MagneticHirschField)
+    h = lib.Handle([chain_config(lib, model, param, fld, 21)])
+    h.set_hopping(-1, exps)
+    h.init_random_field(0)
+    oc = oracle_chain(oracle, model, param, fld, exps, 21)
+    oc.init_random_conf()
+    h.initialize_run()
+    oc.initialize_run()
+    st = h.sweep(3)[0]
+    oc.sweeps(3)
+    assert np.array_equal(h.get_field(0), oc.get_conf())
+    n_neg = oc.analysis()["negative_probability"]
+    assert st["negative_probability"] == n_neg > 0
+    assert 0 < st["min_negative_probability"] <= st["mean_negative_probability"] \
+        <= st["max_negative_probability"] * (1 + 1e-12)
