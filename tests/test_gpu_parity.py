@@ -231,7 +231,7 @@ def test_negative_probability_magnitude_stats(pkg, lib, oracle):
     the same negative probabilities as the oracle and reports the
     MagnitudeStats min <= geometric mean <= max of |p| (statistics.jl:9-36)."""
     from _util import chain_config, make_setup, oracle_chain
-    model, param, fld, exps = make_setup(pkg, L=4, U=-4.0, mu=0.6, beta=2.0, safe_mult=5,
+    model, param, fld, exps = make_setup(pkg, L=4, U=-8.0, mu=1.0, beta=4.0, safe_mult=5,
                                          field=pkg.MagneticHirschField)
     h = lib.Handle([chain_config(lib, model, param, fld, 21)])
     h.set_hopping(-1, exps)
