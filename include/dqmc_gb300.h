@@ -117,6 +117,12 @@ int dqmc_abi_version(void);
  * NULL restores the handle's own stream.  Lets a host time or order the
  * library's launches with its own CUDA events and streams. */
 int dqmc_set_stream(dqmc_handle* h, void* cuda_stream);
+/* Sweeps of handles whose chains all have n_sites <= 32 (real, FP64, dense
+ * hopping, no device measurements or scheduled global updates) run one warp
+ * per chain, eight chains per CTA, instead of one CTA per chain (default
+ * enable = 1; pools always use the CTA kernel).  Same state, workspace and
+ * accept/reject decisions; sums in a different order (G agrees to rounding). */
+int dqmc_set_small_chain_kernel(dqmc_handle* h, int enable);
 /* Device bytes one chain needs (stack + Green's function workspace). */
 int64_t dqmc_chain_bytes(const dqmc_chain_config* cfg, int precision);
 

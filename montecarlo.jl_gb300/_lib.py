@@ -79,6 +79,7 @@ EXPORTS = [
     "dqmc_set_measurements", "dqmc_reset_measurements", "dqmc_get_measurements",
     "dqmc_global_update", "dqmc_set_global_schedule", "dqmc_replica_exchange",
     "dqmc_get_global_stats", "dqmc_calculate_greens_kl", "dqmc_set_checkerboard",
+    "dqmc_set_small_chain_kernel",
 ]
 
 GLOBAL_FLIP = 0
@@ -125,6 +126,7 @@ def load(path: str = LIB_PATH):
     L.dqmc_calculate_greens.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
     L.dqmc_get_stack.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
     L.dqmc_set_stream.argtypes = [P, C.c_void_p]
+    L.dqmc_set_small_chain_kernel.argtypes = [P, C.c_int]
     L.dqmc_get_timers.argtypes = [P, C.c_int, C.POINTER(C.c_uint64)]
     L.dqmc_pool_create.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int, C.POINTER(P)]
     L.dqmc_pool_admit.argtypes = [P, C.POINTER(ChainConfig), C.POINTER(C.c_int)]
@@ -219,6 +221,10 @@ class Handle:
         """Run on a caller-owned cudaStream_t (an int handle, e.g. torch's
         ``torch.cuda.current_stream().cuda_stream``); 0 restores the own stream."""
         check(load().dqmc_set_stream(self.h, C.c_void_p(stream_ptr or None)))
+
+    def set_small_chain_kernel(self, enable=True):
+        """Sweeps of n <= 32 chains one warp per chain (default) or one CTA per chain."""
+        check(load().dqmc_set_small_chain_kernel(self.h, int(bool(enable))))
 
     def set_hopping(self, chain, exps):
         e = [np.asfortranarray(x, dtype=np.float64) for x in exps]

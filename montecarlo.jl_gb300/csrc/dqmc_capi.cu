@@ -149,6 +149,7 @@ struct dqmc_handle {
     std::vector<size_t> slot_off, slot_bytes;
     DqmcChain* pinned = nullptr;           // pinned mirror for graph replays
     int n_max = 0;                         // largest n_sites of a fixed handle's chains
+    bool small_kernel = true;              // sweeps of small chains one warp per chain
     std::vector<double*> ut_mem;           // per-chain unequal-time workspaces (lazy)
     std::vector<double*> cb_mem;           // per-chain checkerboard factors
     cudaGraphExec_t graph = nullptr;
@@ -195,9 +196,16 @@ int launch(dqmc_handle* h, int op, int arg0, int arg1, bool sync) {
         int st = push_descriptors(h);
         if (st != DQMC_OK) return st;
     }
-    CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), op, arg0, arg1, h->stream,
-                                      h->pool ? 0 : h->n_max),
-             "chain kernel launch");
+    bool warp = op == DQMC_OP_SWEEP && !h->pool && h->small_kernel && h->n_max <= 32;
+    for (size_t i = 0; warp && i < h->host.size(); ++i)
+        warp = dqmc_warp_kernel_eligible(h->host[i]);
+    if (warp)
+        CUDA_TRY(dqmc_launch_warp_kernel(h->d_chains, (int)h->host.size(), arg0, h->stream, h->n_max),
+                 "warp sweep kernel launch");
+    else
+        CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), op, arg0, arg1,
+                                          h->stream, h->pool ? 0 : h->n_max),
+                 "chain kernel launch");
     if (!sync) {
         h->busy = true;
         return DQMC_OK;
@@ -388,6 +396,13 @@ int dqmc_destroy(dqmc_handle* h) {
     if (h->pinned) cudaFreeHost(h->pinned);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
+    return DQMC_OK;
+}
+
+int dqmc_set_small_chain_kernel(dqmc_handle* h, int enable) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    h->small_kernel = enable != 0;
     return DQMC_OK;
 }
 

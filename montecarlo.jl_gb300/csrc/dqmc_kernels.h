@@ -15,6 +15,14 @@ cudaError_t dqmc_prepare_chain_kernel();
 cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
                                      cudaStream_t stream, int n_max);
 
+// The sweep of chains with n <= 32 sites, one warp per chain (dqmc_warp.cu):
+// nsweeps sweeps of every chain.  n_max: the largest n of the launch (<= 32).
+// Eligible chains: real, FP64, dense hopping, no device measurements, no
+// scheduled global update (free pool slots are skipped).
+bool dqmc_warp_kernel_eligible(const DqmcChain& d);
+cudaError_t dqmc_launch_warp_kernel(DqmcChain* d_chains, int nchains, int nsweeps,
+                                    cudaStream_t stream, int n_max);
+
 #include <string>
 // Records `msg` as the calling thread's dqmc_last_error() text; returns `code`.
 int dqmc_report_error(int code, const std::string& msg);
