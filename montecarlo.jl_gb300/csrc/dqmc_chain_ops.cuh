@@ -466,10 +466,11 @@ __device__ __noinline__ void add_slice_sequence_right(const Ctx& x, int idx) {
 // Products of the Green's reconstruction: FP64, or on a mixed-precision
 // chain with n >= 48 the double-float product on the FP32 pipe (FP64
 // operands split while staged; ~1e-14 relative per product).  The UDT
-// factorisations and triangular solves between them stay FP64.
+// factorisations and triangular solves between them stay FP64, and so does
+// everything of a checkerboard chain.
 template <bool TA, bool TB>
 __device__ __forceinline__ void rmm(const Ctx& x, double* C, const double* A, const double* B) {
-    if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48 && !x.c->cplx)
+    if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48 && !x.c->cplx && !x.c->cb)
         mm_dfx<false, false, false, TA, TB>(x.n, C, A, B, x.s->tiles);
     else
         mm<TA, TB>(x.n, C, A, B, x.s->tiles);
