@@ -392,15 +392,12 @@ def main():
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     h2.set_hopping(-1, [pin_np[m].T for m in range(4)])  # symmetric: F-order views, no copy
-    for j in range(B_chains):
-        h2.set_field(j, conf_pin[j * n * M:(j + 1) * n * M].reshape(n, M, order="F"))
+    h2.set_fields_batch(0, B_chains, conf_pin)
     h2.initialize_run()
     for i in range(args.steps):
         h2.sweep(1)
-        for j in range(B_chains):
-            h2.greens_into(j, g_pin[j * nf * n * n:(j + 1) * nf * n * n])
-            buf = f_pin[j * n * M:(j + 1) * n * M]
-            _lib.check(_lib.load().dqmc_get_field(h2.h, j, _lib.i8ptr(buf)))
+        h2.greens_batch_into(0, B_chains, g_pin)
+        h2.fields_batch_into(0, B_chains, f_pin)
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     if dist:

@@ -173,6 +173,14 @@ int dqmc_get_timers(dqmc_handle* h, int chain, uint64_t* out);
  * (greens.jl:94-125, physical = 1). */
 int dqmc_get_greens(dqmc_handle* h, int chain, int physical, double* out);
 int dqmc_set_greens(dqmc_handle* h, int chain, const double* in);
+/* Chains first .. first+count-1 at once (one strided copy when they are real
+ * chains of equal configuration with evenly spaced workspaces, as a fixed
+ * handle's equal chains are; chain by chain otherwise): their Green's
+ * functions back to back into out (physical = 1: greens!, computed for every
+ * chain of the handle), their fields into / from n*M int8 each. */
+int dqmc_get_greens_batch(dqmc_handle* h, int first, int count, int physical, double* out);
+int dqmc_get_fields_batch(dqmc_handle* h, int first, int count, int8_t* out);
+int dqmc_set_fields_batch(dqmc_handle* h, int first, int count, const int8_t* in);
 /* Replaces: calculate_greens(mc, slice, output, field, safe_mult) (stack.jl:525-583).
  * safe_mult <= 0 uses the chain's own. */
 int dqmc_calculate_greens(dqmc_handle* h, int chain, int slice, int safe_mult, double* out);

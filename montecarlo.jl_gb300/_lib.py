@@ -79,7 +79,8 @@ EXPORTS = [
     "dqmc_set_measurements", "dqmc_reset_measurements", "dqmc_get_measurements",
     "dqmc_global_update", "dqmc_set_global_schedule", "dqmc_replica_exchange",
     "dqmc_get_global_stats", "dqmc_calculate_greens_kl", "dqmc_set_checkerboard",
-    "dqmc_set_small_chain_kernel",
+    "dqmc_set_small_chain_kernel", "dqmc_get_greens_batch", "dqmc_get_fields_batch",
+    "dqmc_set_fields_batch",
 ]
 
 GLOBAL_FLIP = 0
@@ -127,6 +128,9 @@ def load(path: str = LIB_PATH):
     L.dqmc_get_stack.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
     L.dqmc_set_stream.argtypes = [P, C.c_void_p]
     L.dqmc_set_small_chain_kernel.argtypes = [P, C.c_int]
+    L.dqmc_get_greens_batch.argtypes = [P, C.c_int, C.c_int, C.c_int, dp]
+    L.dqmc_get_fields_batch.argtypes = [P, C.c_int, C.c_int, i8p]
+    L.dqmc_set_fields_batch.argtypes = [P, C.c_int, C.c_int, i8p]
     L.dqmc_get_timers.argtypes = [P, C.c_int, C.POINTER(C.c_uint64)]
     L.dqmc_pool_create.argtypes = [C.c_int, C.c_int, C.c_int64, C.c_int, C.POINTER(P)]
     L.dqmc_pool_admit.argtypes = [P, C.POINTER(ChainConfig), C.POINTER(C.c_int)]
@@ -310,6 +314,17 @@ class Handle:
     def greens_into(self, chain, buf, physical=False):
         """Download G into a preallocated flat float64 buffer (no reshaping)."""
         check(load().dqmc_get_greens(self.h, chain, int(bool(physical)), dptr(buf)))
+
+    def greens_batch_into(self, first, count, buf, physical=False):
+        """Green's functions of chains first .. first+count-1 into one flat buffer."""
+        check(load().dqmc_get_greens_batch(self.h, int(first), int(count), int(bool(physical)),
+                                           dptr(buf)))
+
+    def fields_batch_into(self, first, count, buf):
+        check(load().dqmc_get_fields_batch(self.h, int(first), int(count), i8ptr(buf)))
+
+    def set_fields_batch(self, first, count, buf):
+        check(load().dqmc_set_fields_batch(self.h, int(first), int(count), i8ptr(buf)))
 
     def set_greens(self, chain, G):
         buf = complex_blocks_to_buf(G) if is_complex(self.cfg(chain)) else blocks_to_buf(G)

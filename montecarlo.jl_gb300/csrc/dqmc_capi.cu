@@ -677,6 +677,107 @@ int dqmc_get_greens(dqmc_handle* h, int chain, int physical, double* out) {
     return download_mat(h, chain, h->host[chain].G, out);
 }
 
+// chains first .. first+count-1: real, active, equal configurations, workspaces
+// at one arena stride (so one strided copy moves all of them)
+static bool uniform_range(dqmc_handle* h, int first, int count, size_t* stride) {
+    const dqmc_chain_config& c0 = h->cfg[first];
+    const char* g0 = (const char*)h->host[first].G;
+    const size_t s = count > 1 ? (size_t)((const char*)h->host[first + 1].G - g0) : 0;
+    for (int i = first; i < first + count; ++i) {
+        const dqmc_chain_config& c = h->cfg[i];
+        const DqmcChain& d = h->host[i];
+        if (!d.active || is_cplx(c) || c.n_sites != c0.n_sites || c.n_flavors != c0.n_flavors ||
+            c.slices != c0.slices || (const char*)d.G != g0 + (size_t)(i - first) * s ||
+            (const char*)d.conf != (const char*)h->host[first].conf + (size_t)(i - first) * s ||
+            (const char*)d.out != (const char*)h->host[first].out + (size_t)(i - first) * s)
+            return false;
+    }
+    *stride = s;
+    return count == 1 || s > 0;
+}
+static int check_range(dqmc_handle* h, int first, int count, const void* buf, const char* what) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (!buf || count < 1 || first < 0 || first + count > (int)h->cfg.size())
+        return fail(DQMC_ERR_INVALID, std::string(what) + ": bad range or null buffer");
+    for (int i = first; i < first + count; ++i)
+        if (int st = check_chain(h, i)) return st;
+    return DQMC_OK;
+}
+
+int dqmc_get_greens_batch(dqmc_handle* h, int first, int count, int physical, double* out) {
+    if (int st = check_range(h, first, count, out, "dqmc_get_greens_batch")) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    if (physical)
+        if (int st = launch(h, DQMC_OP_PHYSICAL, 0, 0, true)) return st;
+    size_t stride = 0;
+    if (!uniform_range(h, first, count, &stride)) {
+        size_t off = 0;
+        for (int i = first; i < first + count; ++i) {
+            if (int st = download_mat(h, i, physical ? h->host[i].out : h->host[i].G, out + off))
+                return st;
+            off += user_elems(h->cfg[i]);
+        }
+        return DQMC_OK;
+    }
+    const size_t bytes = mat_elems(h->cfg[first]) * sizeof(double);
+    const void* src = physical ? (const void*)h->host[first].out : (const void*)h->host[first].G;
+    CUDA_TRY(cudaMemcpy2DAsync(out, bytes, src, count > 1 ? stride : bytes, bytes, count,
+                               cudaMemcpyDeviceToHost, h->stream),
+             "download Green's functions");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+int dqmc_get_fields_batch(dqmc_handle* h, int first, int count, int8_t* out) {
+    if (int st = check_range(h, first, count, out, "dqmc_get_fields_batch")) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    size_t stride = 0;
+    if (!uniform_range(h, first, count, &stride)) {
+        size_t off = 0;
+        for (int i = first; i < first + count; ++i) {
+            if (int st = dqmc_get_field(h, i, out + off)) return st;
+            off += (size_t)h->cfg[i].n_sites * h->cfg[i].slices;
+        }
+        return DQMC_OK;
+    }
+    const size_t bytes = (size_t)h->cfg[first].n_sites * h->cfg[first].slices;
+    CUDA_TRY(cudaMemcpy2DAsync(out, bytes, h->host[first].conf, count > 1 ? stride : bytes, bytes,
+                               count, cudaMemcpyDeviceToHost, h->stream),
+             "download fields");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+int dqmc_set_fields_batch(dqmc_handle* h, int first, int count, const int8_t* in) {
+    if (int st = check_range(h, first, count, in, "dqmc_set_fields_batch")) return st;
+    size_t stride = 0;
+    if (!uniform_range(h, first, count, &stride)) {
+        size_t off = 0;
+        for (int i = first; i < first + count; ++i) {
+            if (int st = dqmc_set_field(h, i, in + off)) return st;
+            off += (size_t)h->cfg[i].n_sites * h->cfg[i].slices;
+        }
+        return DQMC_OK;
+    }
+    const dqmc_chain_config& c = h->cfg[first];
+    const size_t bytes = (size_t)c.n_sites * c.slices;
+    const bool ghq = c.field >= 2;
+    for (size_t e = 0; e < bytes * count; ++e) {
+        const int v = in[e];
+        if (!(ghq ? (v >= 1 && v <= 4) : (v == 1 || v == -1)))
+            return fail(DQMC_ERR_INVALID, "dqmc_set_fields_batch: value out of range for the field kind");
+    }
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    CUDA_TRY(cudaMemcpy2DAsync(h->host[first].conf, count > 1 ? stride : bytes, in, bytes, bytes,
+                               count, cudaMemcpyHostToDevice, h->stream),
+             "upload fields");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
 int dqmc_set_greens(dqmc_handle* h, int chain, const double* in) {
     if (int st = check_chain(h, chain)) return st;
     if (!in) return fail(DQMC_ERR_INVALID, "dqmc_set_greens: null in");

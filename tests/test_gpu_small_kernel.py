@@ -71,3 +71,45 @@ def test_warp_kernel_mixed_batch_and_async(pkg, lib):
         h1.sweep(3)
         assert np.array_equal(h.get_field(i), h1.get_field(0))
         assert maxdiff(h.greens(i), h1.greens(0)) < 1e-12
+
+
+def test_batched_transfers_equal_per_chain(pkg, lib):
+    """dqmc_get_greens_batch / dqmc_get_fields_batch / dqmc_set_fields_batch
+    (one strided copy for equal chains, chain by chain otherwise) move the
+    same bytes as the per-chain calls."""
+    for Ls in ((4, 4, 4, 4, 4), (2, 4, 3)):
+        setups = [make_setup(pkg, L=L, U=-4.0, beta=2.0, safe_mult=5) for L in Ls]
+        cfgs = [chain_config(lib, m, p, f, 50 + i) for i, (m, p, f, e) in enumerate(setups)]
+        h = lib.Handle(cfgs)
+        for i, s in enumerate(setups):
+            h.set_hopping(i, s[3])
+        sizes = [len(m.l) * p.slices for m, p, f, e in setups]
+        rng = np.random.default_rng(len(Ls))
+        conf = rng.choice(np.array([-1, 1], dtype=np.int8), size=sum(sizes))
+        h.set_fields_batch(0, len(Ls), conf)
+        back = np.zeros_like(conf)
+        h.fields_batch_into(0, len(Ls), back)
+        assert np.array_equal(back, conf)
+        h.initialize_run()
+        h.sweep(1)
+        nf = [f.unique_flavors * len(m.l) ** 2 for m, p, f, e in setups]
+        for physical in (False, True):
+            g = np.zeros(sum(nf))
+            h.greens_batch_into(0, len(Ls), g, physical=physical)
+            off = 0
+            for i in range(len(Ls)):
+                one = np.zeros(nf[i])
+                h.greens_into(i, one, physical=physical)
+                assert np.array_equal(g[off:off + nf[i]], one)
+                off += nf[i]
+        f = np.zeros(sum(sizes), dtype=np.int8)
+        h.fields_batch_into(0, len(Ls), f)
+        off = 0
+        for i in range(len(Ls)):
+            assert np.array_equal(f[off:off + sizes[i]], h.get_field(i).ravel(order="F"))
+            off += sizes[i]
+        # a sub-range
+        g2 = np.zeros(nf[1] + nf[2])
+        h.greens_batch_into(1, 2, g2)
+        assert np.array_equal(g2[:nf[1]], g[nf[0]:nf[0] + nf[1]]) or physical
+        h.close()
