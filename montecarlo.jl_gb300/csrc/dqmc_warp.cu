@@ -9,7 +9,7 @@
 // column (two lanes per column when n <= 16), the Householder QR gives each
 // lane one trailing column, triangular solves give each lane one row, and the
 // rank-1 update is lane-strided over G, which stays in shared memory for the
-// whole launch.  Sixteen chains run per SM instead of four.
+// whole launch.  Up to 24 chains run per SM instead of four.
 //
 // Same algorithm, state and workspace as the CTA kernel (dqmc_chain_ops.cuh),
 // for the sweep operation only: the decision arithmetic is the same sequence
@@ -84,29 +84,35 @@ __device__ __forceinline__ void wdright(const W& x, double* C, const double* A, 
     __syncwarp();
 }
 
-// C = op(A) op(B) for one n x n block (n <= NB): lane l owns column l % NB and
-// rows [(l / NB) RPL, ... + RPL); fused multiply-adds in ascending k.  C must
-// not alias A or B.
+// C = op(A) op(B) for one n x n block (n <= NB): n <= 16: lane l owns
+// column l % 16 and rows [8 (l / 16), ... + 8); n <= 32: lane l owns column l
+// in two passes of 16 rows (16 accumulators either way).  Fused
+// multiply-adds in ascending k.  C must not alias A or B.
 template <int NB, bool TA, bool TB>
 __device__ __noinline__ void wmm(const W& x, double* __restrict__ C, const double* __restrict__ A,
                                  const double* __restrict__ B) {
-    constexpr int LPC = 32 / NB, RPL = NB / LPC;
-    const int n = x.n, col = x.lane % NB, r0 = (x.lane / NB) * RPL;
-    double acc[RPL];
-#pragma unroll
-    for (int r = 0; r < RPL; ++r) acc[r] = 0.0;
+    constexpr int LPC = NB == 16 ? 2 : 1, RPL = NB == 16 ? 8 : 16, PASSES = NB == 16 ? 1 : 2;
+    const int n = x.n, col = x.lane % (32 / LPC);
     if (col < n) {
-        for (int k = 0; k < n; ++k) {
-            const double b = TB ? B[col + (size_t)k * n] : B[k + (size_t)col * n];
+        for (int pass = 0; pass < PASSES; ++pass) {
+            const int r0 = NB == 16 ? (x.lane / 16) * RPL : pass * RPL;
+            if (r0 >= n) break;
+            double acc[RPL];
 #pragma unroll
-            for (int r = 0; r < RPL; ++r) {
-                const int i = r0 + r;
-                if (i < n) acc[r] = fma(TA ? A[k + (size_t)i * n] : A[i + (size_t)k * n], b, acc[r]);
+            for (int r = 0; r < RPL; ++r) acc[r] = 0.0;
+            for (int k = 0; k < n; ++k) {
+                const double b = TB ? B[col + (size_t)k * n] : B[k + (size_t)col * n];
+#pragma unroll
+                for (int r = 0; r < RPL; ++r) {
+                    const int i = r0 + r;
+                    if (i < n)
+                        acc[r] = fma(TA ? A[k + (size_t)i * n] : A[i + (size_t)k * n], b, acc[r]);
+                }
             }
-        }
 #pragma unroll
-        for (int r = 0; r < RPL; ++r)
-            if (r0 + r < n) C[r0 + r + (size_t)col * n] = acc[r];
+            for (int r = 0; r < RPL; ++r)
+                if (r0 + r < n) C[r0 + r + (size_t)col * n] = acc[r];
+        }
     }
     __syncwarp();
 }
@@ -604,8 +610,11 @@ __device__ __noinline__ void sweep_spatial(const W& x) {
 
 // One warp per chain: `nsweeps` sweeps (local_sweep, local_updates.jl:7-14)
 // of every chain, the sweep counter advanced after each (the scheduler's
-// mc.last_sweep).
-__global__ void __launch_bounds__(32 * WPC, 2)
+// mc.last_sweep).  MINB CTAs per SM: three for n <= 16 (80 registers, 24
+// chains per SM, shared memory 3 x 71 KB), one for n <= 32 (8 chains per
+// SM: 178 KB of shared memory per CTA).
+template <int MINB>
+__global__ void __launch_bounds__(32 * WPC, MINB)
     warp_sweep_kernel(DqmcChain* chains, int nchains, int nsweeps, int nmax) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const Layout L = layout(nmax);
@@ -689,14 +698,22 @@ cudaError_t dqmc_launch_warp_kernel(DqmcChain* d_chains, int nchains, int nsweep
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        e = cudaFuncSetAttribute(dqmc_warp::warp_sweep_kernel,
+        e = cudaFuncSetAttribute(dqmc_warp::warp_sweep_kernel<3>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(dqmc_warp::WPC * dqmc_warp::layout(32).bytes));
+                                 (int)(dqmc_warp::WPC * dqmc_warp::layout(16).bytes));
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dqmc_warp::warp_sweep_kernel<1>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(dqmc_warp::WPC * dqmc_warp::layout(32).bytes));
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
     const int grid = (nchains + dqmc_warp::WPC - 1) / dqmc_warp::WPC;
-    dqmc_warp::warp_sweep_kernel<<<grid, 32 * dqmc_warp::WPC, smem, stream>>>(d_chains, nchains,
-                                                                            nsweeps, nmax);
+    if (nmax == 16)
+        dqmc_warp::warp_sweep_kernel<3><<<grid, 32 * dqmc_warp::WPC, smem, stream>>>(
+            d_chains, nchains, nsweeps, nmax);
+    else
+        dqmc_warp::warp_sweep_kernel<1><<<grid, 32 * dqmc_warp::WPC, smem, stream>>>(
+            d_chains, nchains, nsweeps, nmax);
     return cudaGetLastError();
 }
