@@ -303,9 +303,9 @@ def main():
     n, nf, M = len(model.l), fld.unique_flavors, param.slices
     nr = len(pkg.generate_chunks(M, param.safe_mult))
     # resident chains: two per SM (one CTA each); for lattices of n <= 32
-    # sites, whose sweeps run one warp per chain (eight per CTA), 24 (n <= 16)
+    # sites, whose sweeps run one warp per chain (eight per CTA), 16 (n <= 16)
     # or 8 per SM
-    B_chains = args.chains or (24 if n <= 16 else 8 if n <= 32 else 2) * nsm
+    B_chains = args.chains or (16 if n <= 16 else 8 if n <= 32 else 2) * nsm
 
     def configs(base_seed):
         return [_lib.ChainConfig(n, nf, M, param.safe_mult, fld.kind, 1, fld.alpha, base_seed + j)

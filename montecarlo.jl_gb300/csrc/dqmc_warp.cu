@@ -9,7 +9,7 @@
 // column (two lanes per column when n <= 16), the Householder QR gives each
 // lane one trailing column, triangular solves give each lane one row, and the
 // rank-1 update is lane-strided over G, which stays in shared memory for the
-// whole launch.  Up to 24 chains run per SM instead of four.
+// whole launch.  Sixteen chains run per SM instead of four.
 //
 // Same algorithm, state and workspace as the CTA kernel (dqmc_chain_ops.cuh),
 // for the sweep operation only: the decision arithmetic is the same sequence
@@ -610,9 +610,9 @@ __device__ __noinline__ void sweep_spatial(const W& x) {
 
 // One warp per chain: `nsweeps` sweeps (local_sweep, local_updates.jl:7-14)
 // of every chain, the sweep counter advanced after each (the scheduler's
-// mc.last_sweep).  MINB CTAs per SM: three for n <= 16 (80 registers, 24
-// chains per SM, shared memory 3 x 71 KB), one for n <= 32 (8 chains per
-// SM: 178 KB of shared memory per CTA).
+// mc.last_sweep).  MINB CTAs per SM: two for n <= 16 (16 chains per SM, 71 KB
+// of shared memory each; a third CTA measured no faster: the FP64 pipe and
+// issue are busy), one for n <= 32 (8 chains per SM, 178 KB).
 template <int MINB>
 __global__ void __launch_bounds__(32 * WPC, MINB)
     warp_sweep_kernel(DqmcChain* chains, int nchains, int nsweeps, int nmax) {
@@ -698,7 +698,7 @@ cudaError_t dqmc_launch_warp_kernel(DqmcChain* d_chains, int nchains, int nsweep
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev >= 0 && dev < 64 && !attr_set[dev]) {
-        e = cudaFuncSetAttribute(dqmc_warp::warp_sweep_kernel<3>,
+        e = cudaFuncSetAttribute(dqmc_warp::warp_sweep_kernel<2>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)(dqmc_warp::WPC * dqmc_warp::layout(16).bytes));
         if (e == cudaSuccess)
@@ -710,7 +710,7 @@ cudaError_t dqmc_launch_warp_kernel(DqmcChain* d_chains, int nchains, int nsweep
     }
     const int grid = (nchains + dqmc_warp::WPC - 1) / dqmc_warp::WPC;
     if (nmax == 16)
-        dqmc_warp::warp_sweep_kernel<3><<<grid, 32 * dqmc_warp::WPC, smem, stream>>>(
+        dqmc_warp::warp_sweep_kernel<2><<<grid, 32 * dqmc_warp::WPC, smem, stream>>>(
             d_chains, nchains, nsweeps, nmax);
     else
         dqmc_warp::warp_sweep_kernel<1><<<grid, 32 * dqmc_warp::WPC, smem, stream>>>(
