@@ -608,6 +608,104 @@ __device__ __noinline__ void sweep_spatial(const W& x) {
     }
 }
 
+// The same sweep for Hirsch fields with the proposals evaluated in parallel:
+// from site j on, lane k computes the ratio of site j + k on the current G
+// (valid for every site up to the first acceptance, since G changes only
+// there), each lane takes its uniform at the counter the sequential loop
+// would reach (a ballot and prefix count of the proposals with p <= 1 before
+// it), and the first accepting lane wins; the proposals after it are
+// evaluated again on the updated G.  Every decision is the sequential loop's
+// (same operations, same uniforms); on GB300 a scalar FP64 operation of lane 0
+// costs as much FP64-pipe time as a full warp's, so up to 32 proposals cost
+// one.
+__device__ __noinline__ void sweep_spatial_hirsch(const W& x) {
+    DqmcChain& c = *x.c;
+    const int n = x.n, nf = x.nf, lane = x.lane;
+    int8_t* s = c.conf + (size_t)(c.current_slice - 1) * n;
+    const bool twoflv = (nf == 2);
+    int j = 0;
+    while (j < n) {
+        const int jj = j + lane;
+        const bool valid = jj < n;
+        double p = 0.0, R0 = 1.0, R1 = 1.0, d0 = 0.0, d1 = 0.0;
+        if (valid) {
+            const double g0 = x.G[(size_t)jj * n + jj];
+            const double g1 = twoflv ? x.G[(size_t)x.nn + (size_t)jj * n + jj] : 0.0;
+            const int t = s[jj] > 0 ? 1 : 0;
+            d0 = c.delta0[t];
+            d1 = c.delta1[t];
+            R0 = __dadd_rn(1.0, __dmul_rn(d0, __dsub_rn(1.0, g0)));
+            double detratio;
+            if (twoflv) {
+                R1 = __dadd_rn(1.0, __dmul_rn(d1, __dsub_rn(1.0, g1)));
+                detratio = __dmul_rn(R0, R1);
+            } else {
+                detratio = __dmul_rn(R0, R0);
+            }
+            p = __dmul_rn(c.wboson[t], detratio);
+        }
+        const unsigned need = __ballot_sync(FULL, valid && !(p > 1.0));
+        const unsigned below = (1u << lane) - 1u;  // lanes before this one
+        bool acc = false;
+        if (valid) {
+            if (p > 1.0) {
+                acc = true;
+            } else {
+                const uint64_t w = dqmc_philox_word(c.key, c.ctr + (uint64_t)__popc(need & below));
+                acc = dqmc_word_to_uniform(w) < p;
+            }
+        }
+        const unsigned am = __ballot_sync(FULL, acc);
+        const unsigned vm = __ballot_sync(FULL, valid);
+        const int last = am ? __ffs(am) - 1 : 31 - __clz(vm);  // last proposal of this round
+        const unsigned done = last == 31 ? FULL : ((2u << last) - 1u);
+        // negative probabilities of the proposals made, in order
+        unsigned neg = __ballot_sync(FULL, valid && p < 0.0) & done;
+        while (neg) {
+            const int k = __ffs(neg) - 1;
+            const double pk = __shfl_sync(FULL, p, k);
+            if (lane == 0) {
+                c.n_neg_p += 1;
+                DQMC_MS_PUSH(c.ms_neg, pk);
+            }
+            neg &= neg - 1u;
+        }
+        if (lane == 0) {
+            c.ctr += (uint64_t)__popc(need & done);
+            c.proposals += __popc(vm & done);
+        }
+        if (!am) break;
+        // accept_local! of site j + last
+        const int ja = j + last;
+        double sx0 = 0.0, sx1 = 0.0;
+        if (lane == last) {
+            sx0 = __ddiv_rn(d0, R0);
+            sx1 = twoflv ? __ddiv_rn(d1, R1) : 0.0;
+            s[ja] = (int8_t)(-s[ja]);
+            c.accepted += 1;
+        }
+        sx0 = __shfl_sync(FULL, sx0, last);
+        sx1 = __shfl_sync(FULL, sx1, last);
+        __syncwarp();
+        for (int e = lane; e < nf * n; e += 32) {
+            const int b = e / n, k = e % n;
+            const double* g = x.G + (size_t)b * x.nn;
+            double ig = -g[(size_t)ja * n + k];
+            if (k == ja) ig += 1.0;
+            x.u[e] = ig;
+            x.w[e] = (b ? sx1 : sx0) * g[(size_t)k * n + ja];
+        }
+        __syncwarp();
+        for (int e = lane; e < nf * x.nn; e += 32) {
+            const int b = e / x.nn, r = e % x.nn;
+            const int k = r % n, l = r / n;
+            x.G[e] = fma(-x.u[b * n + k], x.w[b * n + l], x.G[e]);
+        }
+        __syncwarp();
+        j = ja + 1;
+    }
+}
+
 // One warp per chain: `nsweeps` sweeps (local_sweep, local_updates.jl:7-14)
 // of every chain, the sweep counter advanced after each (the scheduler's
 // mc.last_sweep).  MINB CTAs per SM: two for n <= 16 (16 chains per SM, 71 KB
@@ -650,7 +748,8 @@ __global__ void __launch_bounds__(32 * WPC, MINB)
     for (int sw = 0; sw < nsweeps; ++sw) {
         for (int t = 0; t < 2 * c->M; ++t) {
             const long long t0 = tstart(x);
-            sweep_spatial(x);
+            if (c->kind >= 2) sweep_spatial(x);
+            else sweep_spatial_hirsch(x);
             tstop(x, DQMC_PHASE_SWEEP_SPATIAL, t0);
             propagate(x);
         }
