@@ -526,7 +526,6 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout, bool f
                *tr = blk(c.Tr, x, b), *g = blk(Gout, x, b);
         double *dl = c.Dl + b * n, *dr = c.Dr + b * n;
         int* pv = c.pivot + b * n;
-        double* tv = c.tempv + b * n;
         rmm<false, true>(x, g, tl, tr);
         __syncthreads();
         dright(n, tr, g, dr);
