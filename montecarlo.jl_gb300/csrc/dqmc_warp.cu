@@ -124,23 +124,31 @@ __device__ __forceinline__ void mm(const W& x, double* C, const double* A, const
 
 // udt_AVX_pivot! (UDT.jl:216-334) of one block, warp-synchronous: the same
 // outputs as the CTA kernel's udt_pivot (pivot 1-based, reflectors below the
-// diagonal, tau, D = |diag R| (0 -> 1), T pivoted or not); lane l owns
-// trailing column j + l of each step (n <= 32).  scr: n x n (apply only).
-__device__ __noinline__ void wudt(const W& x, double* __restrict__ U, double* __restrict__ D,
-                                  double* __restrict__ In, int* __restrict__ piv,
-                                  double* __restrict__ tau, bool apply, double* __restrict__ scr) {
+// diagonal, tau, D = |diag R| (0 -> 1), T pivoted or not).  Each trailing
+// column of a step is owned by LPC lanes: two for n <= 16 (lane l: column
+// j + l % 16, rows of parity l / 16, sums combined by a shuffle), one above.
+// scr: n x n (apply only).
+template <int LPC>
+__device__ __noinline__ void wudt_t(const W& x, double* __restrict__ U, double* __restrict__ D,
+                                    double* __restrict__ In, int* __restrict__ piv,
+                                    double* __restrict__ tau, bool apply, double* __restrict__ scr) {
     const int n = x.n, lane = x.lane;
+    const int co = LPC == 2 ? (lane & 15) : lane;  // column offset this lane works on
+    const int h = LPC == 2 ? (lane >> 4) : 0;       // its row parity
     for (int i = lane; i < n; i += 32) piv[i] = i + 1;
     __syncwarp();
     for (int j = 0; j < n; ++j) {
         // indmaxcolumn: squared norms of the trailing columns, first maximum
-        const int col = j + lane;
+        const int col = j + co;
+        double s = 0.0;
+        if (col < n) {
+            const double* xc = In + (size_t)col * n;
+            for (int r = j + h; r < n; r += LPC) s = fma(xc[r], xc[r], s);
+        }
+        if (LPC == 2) s += __shfl_xor_sync(FULL, s, 16);
         double best = -1.0;
         int bi = j;
         if (col < n) {
-            const double* xc = In + (size_t)col * n;
-            double s = 0.0;
-            for (int r = j; r < n; ++r) s = fma(xc[r], xc[r], s);
             best = s;
             bi = col;
         }
@@ -182,15 +190,19 @@ __device__ __noinline__ void wudt(const W& x, double* __restrict__ U, double* __
         if (lane == 0) tau[j] = t;
         __syncwarp();
         // reflectorApply! (UDT.jl:53-70)
-        const int ac = j + 1 + lane;
+        const int ac = j + 1 + co;
+        double* a = In + (size_t)ac * n;
+        double aj = 0.0, s2 = 0.0;
         if (ac < n) {
-            double* a = In + (size_t)ac * n;
-            const double aj = a[j];
-            double s = 0.0;
-            for (int r = j + 1; r < n; ++r) s = fma(xj[r], a[r], s);
-            const double vAj = t * (aj + s);
-            a[j] = aj - vAj;
-            for (int r = j + 1; r < n; ++r) a[r] = fma(-xj[r], vAj, a[r]);
+            if (h == 0) aj = a[j];
+            for (int r = j + 1 + h; r < n; r += LPC) s2 = fma(xj[r], a[r], s2);
+        }
+        if (LPC == 2) s2 += __shfl_xor_sync(FULL, s2, 16);
+        double vAj = t * (aj + s2);
+        if (LPC == 2) vAj = __shfl_sync(FULL, vAj, co);  // the parity-0 lane's value
+        if (ac < n) {
+            if (h == 0) a[j] = aj - vAj;
+            for (int r = j + 1 + h; r < n; r += LPC) a[r] = fma(-xj[r], vAj, a[r]);
         }
         __syncwarp();
     }
@@ -202,46 +214,58 @@ __device__ __noinline__ void wudt(const W& x, double* __restrict__ U, double* __
     for (int k = n - 2; k >= 0; --k) {
         const double* v = In + (size_t)k * n;
         const double tk = tau[k];
-        const int col = k + lane;
+        const int col = k + co;
+        double* u = U + (size_t)col * n;
+        double uk = 0.0, s = 0.0;
         if (col < n) {
-            double* u = U + (size_t)col * n;
-            const double uk = u[k];
-            double s = 0.0;
-            for (int r = k + 1; r < n; ++r) s = fma(v[r], u[r], s);
-            const double vB = tk * (uk + s);
-            u[k] = uk - vB;
-            for (int r = k + 1; r < n; ++r) u[r] = fma(-v[r], vB, u[r]);
+            if (h == 0) uk = u[k];
+            for (int r = k + 1 + h; r < n; r += LPC) s = fma(v[r], u[r], s);
+        }
+        if (LPC == 2) s += __shfl_xor_sync(FULL, s, 16);
+        double vB = tk * (uk + s);
+        if (LPC == 2) vB = __shfl_sync(FULL, vB, co);
+        if (col < n) {
+            if (h == 0) u[k] = uk - vB;
+            for (int r = k + 1 + h; r < n; r += LPC) u[r] = fma(-v[r], vB, u[r]);
         }
         __syncwarp();
     }
     // D (UDT.jl:293-301)
     for (int i = lane; i < n; i += 32) {
-        const double a = fabs(In[(size_t)i * n + i]);
-        D[i] = (a == 0.0) ? 1.0 : a;
+        const double av = fabs(In[(size_t)i * n + i]);
+        D[i] = (av == 0.0) ? 1.0 : av;
     }
     __syncwarp();
     // _apply_pivot! (UDT.jl:311-334)
     if (apply) {
         for (int e = lane; e < x.nn; e += 32) {
-            const int i = e % n, j = e / n;
+            const int i = e % n, jj = e / n;
             const double d = 1.0 / D[i];
-            scr[i + (size_t)(piv[j] - 1) * n] = (j >= i) ? d * In[e] : 0.0;
+            scr[i + (size_t)(piv[jj] - 1) * n] = (jj >= i) ? d * In[e] : 0.0;
         }
         __syncwarp();
         for (int e = lane; e < x.nn; e += 32) In[e] = scr[e];
     } else {
         for (int e = lane; e < x.nn; e += 32) {
-            const int i = e % n, j = e / n;
-            if (j >= i) In[e] = (1.0 / D[i]) * In[e];
+            const int i = e % n, jj = e / n;
+            if (jj >= i) In[e] = (1.0 / D[i]) * In[e];
         }
     }
     __syncwarp();
 }
+__device__ __forceinline__ void wudt(const W& x, double* U, double* D, double* In, int* piv,
+                                     double* tau, bool apply, double* scr) {
+    if (x.n <= 16) wudt_t<2>(x, U, D, In, piv, tau, apply, scr);
+    else wudt_t<1>(x, U, D, In, piv, tau, apply, scr);
+}
 
-// rdivp! (real.jl:198-226): A <- A[:, piv] triu(T)^-1, lane i owns row i.
-// O: n x n scratch.
-__device__ __noinline__ void wrdivp(const W& x, double* __restrict__ A, const double* __restrict__ T,
-                                    double* __restrict__ O, const int* __restrict__ piv) {
+// rdivp! (real.jl:198-226): A <- A[:, piv] triu(T)^-1.  Row i is owned by
+// LPC lanes (two for n <= 16: the k-sum split by parity, combined by a
+// shuffle), one above (two accumulation chains).  O: n x n scratch.
+template <int LPC>
+__device__ __noinline__ void wrdivp_t(const W& x, double* __restrict__ A,
+                                      const double* __restrict__ T, double* __restrict__ O,
+                                      const int* __restrict__ piv) {
     const int n = x.n, lane = x.lane;
     for (int j = lane; j < n; j += 32) x.sv[j] = 1.0 / T[(size_t)j * n + j];
     for (int e = lane; e < x.nn; e += 32) {
@@ -249,21 +273,33 @@ __device__ __noinline__ void wrdivp(const W& x, double* __restrict__ A, const do
         O[e] = A[i + (size_t)(piv[j] - 1) * n];
     }
     __syncwarp();
-    if (lane < n) {
-        const int i = lane;
-        for (int j = 0; j < n; ++j) {
-            const double* tj = T + (size_t)j * n;
-            double x0 = O[i + (size_t)j * n], x1 = 0.0;
-            int k = 0;
-            for (; k + 1 < j; k += 2) {
-                x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
-                x1 = fma(-A[i + (size_t)(k + 1) * n], tj[k + 1], x1);
+    const int i = LPC == 2 ? (lane & 15) : lane, h = LPC == 2 ? (lane >> 4) : 0;
+    for (int j = 0; j < n; ++j) {
+        const double* tj = T + (size_t)j * n;
+        double x0 = 0.0, x1 = 0.0;
+        if (i < n) {
+            if (h == 0) x0 = O[i + (size_t)j * n];
+            if (LPC == 2) {
+                for (int k = h; k < j; k += 2) x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
+            } else {
+                int k = 0;
+                for (; k + 1 < j; k += 2) {
+                    x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
+                    x1 = fma(-A[i + (size_t)(k + 1) * n], tj[k + 1], x1);
+                }
+                if (k < j) x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
             }
-            if (k < j) x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
-            A[i + (size_t)j * n] = (x0 + x1) * x.sv[j];
         }
+        if (LPC == 2) x0 += __shfl_xor_sync(FULL, x0, 16);
+        if (i < n && h == 0) A[i + (size_t)j * n] = (x0 + x1) * x.sv[j];
+        if (LPC == 2) __syncwarp();  // the parity-1 lane reads A[i, j] in later columns
     }
     __syncwarp();
+}
+__device__ __forceinline__ void wrdivp(const W& x, double* A, const double* T, double* O,
+                                       const int* piv) {
+    if (x.n <= 16) wrdivp_t<2>(x, A, T, O, piv);
+    else wrdivp_t<1>(x, A, T, O, piv);
 }
 
 // ---- chain-level operations (the CTA kernel's, warp-synchronous) -----------
