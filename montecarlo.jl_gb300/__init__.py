@@ -17,7 +17,8 @@ from .measurements import (LogBinner, double_occupancy as double_occupancy_kerne
                            interaction_energy, occupation_kernel, spin_density_correlation_z,
                            spin_susceptibility_z, structure_factor, time_displaced_sdc_z,
                            susceptibilities, time_displaced_correlations, CORRELATIONS,
-                           current_operator, bilinear_correlation)
+                           current_operator, bilinear_correlation, pair_form_factor,
+                           pair_correlation)
 from .dqmc import (DQMC, ExitCode, Measurement, double_occupancy, greens_measurement,  # noqa: F401
                    occupation, spin_density_correlation)
 

@@ -145,7 +145,7 @@ class DQMC:
         current_current_susceptibility with TimeIntegral) from one device
         call for the Green's functions G(0,0), G(l,l), G(0,l), G(l,0),
         l = 0..M."""
-        from .measurements import current_operator, susceptibilities
+        from .measurements import current_operator, pair_form_factor, susceptibilities
         M = self.parameters.slices
         pairs = [(0, 0)]
         for l in range(M + 1):
@@ -158,7 +158,10 @@ class DQMC:
             ph = self.model.l.positions() @ np.asarray(q, dtype=float)
             phases = (np.cos(ph), np.sin(ph))
         J = current_operator(self.model.hopping_matrix(), self.model.l, current_direction)
-        return susceptibilities(by_l, phases, self.parameters.delta_tau, current=J)
+        pf = {}
+        if len(self.model.l.unitcell.lattice_vectors) >= 2:
+            pf = {k: pair_form_factor(self.model.l, k) for k in ("s*", "d")}
+        return susceptibilities(by_l, phases, self.parameters.delta_tau, current=J, pair_fields=pf)
 
     def calculate_greens(self, slice_, safe_mult=0):
         """calculate_greens(mc, slice) (stack.jl:525-583), effective G."""

@@ -190,6 +190,50 @@ def current_operator(T, lattice, direction=None):
     return A
 
 
+def pair_form_factor(lattice, kind="s"):
+    """Form-factor matrix F of the pair field Delta = sum_ab F[a, b] c_a,up c_b,dn:
+    "s" on-site (F = I), "s*" extended s-wave (1 on every nearest-neighbour
+    bond) and "d" (d_x2-y2: +1 on bonds along the first lattice vector, -1
+    along the second) -- the reference's pairing quads of
+    EachLocalQuadByDistance (pairing.jl:1-52) contracted with these form
+    factors."""
+    n = len(lattice)
+    if kind == "s":
+        return np.eye(n)
+    uc = lattice.unitcell
+    vecs = np.asarray(uc.lattice_vectors, dtype=float)
+    sites = np.asarray(uc.sites, dtype=float)
+    nbu = len(uc.bonds)
+    F = np.zeros((n, n))
+    for k, (a, b) in enumerate(lattice.bonds()):
+        bond = uc.bonds[k % nbu]
+        disp = sites[bond.to - 1] - sites[bond.frm - 1] + np.asarray(bond.uc_shift, float) @ vecs
+        if kind == "s*":
+            F[a, b] += 1.0
+        elif kind == "d":
+            if abs(abs(disp @ vecs[0]) - vecs[0] @ vecs[0]) < 1e-9 and abs(disp @ vecs[1]) < 1e-9:
+                F[a, b] += 1.0
+            elif abs(abs(disp @ vecs[1]) - vecs[1] @ vecs[1]) < 1e-9 and abs(disp @ vecs[0]) < 1e-9:
+                F[a, b] -= 1.0
+        else:
+            raise ValueError(f"unknown pairing form factor {kind!r}")
+    return F
+
+
+def pair_correlation(F, G00, G0l, Gl0, Gll, at_zero):
+    """<Delta(l dtau) Delta^+(0)> + <Delta^+(l dtau) Delta(0)> for the pair field
+    Delta = sum_ab F[a, b] c_a,up c_b,dn (pc_combined_kernel, pairing.jl:95-161,
+    summed with the form factor): sum(conj(F) o (Gl0_up^T F Gl0_dn)) +
+    sum(conj(F) o (X_up^T F X_dn)), X = id - G0l; one block serves both spins."""
+    up, dn = (0, 0) if G00.shape[0] == 1 else (0, 1)
+    n = G00.shape[1]
+    idm = np.eye(n) if at_zero else np.zeros((n, n))
+    Fc = np.conj(F)
+    t1 = np.sum(Fc * (Gl0[up].T @ F @ Gl0[dn]))
+    t2 = np.sum(Fc * ((idm - G0l[up]).T @ F @ (idm - G0l[dn])))
+    return t1 + t2
+
+
 def bilinear_correlation(A, B, G00, G0l, Gl0, Gll, at_zero):
     """<O_A(l dtau) O_B(0)> for spin-summed bilinears O_A = sum_sigma sum_ab
     A_ab c^+_a c_b (Wick's theorem with G(0,0), G(0,l), G(l,0), G(l,l); one
@@ -206,7 +250,8 @@ def bilinear_correlation(A, B, G00, G0l, Gl0, Gll, at_zero):
     return t1 * t2 + ex
 
 
-def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS, current=None):
+def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS, current=None,
+                     pair_fields=None):
     """chi_K(q) = (1/n) sum_l w_l sum_ij e^{i q (r_i - r_j)} C_K(i, j; l dtau)
     for the correlations K of ``time_displaced_correlations``, with the
     TimeIntegral's trapezoid weights (generic.jl:337-366) and real phases
@@ -216,7 +261,8 @@ def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS, current
     and pairing_susceptibility with an on-site lattice iterator.  With
     ``current`` (a ``current_operator`` matrix) also "current": the uniform
     current-current susceptibility (1/n) int <J(tau) J(0)> dtau, the q = 0
-    sum of the reference's current_current_susceptibility."""
+    sum of the reference's current_current_susceptibility.  ``pair_fields``
+    ({name: F}, see ``pair_form_factor``) adds "pairing_<name>" per form factor."""
     c, s = phases
     n = len(c)
     ones = np.ones(n)
@@ -224,6 +270,8 @@ def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS, current
     chi = {k: 0.0 for k in kinds}
     if current is not None:
         chi["current"] = 0.0
+    for name in (pair_fields or {}):
+        chi["pairing_" + name] = 0.0
     for l, (G00, G0l, Gl0, Gll) in enumerate(greens_by_l):
         C = time_displaced_correlations(G00, G0l, Gl0, Gll, l == 0)
         w = (0.5 if l in (0, M) else 1.0) * delta_tau
@@ -235,6 +283,9 @@ def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS, current
         if current is not None:
             chi["current"] += w * float(np.real(
                 bilinear_correlation(current, current, G00, G0l, Gl0, Gll, l == 0)))
+        for name, F in (pair_fields or {}).items():
+            chi["pairing_" + name] += w * float(np.real(
+                pair_correlation(F, G00, G0l, Gl0, Gll, l == 0)))
     return {k: v / n for k, v in chi.items()}
 
 

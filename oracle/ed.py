@@ -107,6 +107,10 @@ class HubbardED:
         elif kind == "pairing":
             D = sum(c[2 * i] @ c[2 * i + 1] for i in range(n))   # sum_i c_i,up c_i,dn
             return D, D.conj().T
+        elif kind == "pair_field":  # phases is then the form factor F[a, b]
+            D = sum(phases[a, b] * c[2 * a] @ c[2 * b + 1]
+                    for a in range(n) for b in range(n) if phases[a, b] != 0)
+            return D, D.conj().T
         else:
             raise ValueError(kind)
         A = sum(phases[i] * O[i] for i in range(n))
@@ -128,7 +132,7 @@ class HubbardED:
         with np.errstate(over="ignore", invalid="ignore", divide="ignore"):
             f = np.where(np.abs(d) < 1e-12, self.beta, (1.0 - np.exp(-self.beta * d)) / d)
         terms = [self.operators("bilinear" if kind == "current" else kind, phases)]
-        if kind == "pairing":
+        if kind in ("pairing", "pair_field"):
             A, B = terms[0]
             terms.append((B, A))
         tot = 0.0

@@ -98,16 +98,18 @@ def test_all_susceptibilities_match_ed_2x2(pkg, lib, U, mu):
     pos = model.l.positions()
     phases = np.cos(pos @ np.array([np.pi, np.pi]))
     want = {k: E.susceptibility(k, phases) for k in pkg.CORRELATIONS}
+    for ff in ("s*", "d"):  # extended-s and d-wave pair fields
+        want["pairing_" + ff] = E.susceptibility("pair_field", pkg.pair_form_factor(model.l, ff))
     mc = pkg.DQMC(model, beta=1.0, delta_tau=DT, safe_mult=10, seed=45, thermalization=200,
                   sweeps=0, measure_rate=1)
     pkg.run(mc)
-    bins = {k: pkg.LogBinner() for k in pkg.CORRELATIONS}
+    bins = {k: pkg.LogBinner() for k in want}
     for _ in range(1200):
         mc.handle.sweep(1)
         chi = mc.susceptibilities()
-        for k in pkg.CORRELATIONS:
+        for k in want:
             bins[k].push(chi[k])
-    for k in pkg.CORRELATIONS:
+    for k in want:
         chi, err = float(bins[k].mean()), float(bins[k].std_error())
         assert abs(chi - want[k]) <= 3.05 * DT ** 2 + 5 * err, (k, chi, want[k], err)
 

@@ -79,3 +79,37 @@ def test_current_and_bilinear_correlations_exact_at_u0(pkg, oracle, field):
         C = time_displaced_correlations(*q, l == 0)["charge"]
         D = np.diag(ph)
         assert abs(ph @ C @ ph - bilinear_correlation(D, D, *q, l == 0)) < 1e-12
+
+
+@pytest.mark.parametrize("kind", ["s", "s*", "d"])
+def test_pair_fields_exact_at_u0(pkg, oracle, kind):
+    """Pair fields with a form factor (on-site s, extended s, d) through
+    pair_correlation equal ED's <Delta(tau) Delta^+> + <Delta^+(tau) Delta> at
+    every tau (2x2 lattice, U = 0, both block structures); the on-site form
+    factor reproduces the on-site pairing kernel."""
+    import ed
+    from montecarlo_gb300.measurements import (pair_correlation, pair_form_factor,
+                                               time_displaced_correlations)
+    for field in ("DensityHirschField", "MagneticHirschField"):
+        model, param, fld, exps = make_setup(pkg, L=2, U=0.0, mu=0.3, beta=1.0, safe_mult=5,
+                                             field=getattr(pkg, field))
+        o = oracle_chain(oracle, model, param, fld, exps, 3)
+        o.init_random_conf()
+        E = ed.HubbardED(4, model.l.bonds(), 1.0, 0.0, 0.3, param.beta)
+        F = pair_form_factor(model.l, kind)
+        assert np.abs(F).sum() > 0
+        D, Dd = E.operators("pair_field", F)
+        M = param.slices
+        pairs = [(0, 0)]
+        for l in range(M + 1):
+            pairs += [(l, l), (0, l), (l, 0)]
+        Gs = [o.greens_physical(g) for g in o.greens_kl(pairs)]
+        for l in range(M + 1):
+            q = (Gs[0], Gs[2 + 3 * l], Gs[3 + 3 * l], Gs[1 + 3 * l])
+            tau = l * param.delta_tau
+            want = E.correlation(D, Dd, tau) + E.correlation(Dd, D, tau)
+            got = pair_correlation(F, *q, l == 0)
+            assert abs(got - want) < 1e-10, (field, kind, l, got, want)
+            if kind == "s":
+                C = time_displaced_correlations(*q, l == 0)["pairing"]
+                assert abs(got - C.sum()) < 1e-12
