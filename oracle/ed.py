@@ -141,3 +141,20 @@ class HubbardED:
             Bba = (self.V.T @ B @ self.V).T
             tot += np.sum(self.rho_diag[:, None] * Aab * Bba * f)
         return float(np.real(tot)) / self.n
+
+    def susceptibility_grid(self, kind, phases, delta_tau):
+        """The same time integral on the imaginary-time grid l * delta_tau with
+        the trapezoid weights of the reference's TimeIntegral (0.5 dtau at both
+        ends), as the reference's ED tests integrate (expectation_value_integrated
+        with step = delta_tau): the DQMC estimator's quadrature, exactly."""
+        M = int(round(self.beta / delta_tau))
+        terms = [self.operators("bilinear" if kind == "current" else kind, phases)]
+        if kind in ("pairing", "pair_field"):
+            A, B = terms[0]
+            terms.append((B, A))
+        tot = 0.0
+        for l in range(M + 1):
+            w = (0.5 if l in (0, M) else 1.0) * delta_tau
+            for A, B in terms:
+                tot += w * self.correlation(A, B, l * delta_tau)
+        return float(np.real(tot)) / self.n

@@ -58,3 +58,16 @@ def test_gpu_dqmc_run_matches_ed_2x2(pkg, lib, U, mu):
     _check(pkg, mc["G"].mean(), mc["G"].std_error(), float(mc["docc"].mean()),
            float(mc["docc"].std_error()), mc["sdcz"].mean(), mc["sdcz"].std_error(), E)
     assert mc.analysis["negative_probability"] == 0
+
+
+def test_ed_grid_integral_converges_to_the_continuous_one(pkg):
+    """The trapezoid time integral on the DQMC grid (susceptibility_grid)
+    approaches the exact spectral integral as dtau -> 0 (error ~ dtau^2)."""
+    import ed
+    model = pkg.HubbardModel(pkg.SquareLattice(2), U=-1.0, mu=0.0)
+    E = ed.HubbardED(4, model.l.bonds(), 1.0, -1.0, 0.0, 1.0)
+    F = pkg.pair_form_factor(model.l, "s*")
+    exact = E.susceptibility("pair_field", F)
+    e1 = abs(E.susceptibility_grid("pair_field", F, 0.1) - exact)
+    e2 = abs(E.susceptibility_grid("pair_field", F, 0.05) - exact)
+    assert e2 < e1 / 3.5 and e1 < 0.2

@@ -97,9 +97,13 @@ def test_all_susceptibilities_match_ed_2x2(pkg, lib, U, mu):
     E = ed.HubbardED(4, model.l.bonds(), 1.0, U, mu, 1.0)
     pos = model.l.positions()
     phases = np.cos(pos @ np.array([np.pi, np.pi]))
-    want = {k: E.susceptibility(k, phases) for k in pkg.CORRELATIONS}
+    # ED integrated on the same imaginary-time grid with the same trapezoid
+    # weights (as the reference's ED tests do): only the Trotter error and the
+    # statistics remain
+    want = {k: E.susceptibility_grid(k, phases, DT) for k in pkg.CORRELATIONS}
     for ff in ("s*", "d"):  # extended-s and d-wave pair fields
-        want["pairing_" + ff] = E.susceptibility("pair_field", pkg.pair_form_factor(model.l, ff))
+        want["pairing_" + ff] = E.susceptibility_grid("pair_field",
+                                                      pkg.pair_form_factor(model.l, ff), DT)
     mc = pkg.DQMC(model, beta=1.0, delta_tau=DT, safe_mult=10, seed=45, thermalization=200,
                   sweeps=0, measure_rate=1)
     pkg.run(mc)
@@ -128,8 +132,8 @@ def test_current_susceptibility_matches_ed_chain4(pkg, lib, U, mu):
     E = ed.HubbardED(4, model.l.bonds(), 1.0, U, mu, 1.0)
     J = pkg.current_operator(model.hopping_matrix(), model.l)
     phases = np.cos(np.pi * model.l.positions()[:, 0])
-    want = {k: E.susceptibility(k, phases) for k in pkg.CORRELATIONS}
-    want["current"] = E.susceptibility("current", J)
+    want = {k: E.susceptibility_grid(k, phases, DT) for k in pkg.CORRELATIONS}
+    want["current"] = E.susceptibility_grid("current", J, DT)
     mc = pkg.DQMC(model, beta=1.0, delta_tau=DT, safe_mult=10, seed=46, thermalization=200,
                   sweeps=0, measure_rate=1, structure_factor_q=[np.pi])
     pkg.run(mc)
