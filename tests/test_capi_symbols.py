@@ -111,3 +111,21 @@ def test_ctypes_structs_match_the_header(pkg, tmp_path):
         assert int(got[cname]) == C.sizeof(py), cname
         for fname, _ in py._fields_:
             assert int(got[f"{cname}.{fname}"]) == getattr(py, fname).offset, (cname, fname)
+
+
+def test_complex_matrix_buffers_round_trip(pkg):
+    """The ctypes side's interleaved-complex buffers (Julia's ComplexF64
+    layout, column-major per block) round-trip the (nf, n, n) blocks."""
+    import numpy as np
+    from montecarlo_gb300 import _lib
+    rng = np.random.default_rng(0)
+    G = rng.standard_normal((2, 5, 5)) + 1j * rng.standard_normal((2, 5, 5))
+    buf = _lib.complex_blocks_to_buf(G)
+    assert buf.dtype == np.float64 and buf.size == 2 * 2 * 25
+    # entry (b, i, j) sits at 2 * (b n^2 + j n + i) (+1 for the imaginary part)
+    assert buf[2 * (25 + 3 * 5 + 1)] == G[1, 1, 3].real
+    assert buf[2 * (25 + 3 * 5 + 1) + 1] == G[1, 1, 3].imag
+    back = _lib.buf_to_blocks(buf.view(np.complex128), 2, 5)
+    assert np.array_equal(back, G)
+    cfg = _lib.ChainConfig(16, 1, 10, 5, 0, 1, 0.0, 1, 0.6)
+    assert _lib.is_complex(cfg) and not _lib.is_complex(_lib.ChainConfig(16, 1, 10, 5, 0, 1, 0.5, 1))
