@@ -113,3 +113,27 @@ def test_pair_fields_exact_at_u0(pkg, oracle, kind):
             if kind == "s":
                 C = time_displaced_correlations(*q, l == 0)["pairing"]
                 assert abs(got - C.sum()) < 1e-12
+
+
+def test_form_factors_and_current_operator_structure(pkg):
+    """Form factors: s = I; s* has every nearest-neighbour bond (row sums =
+    coordination); d is +1 along the first lattice vector and -1 along the
+    second (row sums 0 on the square lattice); all symmetric.  The current
+    operator is Hermitian, antisymmetric in the bond direction and zero on
+    a lattice whose +x and -x neighbours coincide (L = 2)."""
+    from montecarlo_gb300.measurements import current_operator, pair_form_factor
+    lat = pkg.SquareLattice(4)
+    assert np.array_equal(pair_form_factor(lat, "s"), np.eye(16))
+    ss, d = pair_form_factor(lat, "s*"), pair_form_factor(lat, "d")
+    assert np.array_equal(ss, ss.T) and np.array_equal(d, d.T)
+    assert np.all(ss.sum(axis=1) == 4) and np.all(d.sum(axis=1) == 0)
+    assert np.all(np.abs(d).sum(axis=1) == 4)
+    with pytest.raises(ValueError):
+        pair_form_factor(lat, "p")
+    T = pkg.HubbardModel(lat, U=1.0).hopping_matrix()
+    J = current_operator(T, lat)
+    assert np.allclose(J, J.conj().T) and np.allclose(J.real, 0)
+    Jy = current_operator(T, lat, direction=[0.0, 1.0])
+    assert np.abs(J).sum() == np.abs(Jy).sum() > 0 and not np.allclose(J, Jy)
+    lat2 = pkg.SquareLattice(2)
+    assert np.allclose(current_operator(pkg.HubbardModel(lat2, U=1.0).hopping_matrix(), lat2), 0)
