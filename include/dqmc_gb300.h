@@ -81,7 +81,7 @@ typedef struct {
     uint64_t seed;         /* key of the chain's Philox4x32-10 stream */
     double alpha_imag;     /* imaginary part of field.alpha; nonzero: complex chain
                               (FP64 only, n_sites <= 128; no device measurements,
-                              global updates, replica exchange or checkerboard) */
+                              global updates or replica exchange) */
 } dqmc_chain_config;
 
 /* Per-chain counters (DQMCAnalysis, statistics.jl:45-51; AcceptanceStatistics,
