@@ -67,6 +67,27 @@ def main():
                         counter=np.array(c.rng_counter(), dtype=np.uint64),
                         accepted=np.array(c.analysis()["accepted"]), G=c.greens())
 
+    # the complex (field / sign(U) mismatch) oracle: 4x4, DensityHirschField at
+    # repulsive U, mu = 0.3, two sweeps from a fixed configuration
+    import complex_oracle as CO
+    cx = complex_trajectory(pkg, CO)
+    np.savez_compressed(os.path.join(HERE, "complex_trajectory.npz"), **cx)
+
+
+def complex_trajectory(pkg, CO):
+    model = pkg.HubbardModel(pkg.SquareLattice(4), U=-4.0, mu=0.3)
+    param = pkg.DQMCParameters.make(beta=1.0, delta_tau=0.1, safe_mult=5)
+    fld = pkg.DensityHirschField(param, model)
+    exps = pkg.hopping_exponentials(model.hopping_matrix(), param.delta_tau)
+    c = CO.ComplexChain(16, 1, param.slices, 5, fld.kind, fld.alpha, exps, 11)
+    rng = np.random.default_rng(11)
+    conf0 = (2 * rng.integers(0, 2, size=(16, param.slices)) - 1).astype(np.int8)
+    c.set_conf(conf0)
+    c.initialize_run()
+    c.sweeps(2)
+    return dict(conf0=conf0, conf=c.conf, counter=np.array(c.ctr, dtype=np.uint64),
+                accepted=np.array(c.accepted), n_imag=np.array(c.n_imag_p), G=c.G)
+
 
 if __name__ == "__main__":
     main()

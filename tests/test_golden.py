@@ -78,3 +78,18 @@ def test_cuda_path_reproduces_trajectory_fixture(pkg, lib):
     assert h.get_rng(0)[1] == int(d["counter"])
     assert st["accepted"] == int(d["accepted"])
     assert maxdiff(h.greens(0), d["G"]) < 1e-10
+
+
+def test_complex_oracle_reproduces_trajectory_fixture(pkg):
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import complex_oracle as CO
+    from make_golden import complex_trajectory
+    d = _load("complex_trajectory.npz")
+    got = complex_trajectory(pkg, CO)
+    assert np.array_equal(got["conf0"], d["conf0"])
+    assert np.array_equal(got["conf"], d["conf"])
+    for k in ("counter", "accepted", "n_imag"):
+        assert int(got[k]) == int(d[k]), k
+    assert int(d["n_imag"]) > 0
+    assert maxdiff(got["G"], d["G"]) < 1e-12
