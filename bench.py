@@ -190,10 +190,13 @@ def cpu_baseline_sample(pkg, workload, budget_s):
                       f"(C restatement of the reference, FMA contraction on)"}
 
 
-def ensemble_c3(pkg, _lib, n_chains, seconds, seed=3):
+def ensemble_c3(pkg, _lib, n_chains, seconds, stream, seed=3):
     """Batched ensemble of uneven attractive chains: L in {6,8,10,12}, U_phys in
     [-8,-2] (U_ref = -U_phys), beta in {4,8,12}, dtau = 0.1; safe_mult
-    autotuned per chain for a propagation error <= 1e-6; plain FP64 and mixed."""
+    autotuned per chain for a propagation error <= 1e-6 (and lowered for any
+    chain that exceeds it over the timed sweeps, after which the timed run is
+    repeated); plain FP64 and mixed, both batched, and the unbatched plain FP64
+    path (each chain alone in its own launches, one after another)."""
     from montecarlo_gb300 import autotune
 
     rng = np.random.default_rng(seed)
@@ -206,52 +209,194 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, seed=3):
         specs.append((model, model.choose_field(), beta, 0.1, 1000 + j))
     out = {"workload": f"{n_chains} attractive chains, L in {{6,8,10,12}} square, U in [-8,-2] "
                        "(physics), beta in {4,8,12}, dtau=0.1, safe_mult autotuned per chain "
-                       "(propagation error <= 1e-6)"}
+                       "(propagation error <= 1e-6), started from thermalised configurations"}
     t = time.perf_counter()
     confs = autotune.thermalize(specs)
     therm_s = time.perf_counter() - t
     out["thermalize_s"] = therm_s
+    chosen = {}
     for name, prec in (("plain_fp64", _lib.PREC_FP64), ("mixed", _lib.PREC_MIXED)):
         t = time.perf_counter()
         # a 200x margin on the probes: the propagation error's tail over long
-        # runs is far above its value on a few probe sweeps (a 50x margin left
-        # 4 of 256 FP64 chains at 1-2e-6 over the timed sweeps)
+        # runs is far above its value on a few probe sweeps
         ks, errs = autotune.tune_safe_mult(specs, tol=1e-6, precision=prec, confs=confs,
                                            safety=0.005)
         tune_s = time.perf_counter() - t
-        ce = []
-        for (model, fcls, beta, dt, s), k in zip(specs, ks):
-            param = pkg.DQMCParameters.make(beta=beta, delta_tau=dt, safe_mult=k)
-            fld = fcls(param, model)
-            ce.append((_lib.ChainConfig(len(model.l), 1, param.slices, k, fld.kind, 1, fld.alpha, s),
-                       pkg.hopping_exponentials(model.hopping_matrix(), dt)))
-        r = pkg.run_ensemble(ce, seconds=seconds, quantum_us=100000, precision=prec)
-        pe = np.array(r["per_chain_propagation_error"])
-        out[name] = {"sweeps_per_s": r["sweeps_per_s"], "max_propagation_error": r["max_propagation_error"],
+        backoffs, attempts = 0, 0
+        while True:
+            attempts += 1
+            ce = []
+            for (model, fcls, beta, dt, s), k in zip(specs, ks):
+                param = pkg.DQMCParameters.make(beta=beta, delta_tau=dt, safe_mult=k)
+                fld = fcls(param, model)
+                ce.append((_lib.ChainConfig(len(model.l), 1, param.slices, k, fld.kind, 1,
+                                            fld.alpha, s),
+                           pkg.hopping_exponentials(model.hopping_matrix(), dt)))
+            r = pkg.run_ensemble(ce, seconds=seconds, quantum_us=100000, precision=prec,
+                                 confs=confs)
+            pe = np.array(r["per_chain_propagation_error"])
+            if not np.any(pe > 1e-6) or attempts == 3:
+                break
+            ks, nb = autotune.back_off(specs, ks, pe, tol=1e-6, precision=prec)
+            backoffs += nb
+            if nb == 0:
+                break
+        chosen[name] = ks
+        out[name] = {"sweeps_per_s": r["sweeps_per_s"],
+                     "max_propagation_error": r["max_propagation_error"],
                      "median_chain_propagation_error": float(np.median(pe)),
                      "chains_over_1e-6": int(np.sum(pe > 1e-6)),
                      "safe_mult_histogram": {str(k): ks.count(k) for k in sorted(set(ks))},
-                     "autotune_s": tune_s, "timed_s": r["wall"], "launches": r["launches"]}
+                     "autotune_s": tune_s, "backoffs": backoffs, "timed_runs": attempts,
+                     "timed_s": r["wall"], "launches": r["launches"]}
+    out["unbatched_plain_fp64"] = unbatched_plain(pkg, _lib, specs, chosen["plain_fp64"], confs,
+                                                  stream)
     out["mixed_vs_plain"] = out["mixed"]["sweeps_per_s"] / out["plain_fp64"]["sweeps_per_s"]
+    out["mixed_vs_unbatched_plain"] = (out["mixed"]["sweeps_per_s"] /
+                                       out["unbatched_plain_fp64"]["sweeps_per_s"])
+    out["plain_vs_unbatched_plain"] = (out["plain_fp64"]["sweeps_per_s"] /
+                                       out["unbatched_plain_fp64"]["sweeps_per_s"])
     return out
 
 
-def served_c5(pkg, _lib, n_requests, wall_s, seed=5):
+def unbatched_plain(pkg, _lib, specs, ks, confs, stream, per_class=2):
+    """The same ensemble advanced without batching: each chain alone in its own
+    sweep launch (the GPU counterpart of update(::LocalSweep) on one
+    simulation at a time), one chain after another, FP64 at its autotuned
+    safe_mult.  Bounded sample: per (L, beta) class the first `per_class`
+    chains each time one sweep (CUDA events on the launch stream, from its
+    thermalised configuration after the stack build); the ensemble's serial
+    time is the class means weighted by the class sizes."""
+    import torch
+
+    classes = {}
+    for j, (model, fcls, beta, dt, s) in enumerate(specs):
+        classes.setdefault((len(model.l), beta), []).append(j)
+    est, sampled, timed = 0.0, 0, 0.0
+    for key in sorted(classes):
+        js = classes[key]
+        ts = []
+        for j in js[:per_class]:
+            model, fcls, beta, dt, s = specs[j]
+            param = pkg.DQMCParameters.make(beta=beta, delta_tau=dt, safe_mult=ks[j])
+            fld = fcls(param, model)
+            h = _lib.Handle([_lib.ChainConfig(len(model.l), 1, param.slices, ks[j], fld.kind, 1,
+                                              fld.alpha, s)], precision=_lib.PREC_FP64)
+            h.set_hopping(0, pkg.hopping_exponentials(model.hopping_matrix(), dt))
+            h.init_random_field(0)
+            h.set_field(0, confs[j])
+            h.set_stream(stream.cuda_stream)
+            h.initialize_run()
+            h.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            h.sweep_async(1)
+            e1.record(stream)
+            h.synchronize()
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+            h.close()
+        sampled += len(ts)
+        timed += sum(ts)
+        est += float(np.mean(ts)) * len(js)
+    return {"sweeps_per_s": len(specs) / est, "serial_s_per_ensemble_sweep": est,
+            "sample": f"{sampled} of {len(specs)} chains (first {per_class} of each (L, beta) "
+                      f"class), one sweep each, one chain per launch, launches back to back",
+            "timed_s": timed}
+
+
+def c4_line(pkg, _lib, stream, n_chains, seed=4):
+    """16x16 repulsive Hubbard U=4 (physics), MagneticHirschField, beta=10,
+    M=100, safe_mult=10: an ensemble of n_chains chains, one timed sweep each
+    on the FP64 and the mixed path after the stack build; the mixed path's
+    max|dG| against FP64 for identical configurations at stabilisation slices
+    (calculate_greens from scratch)."""
+    import torch
+
+    model = pkg.HubbardModel(pkg.SquareLattice(16), U=-4.0)
+    param = pkg.DQMCParameters.make(beta=10.0, delta_tau=0.1, safe_mult=10)
+    fld = pkg.MagneticHirschField(param, model)
+    exps = pkg.hopping_exponentials(model.hopping_matrix(), param.delta_tau)
+    n, M = len(model.l), param.slices
+    nr = len(pkg.generate_chunks(M, param.safe_mult))
+    out = {"workload": "16x16 square repulsive Hubbard U=4 (physics), mu=0, MagneticHirschField, "
+                       f"beta=10, dtau=0.1 (M=100), safe_mult=10, {n_chains} chains, one timed "
+                       "sweep per path after the stack build"}
+    for name, prec in (("fp64", _lib.PREC_FP64), ("mixed", _lib.PREC_MIXED)):
+        h = _lib.Handle([_lib.ChainConfig(n, 2, M, 10, fld.kind, 1, fld.alpha, seed + j)
+                         for j in range(n_chains)], precision=prec)
+        h.set_hopping(-1, exps)
+        h.init_random_field(-1)
+        h.set_stream(stream.cuda_stream)
+        h.initialize_run()
+        h.synchronize()
+        s0 = [h.stats(i) for i in range(n_chains)]
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.sweep_async(1)
+        e1.record(stream)
+        h.synchronize()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        s1 = [h.stats(i) for i in range(n_chains)]
+        acc = sum(b["accepted"] - a["accepted"] for a, b in zip(s0, s1)) / max(
+            1, sum(b["proposals"] - a["proposals"] for a, b in zip(s0, s1)))
+        out[name] = {"sweeps_per_s": n_chains / t, "launch_s": t,
+                     "max_propagation_error": max(x["max_propagation_error"] for x in s1),
+                     "acceptance": acc}
+        if name == "fp64":
+            out[name]["tflops"] = n_chains * sweep_flops(n, 2, M, nr, acc) / t / 1e12
+        h.close()
+    out["mixed_vs_fp64"] = out["mixed"]["sweeps_per_s"] / out["fp64"]["sweeps_per_s"]
+    hs = [_lib.Handle([_lib.ChainConfig(n, 2, M, 10, fld.kind, 1, fld.alpha, seed)], precision=pr)
+          for pr in (_lib.PREC_FP64, _lib.PREC_MIXED)]
+    for hc in hs:
+        hc.set_hopping(-1, exps)
+        hc.init_random_field(0)
+    slices = (0, M // 2, M)
+    dG = max(float(np.max(np.abs(hs[0].calculate_greens(0, sl) - hs[1].calculate_greens(0, sl))))
+             for sl in slices)
+    for hc in hs:
+        hc.close()
+    out["max_dG_mixed_vs_fp64"] = dG
+    out["dG_slices"] = list(slices)
+    return out
+
+
+def served_c5(pkg, _lib, n_requests, wall_s, seed=5, full=False):
     """Served request stream: Poisson arrivals, square or honeycomb, HBM-budget
-    admission, device-resident chains, time-sliced launches.  Bounded sample
-    of the stream's distribution: L in {4,6,8}, beta in {2,4,8}, 20-200 sweeps."""
-    reqs = pkg.poisson_stream(n_requests, rate=20.0, seed=seed, Ls=(4, 6, 8),
-                              betas=(2.0, 4.0, 8.0), sweeps=(20, 200))
-    out = {"workload": f"{n_requests} Poisson requests at 20/s, square|honeycomb, L in {{4,6,8}}, "
-                       "U in [-8,8] (physics), beta in {2,4,8}, 20-200 sweeps, mixed precision, "
-                       "16 GiB HBM budget, 20 ms time slices"}
-    srv = pkg.Server(max_slots=304, budget_bytes=16 << 30, precision=_lib.PREC_MIXED,
+    admission, device-resident chains, time-sliced launches, mixed precision.
+    full=True: the stated distribution (L in {4,6,8,12,16}, honeycomb up to
+    n = 512, beta in {2,4,8,12}, 200-2000 sweeps), bounded by wall time;
+    otherwise a light-load sample (L in {4,6,8}, beta in {2,4,8}, 20-200
+    sweeps)."""
+    if full:
+        kw = dict(Ls=(4, 6, 8, 12, 16), betas=(2.0, 4.0, 8.0, 12.0), sweeps=(200, 2000))
+        desc = "L in {4,6,8,12,16}, beta in {2,4,8,12}, 200-2000 sweeps"
+    else:
+        kw = dict(Ls=(4, 6, 8), betas=(2.0, 4.0, 8.0), sweeps=(20, 200))
+        desc = "L in {4,6,8}, beta in {2,4,8}, 20-200 sweeps"
+    budget = 64 << 30
+    reqs = pkg.poisson_stream(n_requests, rate=20.0, seed=seed, **kw)
+    out = {"workload": f"{n_requests} Poisson requests at 20/s, square|honeycomb, {desc}, "
+                       f"U in [-8,8] (physics), mixed precision, {budget >> 30} GiB HBM budget, "
+                       f"20 ms time slices, stopped after {wall_s:.0f} s"}
+    srv = pkg.Server(max_slots=304, budget_bytes=budget, precision=_lib.PREC_MIXED,
                      quantum_us=20000)
     r = srv.serve(reqs, realtime=True, max_wall=wall_s)
     srv.close()
+    drawn = {}
+    for q in reqs:
+        key = f"{q.lattice}{q.L}"
+        drawn[key] = drawn.get(key, 0) + 1
     out.update({"sweeps_per_s": r["sweeps_per_s"], "p50_block_s": r["p50_block_s"],
-                "p99_block_s": r["p99_block_s"], "finished": len(r["results"]),
-                "unfinished": r["unfinished"], "launches": r["launches"], "wall_s": r["wall"]})
+                "p99_block_s": r["p99_block_s"], "blocks_completed": r["blocks"],
+                "finished": len(r["results"]), "unfinished": r["unfinished"],
+                "launches": r["launches"], "wall_s": r["wall"],
+                "sample": {"lattices": drawn,
+                           "beta": {str(b): sum(q.beta == b for q in reqs)
+                                    for b in sorted({q.beta for q in reqs})},
+                           "sweeps_requested": int(sum(q.sweeps for q in reqs))}})
     return out
 
 
@@ -544,8 +689,21 @@ def main():
                     "ComplexF64 path), same 8x8 lattice, chains and safe_mult; one flavour "
                     "block of the real 2n x 2n representation (n = 128): 4x the plain "
                     "chain's flops per sweep"}
-        extras["batched"] = ensemble_c3(pkg, _lib, 256, args.extra_seconds)
+        extras["batched"] = ensemble_c3(pkg, _lib, 256, args.extra_seconds, stream)
         extras["served"] = served_c5(pkg, _lib, 48, 5 * args.extra_seconds)
+        extras["served_full"] = served_c5(pkg, _lib, 48, 10 * args.extra_seconds, full=True)
+        extras["c4"] = c4_line(pkg, _lib, stream, 2 * nsm)
+        # the headline ratios of the metric, lifted to the top level
+        b = extras["batched"]
+        extras["c3_mixed_sweeps_per_s"] = b["mixed"]["sweeps_per_s"]
+        extras["c3_plain_fp64_sweeps_per_s"] = b["plain_fp64"]["sweeps_per_s"]
+        extras["c3_unbatched_plain_fp64_sweeps_per_s"] = b["unbatched_plain_fp64"]["sweeps_per_s"]
+        extras["mixed_vs_plain"] = b["mixed_vs_plain"]
+        extras["mixed_vs_unbatched_plain"] = b["mixed_vs_unbatched_plain"]
+        extras["c3_chains_over_1e-6"] = {"plain_fp64": b["plain_fp64"]["chains_over_1e-6"],
+                                         "mixed": b["mixed"]["chains_over_1e-6"]}
+        extras["served_p50_p99_block_s"] = [extras["served"]["p50_block_s"],
+                                            extras["served"]["p99_block_s"]]
 
     # DRAM traffic of the chain kernel from the committed ncu capture, scaled
     # by chains (independent per-chain workspaces)

@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define DQMC_GB300_ABI_VERSION 7
+#define DQMC_GB300_ABI_VERSION 8
 
 /* status codes */
 #define DQMC_OK 0
@@ -103,6 +103,12 @@ typedef struct {
     double min_reported_error, mean_reported_error;
     double min_negative_probability, mean_negative_probability, max_negative_probability;
     double min_imaginary_probability, mean_imaginary_probability;
+    /* near ties of the Metropolis test `rand() < p` (local_updates.jl:53):
+     * local proposals whose drawn uniform u lay within 1e-12 of p (a
+     * rounding-level difference in p could have changed the decision), and
+     * the smallest |u - p| of any proposal that drew a uniform (+inf if none) */
+    int64_t near_ties;
+    double min_tie_gap;
 } dqmc_stats;
 
 /* ---- lifecycle ------------------------------------------------------------
@@ -123,6 +129,13 @@ int dqmc_set_stream(dqmc_handle* h, void* cuda_stream);
  * enable = 1; pools always use the CTA kernel).  Same state, workspace and
  * accept/reject decisions; sums in a different order (G agrees to rounding). */
 int dqmc_set_small_chain_kernel(dqmc_handle* h, int enable);
+/* Mixed-precision chains with 96 <= n_sites <= 256 (real, dense hopping) run
+ * their wraps, slice-matrix chains and reconstruction products on the tensor
+ * cores: tcgen05 MMAs on BF16 digit slices of the operands (six per operand,
+ * exact FP32 accumulation per digit level, about 46 correct bits, the class
+ * of the double-float products they replace).  enable = 0 returns them to the
+ * double-float products on the FP32 pipe (default 1).  chain = -1: all. */
+int dqmc_set_tensor_products(dqmc_handle* h, int chain, int enable);
 /* Device bytes one chain needs (stack + Green's function workspace). */
 int64_t dqmc_chain_bytes(const dqmc_chain_config* cfg, int precision);
 
@@ -285,6 +298,21 @@ int dqmc_replica_exchange(dqmc_handle* h, const int32_t* partner, int32_t* accep
 /* accepted / proposed global and replica moves since creation */
 int dqmc_get_global_stats(dqmc_handle* h, int chain, int64_t* accepted, int64_t* proposals);
 
+/* ---- checkpoint state -----------------------------------------------------------
+ * Replaces: the parts of a saved simulation that live with the chain
+ * (flavors/DQMC/FileIO.jl:10-22: DQMCAnalysis, the scheduler, the
+ * measurements' binners; field, RNG and parameters have their own calls):
+ * the acceptance and DQMCAnalysis counters with their MagnitudeStats, the
+ * near-tie counters, the global-update counts and schedule, the measurement
+ * settings and the device measurement accumulators (log binners, occupation
+ * and G sums), as one flat record of dqmc_checkpoint_doubles() doubles.
+ * dqmc_set_checkpoint restores a record taken from a chain of the same
+ * n_sites and n_flavors; the stack is not part of it (rebuild it with
+ * dqmc_initialize_run, as the reference's resume! does). */
+int64_t dqmc_checkpoint_doubles(dqmc_handle* h, int chain); /* < 0: bad chain */
+int dqmc_get_checkpoint(dqmc_handle* h, int chain, double* out);
+int dqmc_set_checkpoint(dqmc_handle* h, int chain, const double* in);
+
 /* ---- pools: batched and served chains -------------------------------------
  * Replaces: a set of independent simulations driven one after another
  * (the reference's mpi_queue / pmap task farms, src/mpi.jl:26-168).  A pool
@@ -326,8 +354,11 @@ int64_t dqmc_pool_free_bytes(dqmc_handle* h);
  * Limit: n_flavors * n_sites^2 <= 8192; larger chains return DQMC_ERR_INVALID.
  * The work is queued on cuda_stream (NULL = legacy default stream); the result
  * is ready when that stream reaches it.  The first call on a device looks up
- * the array's address (make it before any stream capture).  All calls share
- * the array: calls that overlap on the GPU race and must be serialised. */
+ * the array's address (make it before any stream capture) and keeps it for
+ * the life of the process: do not call this entry point on a device after a
+ * cudaDeviceReset (or any release and re-creation of its primary context) in
+ * the same process.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialised. */
 int dqmc_calculate_greens_noalloc(const dqmc_chain_config* cfg, const double* d_hopping,
                                   const int8_t* d_conf, int slice, int safe_mult, double* d_out,
                                   void* cuda_stream);

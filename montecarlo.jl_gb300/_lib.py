@@ -47,7 +47,8 @@ class Stats(C.Structure):
                 ("mean_negative_probability", C.c_double),
                 ("max_negative_probability", C.c_double),
                 ("min_imaginary_probability", C.c_double),
-                ("mean_imaginary_probability", C.c_double)]
+                ("mean_imaginary_probability", C.c_double),
+                ("near_ties", C.c_int64), ("min_tie_gap", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -80,7 +81,8 @@ EXPORTS = [
     "dqmc_global_update", "dqmc_set_global_schedule", "dqmc_replica_exchange",
     "dqmc_get_global_stats", "dqmc_calculate_greens_kl", "dqmc_set_checkerboard",
     "dqmc_set_small_chain_kernel", "dqmc_get_greens_batch", "dqmc_get_fields_batch",
-    "dqmc_set_fields_batch",
+    "dqmc_set_fields_batch", "dqmc_checkpoint_doubles", "dqmc_get_checkpoint",
+    "dqmc_set_checkpoint", "dqmc_set_tensor_products",
 ]
 
 GLOBAL_FLIP = 0
@@ -152,6 +154,11 @@ def load(path: str = LIB_PATH):
     L.dqmc_get_measurements.argtypes = [P, C.c_int, C.POINTER(Observables), C.c_void_p,
                                         C.c_void_p]
     L.dqmc_pool_free_bytes.restype = C.c_int64
+    L.dqmc_set_tensor_products.argtypes = [P, C.c_int, C.c_int]
+    L.dqmc_checkpoint_doubles.argtypes = [P, C.c_int]
+    L.dqmc_checkpoint_doubles.restype = C.c_int64
+    L.dqmc_get_checkpoint.argtypes = [P, C.c_int, dp]
+    L.dqmc_set_checkpoint.argtypes = [P, C.c_int, dp]
     _lib = L
     return L
 
@@ -229,6 +236,11 @@ class Handle:
     def set_small_chain_kernel(self, enable=True):
         """Sweeps of n <= 32 chains one warp per chain (default) or one CTA per chain."""
         check(load().dqmc_set_small_chain_kernel(self.h, int(bool(enable))))
+
+    def set_tensor_products(self, enable=True, chain=-1):
+        """Tensor-core split-precision products for mixed chains of
+        96 <= n <= 256 (default on) or the double-float FP32-pipe products."""
+        check(load().dqmc_set_tensor_products(self.h, int(chain), int(bool(enable))))
 
     def set_hopping(self, chain, exps):
         e = [np.asfortranarray(x, dtype=np.float64) for x in exps]
@@ -403,6 +415,23 @@ class Handle:
         acc = np.zeros(self.n_chains, dtype=np.int32)
         check(load().dqmc_replica_exchange(self.h, p.ctypes.data, acc.ctypes.data))
         return acc.astype(bool)
+
+    def checkpoint(self, chain):
+        """The chain's checkpoint record (counters, schedule, measurement
+        accumulators) as a flat float64 array."""
+        nd = int(load().dqmc_checkpoint_doubles(self.h, chain))
+        if nd < 0:
+            check(load().dqmc_get_checkpoint(self.h, chain, None))
+        buf = np.zeros(nd)
+        check(load().dqmc_get_checkpoint(self.h, chain, dptr(buf)))
+        return buf
+
+    def restore_checkpoint(self, chain, record):
+        buf = np.ascontiguousarray(record, dtype=np.float64)
+        nd = int(load().dqmc_checkpoint_doubles(self.h, chain))
+        if buf.size != nd:
+            raise DQMCError(1, f"checkpoint record of {buf.size} doubles, chain needs {nd}")
+        check(load().dqmc_set_checkpoint(self.h, chain, dptr(buf)))
 
     def global_stats(self, chain):
         a, p = C.c_int64(), C.c_int64()

@@ -14,6 +14,13 @@ from them overestimate the stable interval):
    -- all chains x candidates in one batched launch -- and measure the largest
    propagation error over a few sweeps;
 3. keep the largest candidate under the bound (the smallest one if none is).
+
+Choices are cached per process by (sites, flavours, slices, |U|, mu, field,
+precision, bound), so a server that admits a chain of an already tuned kind
+reuses the choice without probing, and ``back_off`` lowers the interval of
+chains whose propagation error exceeded the bound over a longer run (the
+error's tail over many sweeps lies above its value on a few probe sweeps) and
+records the lowered choice.
 """
 from __future__ import annotations
 
@@ -23,6 +30,39 @@ from . import _lib
 from .model import DQMCParameters, hopping_exponentials
 
 CANDIDATES = (2, 3, 4, 5, 6, 8, 10, 12, 15)
+
+# (n, nf, slices, |U|, mu, field kind, precision, bound) -> safe_mult
+_CACHE = {}
+
+
+def cache_key(model, field_cls, beta, delta_tau, precision, tol):
+    param = DQMCParameters.make(beta=beta, delta_tau=delta_tau)
+    fld = field_cls(param, model)
+    return (len(model.l), fld.unique_flavors, param.slices, round(abs(float(model.U)), 9),
+            round(float(model.mu), 9), fld.kind, int(precision), float(tol))
+
+
+def cached(model, field_cls, beta, delta_tau, precision=_lib.PREC_FP64, tol=1e-6):
+    """The cached safe_mult of this kind of chain, or None."""
+    return _CACHE.get(cache_key(model, field_cls, beta, delta_tau, precision, tol))
+
+
+def lower(k):
+    """The next smaller candidate interval (2 stays 2)."""
+    smaller = [c for c in CANDIDATES if c < k]
+    return max(smaller) if smaller else min(CANDIDATES)
+
+
+def back_off(specs, ks, errors, tol=1e-6, precision=_lib.PREC_FP64):
+    """Lower the interval of every chain whose measured propagation error
+    exceeds `tol`; returns the new choices and the number lowered."""
+    out, n = list(ks), 0
+    for j, (m, f, b, dt, s) in enumerate(specs):
+        if errors[j] > tol and out[j] > min(CANDIDATES):
+            out[j] = lower(out[j])
+            _CACHE[cache_key(m, f, b, dt, precision, tol)] = out[j]
+            n += 1
+    return out, n
 
 
 def _cfg(model, field_cls, beta, delta_tau, k, seed):
@@ -49,12 +89,19 @@ def thermalize(specs, sweeps=6, safe_mult=4, device=0):
 
 
 def tune_safe_mult(specs, tol=1e-6, precision=_lib.PREC_FP64, candidates=CANDIDATES,
-                   confs=None, therm_sweeps=6, probe_sweeps=3, safety=0.1, device=0):
-    """Chosen safe_mult per spec and the propagation error measured with it."""
+                   confs=None, therm_sweeps=6, probe_sweeps=3, safety=0.1, device=0,
+                   use_cache=True):
+    """Chosen safe_mult per spec and the propagation error measured with it
+    (NaN for a choice taken from the cache)."""
+    keys = [cache_key(m, f, b, dt, precision, tol) for m, f, b, dt, s in specs]
+    todo = [j for j, k in enumerate(keys) if not (use_cache and k in _CACHE)]
+    if not todo:
+        return [_CACHE[k] for k in keys], [float("nan")] * len(specs)
     if confs is None:
         confs = thermalize(specs, sweeps=therm_sweeps, device=device)
     cfgs, owner, ks = [], [], []
-    for j, (m, f, b, dt, s) in enumerate(specs):
+    for j in todo:
+        m, f, b, dt, s = specs[j]
         M = DQMCParameters.make(beta=b, delta_tau=dt).slices
         for k in sorted({min(k, M) for k in candidates}):
             cfgs.append(_cfg(m, f, b, dt, k, s))
@@ -69,14 +116,20 @@ def tune_safe_mult(specs, tol=1e-6, precision=_lib.PREC_FP64, candidates=CANDIDA
     h.initialize_run()
     st = h.sweep(probe_sweeps)
     h.close()
-    errs = [dict() for _ in specs]
+    errs = {j: dict() for j in todo}
     for r, j in enumerate(owner):
         errs[j][ks[r]] = st[r]["max_propagation_error"]
     chosen, err_at = [], []
     bound = safety * tol
-    for e in errs:
+    for j, key in enumerate(keys):
+        if j not in errs:
+            chosen.append(_CACHE[key])
+            err_at.append(float("nan"))
+            continue
+        e = errs[j]
         ok = [k for k, v in e.items() if v <= bound]
         k = max(ok) if ok else min(e)
+        _CACHE[key] = k
         chosen.append(k)
         err_at.append(e[k])
     return chosen, err_at

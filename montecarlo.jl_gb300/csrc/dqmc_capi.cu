@@ -279,6 +279,8 @@ void fill_descriptor(DqmcChain& d, const dqmc_chain_config& c, char* b, const La
         ms[1] = INFINITY;
         ms[2] = 0.0;
     }
+    d.min_tie_gap = INFINITY;
+    d.tc_enable = 0;
     d.key = c.seed; d.ctr = 0;
     d.current_slice = 0; d.current_range = 1; d.direction = 1;
     d.active = 1;
@@ -403,6 +405,17 @@ int dqmc_set_small_chain_kernel(dqmc_handle* h, int enable) {
     if (!h) return fail(DQMC_ERR_INVALID, "null handle");
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     h->small_kernel = enable != 0;
+    return DQMC_OK;
+}
+
+int dqmc_set_tensor_products(dqmc_handle* h, int chain, int enable) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    int lo = chain, hi = chain + 1;
+    if (chain == -1) { lo = 0; hi = (int)h->cfg.size(); }
+    else if (int st = check_chain(h, chain)) return st;
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    for (int i = lo; i < hi; ++i) h->host[i].tc_enable = enable ? 1 : 0;
+    h->host_dirty = true;
     return DQMC_OK;
 }
 
@@ -571,6 +584,8 @@ static void fill_stats(const DqmcChain& d, dqmc_stats* s) {
     s->current_range = d.current_range;
     s->direction = d.direction;
     s->status = d.status;
+    s->near_ties = d.n_near_tie;
+    s->min_tie_gap = d.min_tie_gap;
 }
 
 static int check_scheduled(dqmc_handle* h);
@@ -1183,6 +1198,92 @@ int dqmc_get_global_stats(dqmc_handle* h, int chain, int64_t* accepted, int64_t*
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     if (accepted) *accepted = h->host[chain].g_accepted;
     if (proposals) *proposals = h->host[chain].g_proposals;
+    return DQMC_OK;
+}
+
+/* ---- checkpoint state --------------------------------------------------------- */
+
+// Counters of a chain's checkpoint record, in order (integers stored as doubles,
+// exact below 2^53): the DQMCAnalysis / acceptance counters, the MagnitudeStats
+// accumulators, global-update and scheduler counts, the measurement settings.
+#define DQMC_CKPT_HEADER 28
+
+static void ckpt_pack(const DqmcChain& d, double* o) {
+    o[0] = (double)d.accepted;     o[1] = (double)d.proposals;
+    o[2] = (double)d.n_prop_err;   o[3] = (double)d.n_neg_p;
+    o[4] = d.prop_err_max;         o[5] = d.prop_err_reported;
+    o[6] = (double)d.n_imag_p;     o[7] = d.max_imag_p;
+    for (int q = 0; q < 3; ++q) {
+        o[8 + q] = d.ms_prop[q];
+        o[11 + q] = d.ms_neg[q];
+        o[14 + q] = d.ms_imag[q];
+    }
+    o[17] = (double)d.n_near_tie;  o[18] = d.min_tie_gap;
+    o[19] = (double)d.g_accepted;  o[20] = (double)d.g_proposals;
+    o[21] = (double)d.sched_calls; o[22] = (double)d.global_kind;
+    o[23] = (double)d.sweep;       o[24] = (double)d.meas_enable;
+    o[25] = (double)d.meas_rate;   o[26] = (double)d.meas_greens;
+    o[27] = d.meas_U;
+}
+
+static void ckpt_unpack(DqmcChain& d, const double* o) {
+    d.accepted = (long long)o[0];     d.proposals = (long long)o[1];
+    d.n_prop_err = (long long)o[2];   d.n_neg_p = (long long)o[3];
+    d.prop_err_max = o[4];            d.prop_err_reported = o[5];
+    d.n_imag_p = (long long)o[6];     d.max_imag_p = o[7];
+    for (int q = 0; q < 3; ++q) {
+        d.ms_prop[q] = o[8 + q];
+        d.ms_neg[q] = o[11 + q];
+        d.ms_imag[q] = o[14 + q];
+    }
+    d.n_near_tie = (long long)o[17];  d.min_tie_gap = o[18];
+    d.g_accepted = (long long)o[19];  d.g_proposals = (long long)o[20];
+    d.sched_calls = (long long)o[21]; d.global_kind = (int)o[22];
+    d.sweep = (long long)o[23];       d.meas_enable = (int)o[24];
+    d.meas_rate = (int)o[25];         d.meas_greens = (int)o[26];
+    d.meas_U = o[27];
+}
+
+int64_t dqmc_checkpoint_doubles(dqmc_handle* h, int chain) {
+    if (check_chain(h, chain)) return -1;
+    const DqmcChain& d = h->host[chain];
+    return (int64_t)(DQMC_CKPT_HEADER + DQMC_MEAS_DOUBLES(d.n, d.nf));
+}
+
+int dqmc_get_checkpoint(dqmc_handle* h, int chain, double* out) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!out) return fail(DQMC_ERR_INVALID, "dqmc_get_checkpoint: null out");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    const DqmcChain& d = h->host[chain];
+    ckpt_pack(d, out);
+    CUDA_TRY(cudaMemcpyAsync(out + DQMC_CKPT_HEADER, d.meas,
+                             DQMC_MEAS_DOUBLES(d.n, d.nf) * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream),
+             "download measurement accumulators");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    return DQMC_OK;
+}
+
+int dqmc_set_checkpoint(dqmc_handle* h, int chain, const double* in) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!in) return fail(DQMC_ERR_INVALID, "dqmc_set_checkpoint: null in");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    const int gk = (int)in[22], rate = (int)in[25];
+    if (!(gk == -1 || gk == DQMC_GLOBAL_FLIP || gk == DQMC_GLOBAL_SHUFFLE) || rate < 1 ||
+        !(in[0] >= 0 && in[1] >= in[0]))
+        return fail(DQMC_ERR_INVALID, "dqmc_set_checkpoint: not a checkpoint record");
+    DqmcChain& d = h->host[chain];
+    if (gk >= 0 && d.cplx)
+        return fail(DQMC_ERR_INVALID, "dqmc_set_checkpoint: global updates on a complex chain");
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    CUDA_TRY(cudaMemcpyAsync(d.meas, in + DQMC_CKPT_HEADER,
+                             DQMC_MEAS_DOUBLES(d.n, d.nf) * sizeof(double),
+                             cudaMemcpyHostToDevice, h->stream),
+             "upload measurement accumulators");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    ckpt_unpack(d, in);
+    h->host_dirty = true;
     return DQMC_OK;
 }
 

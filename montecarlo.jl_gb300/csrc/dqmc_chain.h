@@ -111,7 +111,27 @@ struct DqmcChain {
     // (> 1e-7), negative probabilities and imaginary probabilities: max, min
     // and sum of log10 |value| each (counts: n_prop_err, n_neg_p, n_imag_p)
     double ms_prop[3], ms_neg[3], ms_imag[3];
+    // near ties of the Metropolis test `rand() < p` (local_updates.jl:53):
+    // local proposals that drew a uniform u (p <= 1) with |u - p| < 1e-12,
+    // where a rounding-level difference in p could change the decision, and
+    // the smallest |u - p| of any drawn proposal (+inf before the first)
+    long long n_near_tie;
+    double min_tie_gap;
+    // mixed chains with 96 <= n <= 256: run the products on the tensor cores
+    // (tcgen05 split-precision products) instead of the FP32 pipe (1 = on)
+    int tc_enable, pad4;
 };
+// the near-tie window of DqmcChain::n_near_tie
+#define DQMC_NEAR_TIE 1e-12
+#ifdef __CUDACC__
+// record the gap between a drawn uniform u and the probability p it is tested
+// against (the decision itself is `u < p`)
+__device__ __forceinline__ void note_tie(DqmcChain& c, double u, double p) {
+    const double gap = fabs(u - p);
+    if (gap < DQMC_NEAR_TIE) c.n_near_tie += 1;
+    if (gap < c.min_tie_gap) c.min_tie_gap = gap;
+}
+#endif
 #define DQMC_MS_PUSH(ms, v)                               \
     do {                                                  \
         const double l_ = log10(fabs(v));                 \

@@ -7,18 +7,12 @@
 #include <stdint.h>
 
 #include "dqmc_device.cuh"
+#include "dqmc_tc.cuh"
 
 namespace dqmc {
 namespace {  // internal linkage: each translation unit gets its own copy
 
 struct Smem {
-    union {                      // never live at the same time
-        double tiles[2 * 16 * 64];  // mm() / mm_dfx() staging
-        struct {
-            double col[2][DQMC_NMAX];  // rank-1: (I - G)[:, i] per block
-            double row[2][DQMC_NMAX];  // rank-1: (Delta/R) G[i, :] per block
-        } r1;
-    };
     double sv[DQMC_NMAX];        // column norms / small vectors
     double ev[2 * DQMC_NMAX];    // interaction exponential of the current slice
     double sxd[4];
@@ -28,12 +22,39 @@ struct Smem {
     double* Gglob;               // the chain's G in global memory
     int gres;                    // G currently lives in `arena`
     int arena_cap;               // doubles of `arena` this launch allocated
+    int tc_on;                   // this chain's products run on the tensor cores (mm_tc)
+    int gdfg;                    // G stays in global memory but holds float pairs (n > 64)
+    TcState tc;                  // TMEM base and mbarriers of mm_tc (16-byte aligned)
+    // `tiles` and `arena` are adjacent and 16-byte aligned: mm_tc stages its
+    // operand slices in both (chains with n > 64 use neither otherwise)
+    union {                      // never live at the same time
+        double tiles[2 * 16 * 64];  // mm() / mm_dfx() staging
+        struct {
+            double col[2][DQMC_NMAX];  // rank-1: (I - G)[:, i] per block
+            double row[2][DQMC_NMAX];  // rank-1: (Delta/R) G[i, :] per block
+        } r1;
+    };
     // last member: a launch allocates only the 2 n (n + 1) doubles its chains
     // use (max over chains with n <= 64).  Shared-memory QR of one or two
     // blocks when n <= 64; between stabilisations of a sweep it holds G
     // (G-resident mode).
     double arena[2 * 64 * 65];
 };
+static_assert(sizeof(double) * 2 * 16 * 64 + sizeof(double) * 2 * 64 * 65 >= DQMC_TC_SMEM,
+              "mm_tc staging must fit tiles + arena");
+
+// Products of a chain run on the tensor cores (mm_tc) when it is a real,
+// mixed-precision chain with dense hopping and DQMC_TC_NMIN <= n <= 256, its
+// tensor products are enabled, and the launch has the whole arena (then
+// `tiles` + `arena` hold mm_tc's staging).
+#define DQMC_TC_NMIN 96
+__device__ __forceinline__ bool tc_eligible(const DqmcChain& c, int arena_cap) {
+    return c.prec == DQMC_PREC_MIXED_ID && !c.cplx && !c.cb && c.tc_enable && c.n >= DQMC_TC_NMIN &&
+           c.n <= DQMC_TC_NMAX && arena_cap >= 2 * 64 * 65;
+}
+__device__ __forceinline__ unsigned char* tc_stage(Smem* s) {
+    return reinterpret_cast<unsigned char*>(s->tiles);
+}
 
 struct Ctx {
     Smem* s;
@@ -47,24 +68,40 @@ __device__ __forceinline__ double* blk(double* p, const Ctx& x, int b) { return 
 // G-resident mode (n <= 64): during sweeps G stays in shared memory for the
 // rank-1 updates and wraps, and moves to global memory while a stabilisation
 // needs the arena for its QR factorisations.
-__device__ __forceinline__ bool g_resident_possible(const Ctx& x) {
-    return x.n <= 64 && (size_t)x.nf * x.nn <= (size_t)x.s->arena_cap;
-}
 // On a mixed-precision chain with n >= 32 the resident G is double-float
 // (float2 per entry, same bytes): the rank-1 updates and the wraps then run
 // entirely on the FP32 pipe; it is rounded back to FP64 whenever it leaves
 // shared memory.  (At n = 16 the split arithmetic costs more than it saves.)
+// A mixed chain with n > 64 keeps G in its global buffer but, between
+// stabilisations, as float pairs in place (gdfg): the delayed rank-k updates
+// and the wraps then issue no FP64 instruction either.
 __device__ __forceinline__ bool df_mode(const Ctx& x) {
     return x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 32 && !x.c->cb && !x.c->cplx;
 }
-__device__ __forceinline__ bool df_resident(const Ctx& x) { return df_mode(x) && x.s->gres; }
+#ifndef DQMC_DF_GLOBAL
+#define DQMC_DF_GLOBAL 0
+#endif
+__device__ __forceinline__ bool df_global_possible(const Ctx& x) {
+    return DQMC_DF_GLOBAL && df_mode(x) && x.n > 64;
+}
+__device__ __forceinline__ bool g_resident_possible(const Ctx& x) {
+    return (x.n <= 64 && (size_t)x.nf * x.nn <= (size_t)x.s->arena_cap) || df_global_possible(x);
+}
+__device__ __forceinline__ bool df_resident(const Ctx& x) {
+    return df_mode(x) && (x.s->gres || x.s->gdfg);
+}
 __device__ __forceinline__ float2* arena_df(const Ctx& x) {
     return reinterpret_cast<float2*>(x.s->arena);
 }
-// the resident G (either form) as FP64 into dst
+// the double-float G wherever it lives (shared arena or its global buffer)
+__device__ __forceinline__ float2* gdf_ptr(const Ctx& x) {
+    return reinterpret_cast<float2*>(x.c->G);
+}
+// the resident G (either form) as FP64 into dst (dst may be G's own global
+// buffer: element e is read before it is written, by the same thread)
 __device__ void g_resident_to(const Ctx& x, double* dst) {
     if (df_mode(x)) {
-        const float2* a = arena_df(x);
+        const float2* a = gdf_ptr(x);
         for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) dst[e] = df_to_d(a[e]);
     } else {
         for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) dst[e] = x.s->arena[e];
@@ -72,6 +109,14 @@ __device__ void g_resident_to(const Ctx& x, double* dst) {
 }
 __device__ void g_to_arena(const Ctx& x) {
     __syncthreads();
+    if (x.n > 64) {  // in place, float pairs in the global buffer
+        float2* a = reinterpret_cast<float2*>(x.s->Gglob);
+        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) a[e] = d_to_df(x.s->Gglob[e]);
+        __syncthreads();
+        if (threadIdx.x == 0) x.s->gdfg = 1;
+        __syncthreads();
+        return;
+    }
     if (df_mode(x)) {
         float2* a = arena_df(x);
         for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) a[e] = d_to_df(x.s->Gglob[e]);
@@ -86,7 +131,7 @@ __device__ void g_to_global(const Ctx& x) {
     __syncthreads();
     g_resident_to(x, x.s->Gglob);
     __syncthreads();
-    if (threadIdx.x == 0) { x.c->G = x.s->Gglob; x.s->gres = 0; }
+    if (threadIdx.x == 0) { x.c->G = x.s->Gglob; x.s->gres = 0; x.s->gdfg = 0; }
     __syncthreads();
 }
 
@@ -125,6 +170,18 @@ __device__ __forceinline__ void phase_stop(const Ctx& x, int phase, long long t0
 // untransposed (identical sums; the untransposed staging needs fewer
 // registers).  Below n = 48 the mixed path keeps the FP64 product: the
 // matrices are too small for the split arithmetic to pay.
+// A failed tensor-core product (an mbarrier wait that timed out) sets the
+// chain's status to DQMC_STATUS_TC_TIMEOUT and turns the tensor path off for
+// the rest of the launch.
+#define DQMC_STATUS_TC_TIMEOUT 7
+__device__ __forceinline__ void tc_failed(const Ctx& x) {
+    if (threadIdx.x == 0) {
+        x.c->status = DQMC_STATUS_TC_TIMEOUT;
+        x.s->tc_on = 0;
+    }
+    __syncthreads();
+}
+
 template <bool TA, bool TB>
 __device__ __forceinline__ void smm(const Ctx& x, bool wrap, double* C, const double* A,
                                     const double* B) {
@@ -132,6 +189,15 @@ __device__ __forceinline__ void smm(const Ctx& x, bool wrap, double* C, const do
     const DqmcChain& c = *x.c;
     if (c.prec == DQMC_PREC_MIXED_ID && x.n >= 48) {
         // the transposed operand is eT2 or eT2inv: take its float-pair split
+        if (x.s->tc_on) {
+            const bool ok = TA ? mm_tc<true, false, false>(x.n, C, A == c.eT2 ? c.eT2df : c.eT2invdf,
+                                                          B, tc_stage(x.s), &x.s->tc)
+                               : mm_tc<false, true, false>(x.n, C, A,
+                                                           B == c.eT2 ? c.eT2df : c.eT2invdf,
+                                                           tc_stage(x.s), &x.s->tc);
+            if (ok) return;
+            tc_failed(x);
+        }
         if (TA)
             mm_dfx<true, false, false>(x.n, C, A == c.eT2 ? c.eT2df : c.eT2invdf, B, x.s->tiles);
         else
@@ -292,6 +358,16 @@ __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* 
     }
 }
 
+// C = A B for double-float operands and result: tensor cores when the chain
+// has them, else the FP32-pipe product
+__device__ __forceinline__ void mm_df3(const Ctx& x, float2* C, const float2* A, const float2* B) {
+    if (x.s->tc_on) {
+        if (mm_tc<true, true, true>(x.n, C, A, B, tc_stage(x.s), &x.s->tc)) return;
+        tc_failed(x);
+    }
+    mm_dfx<true, true, true>(x.n, C, A, B, x.s->tiles);
+}
+
 // wrap_greens! of the resident double-float G of a mixed chain: the same
 // four slice-matrix steps with double-float diagonals (exact float pairs of
 // the interaction exponentials) and double-float products; tmp1 holds the
@@ -299,9 +375,9 @@ __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* 
 __device__ __noinline__ void wrap_greens_df(const Ctx& x, int curr_slice, int direction) {
     const DqmcChain& c = *x.c;
     const int n = x.n;
-    float2* G = arena_df(x);
+    float2* G = gdf_ptr(x);
     float2* T = reinterpret_cast<float2*>(c.tmp1);
-    float2* ev = reinterpret_cast<float2*>(x.s->ev + 256);  // beyond the nf*n FP64 entries
+    float2* ev = reinterpret_cast<float2*>(x.s->ev + DQMC_NMAX);  // beyond the nf*n FP64 entries
     const int slice = direction == -1 ? curr_slice - 1 : curr_slice;
     for (int half = 0; half < 2; ++half) {
         // direction +1: B(l) G B(l)^-1 = eT2 (eV (G eV^-1)) eT2inv, as
@@ -320,9 +396,9 @@ __device__ __noinline__ void wrap_greens_df(const Ctx& x, int curr_slice, int di
                 if (direction == 1) {  // G <- eT2 * (eV * G)
                     dleft_df(n, t, d, g);
                     __syncthreads();
-                    mm_dfx<true, true, true>(n, g, hop, t, x.s->tiles);
+                    mm_df3(x, g, hop, t);
                 } else {                 // G <- eV^-1 * (eT2inv * G)
-                    mm_dfx<true, true, true>(n, t, hop, g, x.s->tiles);
+                    mm_df3(x, t, hop, g);
                     __syncthreads();
                     dleft_df(n, g, d, t);
                 }
@@ -330,9 +406,9 @@ __device__ __noinline__ void wrap_greens_df(const Ctx& x, int curr_slice, int di
                 if (direction == 1) {  // G <- (G * eV^-1) * eT2inv
                     dright_df(n, t, g, d);
                     __syncthreads();
-                    mm_dfx<true, true, true>(n, g, t, hop, x.s->tiles);
+                    mm_df3(x, g, t, hop);
                 } else {                 // G <- (G * eT2) * eV
-                    mm_dfx<true, true, true>(n, t, g, hop, x.s->tiles);
+                    mm_df3(x, t, g, hop);
                     __syncthreads();
                     dright_df(n, g, t, d);
                 }
@@ -470,10 +546,15 @@ __device__ __noinline__ void add_slice_sequence_right(const Ctx& x, int idx) {
 // everything of a checkerboard chain.
 template <bool TA, bool TB>
 __device__ __forceinline__ void rmm(const Ctx& x, double* C, const double* A, const double* B) {
-    if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48 && !x.c->cplx && !x.c->cb)
+    if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48 && !x.c->cplx && !x.c->cb) {
+        if (x.s->tc_on) {
+            if (mm_tc<false, false, false, TA, TB>(x.n, C, A, B, tc_stage(x.s), &x.s->tc)) return;
+            tc_failed(x);
+        }
         mm_dfx<false, false, false, TA, TB>(x.n, C, A, B, x.s->tiles);
-    else
+    } else {
         mm<TA, TB>(x.n, C, A, B, x.s->tiles);
+    }
 }
 
 __device__ __noinline__ void calculate_greens_pair(const Ctx& x, double* Gout, bool finish) {
@@ -675,7 +756,7 @@ __device__ __noinline__ void propagate(const Ctx& x) {
                 __syncthreads();
             } else if (cs - 1 == c.rlast[cr - 1]) {
                 const int idx = cr;
-                const bool was_res = x.s->gres;
+                const bool was_res = x.s->gres || x.s->gdfg;
                 if (was_res) g_to_global(x);
                 copy(x.nf * (int)x.nn, c.Ur, ustk(x, idx + 1));
                 copy(x.nf * x.n, c.Dr, dstk(x, idx + 1));
@@ -723,7 +804,7 @@ __device__ __noinline__ void propagate(const Ctx& x) {
                 }
             } else if (cs + 1 == c.rfirst[cr - 1]) {
                 const int idx = cr;
-                const bool was_res = x.s->gres;
+                const bool was_res = x.s->gres || x.s->gdfg;
                 if (was_res) g_to_global(x);
                 copy(x.nf * (int)x.nn, c.Ul, ustk(x, idx));
                 copy(x.nf * x.n, c.Dl, dstk(x, idx));
@@ -899,7 +980,9 @@ __device__ __noinline__ long long sweep_spatial_cplx(const Ctx& x) {
                 } else {
                     const uint64_t w = dqmc_philox_word(c.key, c.ctr);
                     c.ctr += 1;
-                    accept = dqmc_word_to_uniform(w) < p;
+                    const double u = dqmc_word_to_uniform(w);
+                    accept = u < p;
+                    note_tie(c, u, p);
                 }
                 c.proposals += 1;
                 if (accept) {
@@ -1043,7 +1126,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     // values (the diagonal and the update vectors are formed in FP64), the
     // n x n rank-1 update runs in double-float on the FP32 pipe
     const bool dfg = df_resident(x);
-    const float2* gdf = arena_df(x);
+    const float2* gdf = gdf_ptr(x);
     for (int e = tid; e < nf * n; e += DQMC_NT) {
         const int b = e / n, k = e % n;
         const size_t at = (size_t)b * x.nn + (size_t)k * n + k;
@@ -1100,7 +1183,9 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 } else {
                     const uint64_t w = dqmc_philox_word(c.key, c.ctr);
                     c.ctr += 1;
-                    accept = dqmc_word_to_uniform(w) < p;
+                    const double u = dqmc_word_to_uniform(w);
+                    accept = u < p;
+                    note_tie(c, u, p);
                 }
                 c.proposals += 1;
                 if (accept) {
@@ -1149,7 +1234,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
             const double rw = x.s->sxd[b] * gjk;
             x.s->r1.col[b][k] = ig;
             x.s->r1.row[b][k] = rw;
-            if (dfg) {  // float pairs of -col and row behind the FP64 vectors (n <= 64)
+            if (dfg && !delayed) {  // float pairs of -col and row behind the FP64 vectors
                 reinterpret_cast<float2*>(x.s->r1.col[b] + 256)[k] = d_to_df(-ig);
                 reinterpret_cast<float2*>(x.s->r1.row[b] + 256)[k] = d_to_df(rw);
             }
@@ -1471,9 +1556,10 @@ __device__ __noinline__ void measure(const Ctx& x) {
     const size_t nn = x.nn;
     const double* src = c.G;
     if (df_resident(x)) {  // FP64 snapshot of the double-float resident G
-        g_resident_to(x, x.s->Gglob);
+        double* snap = x.s->gdfg ? c.Gtmp : x.s->Gglob;
+        g_resident_to(x, snap);
         __syncthreads();
-        src = x.s->Gglob;
+        src = snap;
     }
     greens_physical(x, src, c.out);
     const double* g1 = c.out;

@@ -46,6 +46,24 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
         if (threadIdx.x == 0) chains[blockIdx.x].status = 1;
         return;
     }
+    // tensor-core products: one warp allocates the accumulators' TMEM columns
+    // (two CTAs per SM at most, 2 x 256 of the SM's 512 columns) and thread 0
+    // sets up the mbarriers; released after the operation
+    const bool use_tc = tc_eligible(s->c, arena_cap);
+    if (use_tc) {
+        if ((threadIdx.x >> 5) == 0) tc_alloc(&s->tc.tmem, DQMC_TC_COLS);
+        if (threadIdx.x == 0) {
+            mbar_init(&s->tc.bar[0], 1);
+            mbar_init(&s->tc.bar[1], 1);
+            s->tc.phase[0] = s->tc.phase[1] = 0;
+            s->tc.status = 0;
+            asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        }
+        tc_fence_before();
+    }
+    if (threadIdx.x == 0) s->tc_on = use_tc ? 1 : 0;
+    __syncthreads();
+    if (use_tc) tc_fence_after();
     switch (op) {
     case DQMC_OP_RUN: {
         // time slice of a pool: build the stack of a newly admitted chain,
@@ -145,6 +163,13 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
         break;
     }
     __syncthreads();
+    if (use_tc) {
+        // every product waited for its MMAs; release the columns
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if ((threadIdx.x >> 5) == 0) tc_dealloc(s->tc.tmem, DQMC_TC_COLS);
+    }
     // write back the mutable state
     if (threadIdx.x == 0) {
         DqmcChain& g = chains[blockIdx.x];
@@ -156,6 +181,8 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
         g.prop_err_reported = s->c.prop_err_reported;
         g.n_prop_err = s->c.n_prop_err;
         g.n_neg_p = s->c.n_neg_p;
+        g.n_near_tie = s->c.n_near_tie;
+        g.min_tie_gap = s->c.min_tie_gap;
         g.n_imag_p = s->c.n_imag_p;
         g.max_imag_p = s->c.max_imag_p;
         for (int q = 0; q < 3; ++q) {

@@ -611,7 +611,9 @@ __device__ __noinline__ void sweep_spatial(const W& x) {
             } else {
                 const uint64_t w = dqmc_philox_word(c.key, c.ctr);
                 c.ctr += 1;
-                accept = dqmc_word_to_uniform(w) < p;
+                const double u = dqmc_word_to_uniform(w);
+                accept = u < p;
+                note_tie(c, u, p);
             }
             c.proposals += 1;
             if (accept) {
@@ -683,18 +685,38 @@ __device__ __noinline__ void sweep_spatial_hirsch(const W& x) {
         const unsigned need = __ballot_sync(FULL, valid && !(p > 1.0));
         const unsigned below = (1u << lane) - 1u;  // lanes before this one
         bool acc = false;
+        double gap = INFINITY;  // |u - p| of this lane's drawn uniform
         if (valid) {
             if (p > 1.0) {
                 acc = true;
             } else {
                 const uint64_t w = dqmc_philox_word(c.key, c.ctr + (uint64_t)__popc(need & below));
-                acc = dqmc_word_to_uniform(w) < p;
+                const double u = dqmc_word_to_uniform(w);
+                acc = u < p;
+                gap = fabs(u - p);
             }
         }
         const unsigned am = __ballot_sync(FULL, acc);
         const unsigned vm = __ballot_sync(FULL, valid);
         const int last = am ? __ffs(am) - 1 : 31 - __clz(vm);  // last proposal of this round
         const unsigned done = last == 31 ? FULL : ((2u << last) - 1u);
+        {
+            // near ties among the proposals made; the smallest gap by the bit
+            // patterns of the non-negative gaps (integer pipe)
+            const unsigned ties = __ballot_sync(FULL, gap < DQMC_NEAR_TIE) & done;
+            long long gb = ((done >> lane) & 1u) ? __double_as_longlong(gap)
+                                                 : __double_as_longlong(INFINITY);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const long long og = __shfl_xor_sync(FULL, gb, o);
+                gb = og < gb ? og : gb;
+            }
+            if (lane == 0) {
+                c.n_near_tie += __popc(ties);
+                const double gmin = __longlong_as_double(gb);
+                if (gmin < c.min_tie_gap) c.min_tie_gap = gmin;
+            }
+        }
         // negative probabilities of the proposals made, in order
         unsigned neg = __ballot_sync(FULL, valid && p < 0.0) & done;
         while (neg) {
@@ -803,6 +825,8 @@ __global__ void __launch_bounds__(32 * WPC, MINB)
         g.prop_err_reported = c->prop_err_reported;
         g.n_prop_err = c->n_prop_err;
         g.n_neg_p = c->n_neg_p;
+        g.n_near_tie = c->n_near_tie;
+        g.min_tie_gap = c->min_tie_gap;
         g.accepted = c->accepted;
         g.proposals = c->proposals;
         for (int p = 0; p < 8; ++p) g.timers[p] = c->timers[p];

@@ -41,13 +41,17 @@ class DQMC:
     equal-time observables), ``structure_factor_q`` (the q of S^z(q),
     default (pi, pi, ...)) and ``global_update`` (None, "flip" or "shuffle":
     the scheduler SimpleScheduler(LocalSweep(), GlobalFlip() / GlobalShuffle()),
-    scheduler.jl:258-289).
+    scheduler.jl:258-289).  ``recorder`` (default: a ``ConfigRecorder`` with
+    ``recording_rate``, which defaults to ``measure_rate``; ``False``: record
+    nothing, the reference's Discarder) receives the field configuration after
+    every recorded sweep past thermalisation (DQMC.jl:41, 216).
     """
 
     def __init__(self, model, *, seed: int = -1, field=None, measurements=None,
                  thermalization_measurements=None, last_sweep: int = 0, measure_rate: int = 10,
                  precision: str = "fp64", device: int = 0, device_measurements: bool = True,
-                 structure_factor_q=None, global_update=None, **kwargs):
+                 structure_factor_q=None, global_update=None, recorder=None,
+                 recording_rate: int = None, **kwargs):
         self.model = model
         self.parameters = DQMCParameters.make(measure_rate=measure_rate, **kwargs)
         fcls = field if field is not None else model.choose_field()
@@ -91,6 +95,11 @@ class DQMC:
         if global_update not in (None, "flip", "shuffle"):
             raise ValueError("global_update must be None, 'flip' or 'shuffle'")
         self.global_update = global_update
+        if recorder is None:
+            recorder = ConfigRecorder(recording_rate or measure_rate)
+        # an empty recorder is falsy (len 0): test for the Discarder spelling
+        self.recorder = None if recorder is False else recorder
+        self._restore_record = None
 
     # -- stack --------------------------------------------------------------
     def init(self):
@@ -100,6 +109,11 @@ class DQMC:
         if self.global_update is not None:
             self.handle.set_global_schedule(
                 _lib.GLOBAL_FLIP if self.global_update == "flip" else _lib.GLOBAL_SHUFFLE, 0)
+        if self._restore_record is not None:
+            # a resumed chain: its counters, scheduler position and measurement
+            # accumulators as saved (the rebuild above is not a sweep)
+            self.handle.restore_checkpoint(0, self._restore_record)
+            self._restore_record = None
         self.initialized = True
 
     @property
@@ -187,21 +201,28 @@ class DQMC:
         st = self.handle.stats(0)
         acc0, prop0 = st["accepted"], st["proposals"]
         while self.last_sweep < total:
-            # advance in device launches up to the next measurement point
-            # (measurements read G after every measure_rate-th sweep)
+            # advance in device launches up to the next measurement or
+            # recording point (both read the chain after that sweep)
             if self.last_sweep < th:
                 k = th - self.last_sweep
-            elif self.measurements:
-                k = p.measure_rate - (self.last_sweep % p.measure_rate)
             else:
-                k = total - self.last_sweep
+                stops = [total - self.last_sweep]
+                if self.measurements:
+                    stops.append(p.measure_rate - (self.last_sweep % p.measure_rate))
+                if self.recorder is not None:
+                    stops.append(self.recorder.rate - (self.last_sweep % self.recorder.rate))
+                k = min(stops)
             k = max(1, min(k, total - self.last_sweep, self.max_sweeps_per_launch))
             if self.device_measurements:
                 self._device_measure(self.last_sweep >= th)
             self.handle.sweep(k)
             self.last_sweep += k
-            if self.last_sweep > th and self.last_sweep % p.measure_rate == 0:
-                self._measure()
+            if self.last_sweep > th:
+                if self.recorder is not None:
+                    self.recorder.push(self.handle.get_field(0), self.last_sweep,
+                                       ghq=self.field.kind >= 2)
+                if self.last_sweep % p.measure_rate == 0:
+                    self._measure()
             if safe_before is not None and time.time() > safe_before:
                 return ExitCode.CANCELLED_TIME_LIMIT
         st = self.handle.stats(0)
@@ -297,11 +318,17 @@ class ConfigRecorder:
         return c.reshape(self.shape, order="F")
 
 
-def replay(mc, configurations, measure_rate: int = 1):
-    """replay! (DQMC.jl:418-505): for every recorded configuration recompute G
-    from scratch (calculate_greens(mc, 0), the equal-time G at slice 1) and run
-    the measurements on its physical form."""
-    for i in range(0, len(configurations), measure_rate):
+def replay(mc, configurations=None, measure_rate: int = 1):
+    """replay! (DQMC.jl:418-505): for every recorded configuration from
+    ``mc.last_sweep + 1`` on (1-based; every ``measure_rate``-th), recompute G
+    from scratch (calculate_greens(mc, 0), the equal-time G at slice 1), run
+    the measurements on its physical form and set ``mc.last_sweep`` to the
+    configuration's 1-based index, so a replay interrupted (or saved and
+    resumed) continues where it stopped.  ``configurations`` defaults to the
+    simulation's recorder."""
+    if configurations is None:
+        configurations = mc.recorder
+    for i in range(mc.last_sweep, len(configurations), measure_rate):
         conf = configurations[i]
         mc.handle.set_field(0, np.asfortranarray(conf))
         G_eff = mc.handle.calculate_greens(0, 0)
@@ -314,25 +341,53 @@ def replay(mc, configurations, measure_rate: int = 1):
 
 def save(mc, path):
     """Checkpoint of a simulation (FileIO.jl:10-57; flavors/DQMC/FileIO.jl:10-22):
-    parameters, model, field, RNG state, last sweep and recorded
-    configurations.  The stack is not saved: resume rebuilds it from the field,
-    as the reference does (DQMC.jl:178-179)."""
+    parameters (including checkerboard and check_propagation_error), model,
+    field, RNG state, last sweep, the scheduler's global update, the recorded
+    configurations, the DQMCAnalysis counters and the device measurement
+    accumulators (one checkpoint record of the chain), and the values pushed
+    into every host measurement's binner (by measurement name).  The stack is
+    not saved: resume rebuilds it from the field, as the reference does
+    (DQMC.jl:178-179)."""
     key, ctr = mc.handle.get_rng(0)
     conf = mc.handle.get_field(0)
     p = mc.parameters
     lat = mc.model.l
+    extra = {}
+    rec = mc.recorder
+    if rec is not None:
+        extra["rec_rate"] = np.array([rec.rate])
+        extra["rec_ghq"] = np.array([int(rec.ghq)])
+        extra["rec_shape"] = np.array(rec.shape if rec.shape is not None else (0, 0))
+        extra["rec_configs"] = (np.stack(rec.configs) if rec.configs
+                                else np.zeros((0, 0), dtype=np.uint8))
+    names = []
+    for name, obs in mc.measurements.items():
+        binner = getattr(obs, "observable", None)
+        if binner is None or not len(binner):
+            continue
+        names.append(str(name))
+        extra[f"meas_{len(names) - 1}"] = np.stack(binner.values)
+    extra["meas_names"] = np.array(names, dtype=str)
     np.savez(path, conf=conf, rng=np.array([key, ctr], dtype=np.uint64),
              last_sweep=mc.last_sweep, seed=mc.seed,
              params=np.array([p.beta, p.delta_tau, p.slices, p.safe_mult, p.thermalization,
-                              p.sweeps, p.measure_rate], dtype=np.float64),
+                              p.sweeps, p.measure_rate, float(p.checkerboard),
+                              float(p.check_propagation_error)], dtype=np.float64),
              model=np.array([mc.model.t, mc.model.mu, mc.model.U]),
              lattice=np.array([lat.name] + [str(x) for x in lat.Ls]),
-             field=np.array([type(mc.field).__name__]), precision=np.array([mc.precision]))
+             field=np.array([type(mc.field).__name__]), precision=np.array([mc.precision]),
+             global_update=np.array([mc.global_update or ""]),
+             device_measurements=np.array([int(mc.device_measurements)]),
+             chain_record=mc.handle.checkpoint(0), **extra)
 
 
 def resume(path, **kwargs):
     """Rebuild a simulation from a checkpoint; the next run continues the
-    chain where it stopped (resume!, FileIO.jl:155-171)."""
+    chain where it stopped (resume!, FileIO.jl:155-171): same field, RNG
+    position, parameters, checkerboard hopping, global-update schedule,
+    analysis counters, device accumulators and recorded configurations.
+    Host measurements passed in ``measurements=`` get back the values saved
+    under their names."""
     from . import lattices, model as _model
 
     d = np.load(path, allow_pickle=False)
@@ -342,15 +397,42 @@ def resume(path, **kwargs):
             "Triangular": lattices.TriangularLattice}[name]
     t, mu, U = [float(x) for x in d["model"]]
     m = _model.HubbardModel(ctor(*[int(x) for x in Ls]), U=U, mu=mu, t=t)
-    beta, dt, slices, k, th, sw, mr = d["params"]
+    prm = d["params"]
+    beta, dt, slices, k, th, sw, mr = prm[:7]
+    cb = bool(prm[7]) if prm.size > 7 else False
+    cpe = bool(prm[8]) if prm.size > 8 else True
+    gu = str(d["global_update"][0]) if "global_update" in d.files else ""
+    kw = dict(kwargs)
+    kw.setdefault("global_update", gu or None)
+    if "device_measurements" in d.files:
+        kw.setdefault("device_measurements", bool(d["device_measurements"][0]))
+    if "rec_rate" in d.files:
+        kw.setdefault("recorder", ConfigRecorder(int(d["rec_rate"][0])))
+    else:
+        kw.setdefault("recorder", False)
     mc = DQMC(m, seed=int(d["seed"]), field=getattr(_model, str(d["field"][0])),
               beta=float(beta), delta_tau=float(dt), safe_mult=int(k), thermalization=int(th),
-              sweeps=int(sw), measure_rate=int(mr), precision=str(d["precision"][0]), **kwargs)
+              sweeps=int(sw), measure_rate=int(mr), precision=str(d["precision"][0]),
+              checkerboard=cb, check_propagation_error=cpe, **kw)
     mc.field.conf[:] = d["conf"]
     mc.handle.set_field(0, np.asfortranarray(d["conf"]))
     key, ctr = [int(x) for x in d["rng"]]
     mc.handle.set_rng(0, key, ctr)
     mc.last_sweep = int(d["last_sweep"])
+    if "chain_record" in d.files:
+        mc.handle.restore_checkpoint(0, d["chain_record"])
+        mc._restore_record = np.array(d["chain_record"])  # again after the stack rebuild
+    if mc.recorder is not None and "rec_configs" in d.files:
+        rc = d["rec_configs"]
+        mc.recorder.configs = [rc[i].copy() for i in range(rc.shape[0])]
+        shp = tuple(int(x) for x in d["rec_shape"])
+        mc.recorder.shape = shp if rc.shape[0] else None
+        mc.recorder.ghq = bool(d["rec_ghq"][0])
+    if "meas_names" in d.files:
+        for i, nm in enumerate(d["meas_names"]):
+            obs = mc.measurements.get(str(nm))
+            if obs is not None and hasattr(obs, "observable"):
+                obs.observable.values = [np.array(v) for v in d[f"meas_{i}"]]
     return mc
 
 

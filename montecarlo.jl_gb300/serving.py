@@ -157,8 +157,12 @@ class Server:
         # sweeps of requests still running at a wall-clock stop count too
         for slot, (req, *_rest) in active.items():
             total_sweeps += self.pool.slot(slot)[0]
+        # block latencies of finished requests and of the blocks that requests
+        # still running at a wall-clock stop completed
         lat = [x for r in results.values() for x in r.block_latencies]
+        lat += [x for (_req, _ta, _tl, _nb, lats) in active.values() for x in lats]
         return dict(results=results, wall=wall, launches=launches, sweeps=total_sweeps,
+                    blocks=len(lat),
                     sweeps_per_s=total_sweeps / wall if wall > 0 else math.nan,
                     p50_block_s=float(np.percentile(lat, 50)) if lat else None,
                     p99_block_s=float(np.percentile(lat, 99)) if lat else None,
@@ -166,19 +170,23 @@ class Server:
 
 
 def run_ensemble(configs_and_exps, seconds: float, quantum_us=50000, precision=_lib.PREC_FP64,
-                 use_graph=True, device=0, budget_bytes=None):
+                 use_graph=True, device=0, budget_bytes=None, confs=None):
     """Advance an uneven ensemble of chains for about `seconds` of device time
-    in time-sliced launches; returns aggregate sweeps/s and per-chain sweeps."""
+    in time-sliced launches; returns aggregate sweeps/s and per-chain sweeps.
+    ``confs`` (optional): starting field configurations (e.g. thermalised
+    ones) in place of the seeded random ones; the streams stay seeded."""
     nbytes = sum(_lib.chain_bytes(c, precision) + 4096 for c, _ in configs_and_exps)
     pool = _lib.Pool(len(configs_and_exps), budget_bytes or nbytes, precision=precision,
                      device=device)
     slots = []
-    for cfg, exps in configs_and_exps:
+    for j, (cfg, exps) in enumerate(configs_and_exps):
         s = pool.admit(cfg)
         if s is None:
             raise RuntimeError("ensemble does not fit the pool budget")
         pool.set_hopping(s, exps)
         pool.init_random_field(s)
+        if confs is not None:
+            pool.set_field(s, confs[j])
         pool.set_quota(s, 1 << 40)
         slots.append(s)
     pool.run(quantum_us, use_graph)  # stack builds + warm-up slice

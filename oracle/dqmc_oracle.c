@@ -76,6 +76,8 @@ struct OcChain {
     int8_t* temp_conf;            /* temp_conf(field): the configuration before a global move */
     double* tempvf;               /* stack.tempvf: Dl of the current G during a global move */
     long g_accepted, g_proposals;
+    long n_near_tie;              /* drawn uniforms within 1e-12 of p (local_updates.jl:53) */
+    double min_tie_gap;           /* smallest |u - p| of a drawn uniform (+inf: none) */
 };
 
 int oc_generate_chunks(int length, int max_chunk, int* first, int* last) {
@@ -337,6 +339,7 @@ OcChain* oc_create(int n, int nf, int M, int safe_mult, int kind, double alpha,
                    const double* eT2, const double* eT2inv, const double* eTh,
                    const double* eThinv, uint64_t seed, int check_propagation_error) {
     OcChain* c = (OcChain*)calloc(1, sizeof(OcChain));
+    c->min_tie_gap = INFINITY;
     c->n = n; c->nf = nf; c->M = M; c->k = safe_mult; c->kind = kind; c->alpha = alpha;
     c->check_prop = check_propagation_error;
     int maxch = (M + safe_mult - 1) / safe_mult;
@@ -793,7 +796,13 @@ int oc_sweep_spatial(OcChain* c) {
         if (p < 0.0) c->n_neg_p++;
         int acc = 0;
         if (p > 1.0) acc = 1;
-        else acc = oc_word_to_uniform(next_word(c)) < p;
+        else {
+            const double u = oc_word_to_uniform(next_word(c));
+            acc = u < p;
+            const double gap = fabs(u - p);
+            if (gap < 1e-12) c->n_near_tie++;
+            if (gap < c->min_tie_gap) c->min_tie_gap = gap;
+        }
         if (acc) {
             for (int b = 0; b < nf; ++b)
                 update_block(n, c->greens + b * nn, R[b], delta[b], i, IG, Gr);
@@ -1052,6 +1061,8 @@ void oc_get_analysis(const OcChain* c, double* out) {
     out[2] = c->prop_err_reported;
     out[3] = (double)c->n_neg_p;
     out[4] = (double)c->accepted;
+    out[5] = (double)c->n_near_tie;
+    out[6] = c->min_tie_gap;
 }
 
 /* ---------------------------------------------------- threaded baseline */

@@ -75,8 +75,9 @@ void oc_get_state(const OcChain* c, int* state4);
 /* which = 0 u_stack, 1 t_stack (nf*n*n), 2 d_stack (nf*n); idx 1-based */
 void oc_get_stack(const OcChain* c, int which, int idx, double* out);
 /* analysis: [max propagation error over all stabilisations, count > 1e-7,
- *            max reported (>1e-7), negative-p count, accepted total] */
-void oc_get_analysis(const OcChain* c, double* out5);
+ *            max reported (>1e-7), negative-p count, accepted total,
+ *            near ties (drawn uniforms within 1e-12 of p), smallest |u - p|] */
+void oc_get_analysis(const OcChain* c, double* out7);
 
 /* checkerboard = true (stack.jl:240-246, linalg/checkerboard.jl): the four
  * hopping factors as np parts each, data = 4 x (D[n], np x (cosh-or-1[n],

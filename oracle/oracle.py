@@ -301,11 +301,11 @@ class OracleChain:
         return a.value, p.value
 
     def analysis(self):
-        out = np.zeros(5)
+        out = np.zeros(7)
         lib().oc_get_analysis(self.h, _dp(out))
         return dict(propagation_error_max=out[0], propagation_error_count=int(out[1]),
                     propagation_error_reported=out[2], negative_probability=int(out[3]),
-                    accepted=int(out[4]))
+                    accepted=int(out[4]), near_ties=int(out[5]), min_tie_gap=out[6])
 
 
 def run_chains_threaded(chains, nsweeps, threads):
