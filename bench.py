@@ -321,9 +321,11 @@ def c4_line(pkg, _lib, stream, n_chains, seed=4):
     nr = len(pkg.generate_chunks(M, param.safe_mult))
     out = {"workload": "16x16 square repulsive Hubbard U=4 (physics), mu=0, MagneticHirschField, "
                        f"beta=10, dtau=0.1 (M=100), safe_mult=10, {n_chains} chains, one timed "
-                       "sweep per path after the stack build"}
-    for name, prec in (("fp64", _lib.PREC_FP64), ("mixed", _lib.PREC_MIXED)):
-        h = _lib.Handle([_lib.ChainConfig(n, 2, M, 10, fld.kind, 1, fld.alpha, seed + j)
+                       "sweep per path after the stack build; mixed: tensor-core products "
+                       "(tcgen05, 7 BF16 digit slices) for the wraps, slice chains and "
+                       "reconstruction"}
+    def one(prec, k):
+        h = _lib.Handle([_lib.ChainConfig(n, 2, M, k, fld.kind, 1, fld.alpha, seed + j)
                          for j in range(n_chains)], precision=prec)
         h.set_hopping(-1, exps)
         h.init_random_field(-1)
@@ -341,13 +343,29 @@ def c4_line(pkg, _lib, stream, n_chains, seed=4):
         s1 = [h.stats(i) for i in range(n_chains)]
         acc = sum(b["accepted"] - a["accepted"] for a, b in zip(s0, s1)) / max(
             1, sum(b["proposals"] - a["proposals"] for a, b in zip(s0, s1)))
-        out[name] = {"sweeps_per_s": n_chains / t, "launch_s": t,
-                     "max_propagation_error": max(x["max_propagation_error"] for x in s1),
-                     "acceptance": acc}
-        if name == "fp64":
-            out[name]["tflops"] = n_chains * sweep_flops(n, 2, M, nr, acc) / t / 1e12
+        pe = [x["max_propagation_error"] for x in s1]
         h.close()
+        return {"sweeps_per_s": n_chains / t, "launch_s": t, "safe_mult": k,
+                "max_propagation_error": max(pe), "chains_over_1e-6": int(sum(v > 1e-6 for v in pe)),
+                "acceptance": acc}
+
+    out["fp64"] = one(_lib.PREC_FP64, 10)
+    out["fp64"]["tflops"] = n_chains * sweep_flops(n, 2, M, nr, out["fp64"]["acceptance"]) / \
+        out["fp64"]["launch_s"] / 1e12
+    out["mixed"] = one(_lib.PREC_MIXED, 10)
     out["mixed_vs_fp64"] = out["mixed"]["sweeps_per_s"] / out["fp64"]["sweeps_per_s"]
+    # the largest safe_mult at which every mixed chain's propagation error
+    # stays <= 1e-6 over the timed sweep
+    strict = out["mixed"] if out["mixed"]["max_propagation_error"] <= 1e-6 else None
+    for k in (6, 5, 4, 3):
+        if strict is not None:
+            break
+        r = one(_lib.PREC_MIXED, k)
+        if r["max_propagation_error"] <= 1e-6:
+            strict = r
+    out["mixed_strict_1e-6"] = strict
+    if strict is not None:
+        out["mixed_strict_vs_fp64"] = strict["sweeps_per_s"] / out["fp64"]["sweeps_per_s"]
     hs = [_lib.Handle([_lib.ChainConfig(n, 2, M, 10, fld.kind, 1, fld.alpha, seed)], precision=pr)
           for pr in (_lib.PREC_FP64, _lib.PREC_MIXED)]
     for hc in hs:

@@ -129,13 +129,19 @@ int dqmc_set_stream(dqmc_handle* h, void* cuda_stream);
  * enable = 1; pools always use the CTA kernel).  Same state, workspace and
  * accept/reject decisions; sums in a different order (G agrees to rounding). */
 int dqmc_set_small_chain_kernel(dqmc_handle* h, int enable);
-/* Mixed-precision chains with 96 <= n_sites <= 256 (real, dense hopping) run
- * their wraps, slice-matrix chains and reconstruction products on the tensor
- * cores: tcgen05 MMAs on BF16 digit slices of the operands (six per operand,
- * exact FP32 accumulation per digit level, about 46 correct bits, the class
- * of the double-float products they replace).  enable = 0 returns them to the
- * double-float products on the FP32 pipe (default 1).  chain = -1: all. */
-int dqmc_set_tensor_products(dqmc_handle* h, int chain, int enable);
+/* Mixed-precision chains with 96 <= n_sites <= 256 (real, dense hopping) can
+ * run products on the tensor cores: tcgen05 MMAs on BF16 digit slices of the
+ * operands (six per operand, exact FP32 accumulation per digit level, 47 bits
+ * relative to each row's / column's largest entry) instead of the
+ * double-float products on the FP32 pipe.  mask: DQMC_TC_WRAPS (the ordinary
+ * wraps of G), DQMC_TC_SLICES (the slice-matrix chains of the stack),
+ * DQMC_TC_GREENS (the products of the Green's reconstruction); 0: none.
+ * The default for new chains is DQMC_TC_DEFAULT.  chain = -1: all. */
+#define DQMC_TC_WRAPS 1
+#define DQMC_TC_SLICES 2
+#define DQMC_TC_GREENS 4
+#define DQMC_TC_DEFAULT (DQMC_TC_WRAPS | DQMC_TC_SLICES | DQMC_TC_GREENS)
+int dqmc_set_tensor_products(dqmc_handle* h, int chain, int mask);
 /* Device bytes one chain needs (stack + Green's function workspace). */
 int64_t dqmc_chain_bytes(const dqmc_chain_config* cfg, int precision);
 
@@ -297,6 +303,60 @@ int dqmc_set_global_schedule(dqmc_handle* h, int chain, int kind);
 int dqmc_replica_exchange(dqmc_handle* h, const int32_t* partner, int32_t* accepted);
 /* accepted / proposed global and replica moves since creation */
 int dqmc_get_global_stats(dqmc_handle* h, int chain, int64_t* accepted, int64_t* proposals);
+
+/* ---- time-displaced measurements on the device ----------------------------------
+ * Replaces: the TimeIntegral measurements of run! (generic.jl:337-366: the
+ * unequal-time G(0,0), G(0,l), G(l,0), G(l,l) of the UnequalTimeStack for
+ * l = 0..M with trapezoid weights) with the Wick kernels full_cdc_kernel
+ * (charge_density.jl:65-112), full_sdc_x/y/z_kernel (spin_density.jl:100-227)
+ * and pc_combined_kernel (pairing.jl:95-161), reduced by distance as
+ * EachSitePairByDistance does (lattice_iterators.jl:160-260,
+ * generic.jl:434-461, divided by the number of sites, :582-584), and the
+ * susceptibilities charge_density_susceptibility,
+ * spin_density_susceptibility (x, y, z at q), pairing_susceptibility (on
+ * site, and with the extended-s and d-wave form factors of the caller's
+ * bonds) and the uniform current_current_susceptibility of the caller's
+ * current operator.  Everything is computed and log-binned on the device,
+ * after every measure_rate-th sweep (the chain's sweep counter, shared with
+ * the equal-time measurements) inside dqmc_sweep / dqmc_pool_run, or now
+ * with dqmc_td_measure.  Real chains only. */
+typedef struct {
+    int32_t enable;          /* 1: measure; 0: stop measuring (accumulators are kept) */
+    int32_t measure_rate;    /* >= 1 */
+    int32_t n_slots;         /* P: length of each by-distance array (Ndir * B * B) */
+    int32_t n_form[2];       /* bonds of the extended-s and d form factors (0: none) */
+    int32_t n_current;       /* nonzero entries of the current operator (0: none) */
+    double delta_tau;
+    int64_t sweep;           /* the chain's sweep counter now; < 0 keeps it */
+    const int32_t* pair_slot;     /* n_sites^2: by-distance slot of (src, trg) at src + n*trg */
+    const double* q_cos;          /* n_sites cos(q . r_i) (NULL: q = 0) */
+    const double* q_sin;          /* n_sites sin(q . r_i) (NULL: zeros) */
+    const int32_t* form_sites;    /* 2 * (n_form[0] + n_form[1]) 0-based site pairs (a, b) */
+    const double* form_values;    /* F_ab of those pairs */
+    const int32_t* current_sites; /* 2 * n_current: (r, s) of the entries A[r, s] */
+    const double* current_values; /* 2 * n_current: (re, im) of A[r, s] */
+} dqmc_td_config;
+
+/* Susceptibilities: 0 charge(q), 1 spin x(q), 2 spin y(q), 3 spin z(q),
+ * 4 on-site s-wave pairing, 5 extended-s pairing, 6 d-wave pairing,
+ * 7 uniform current (all (1/n) int_0^beta d tau); errors as for
+ * dqmc_observables. */
+typedef struct {
+    int64_t count;
+    double mean[8];
+    double error[8];
+    int32_t error_level[8];
+} dqmc_td_observables;
+
+/* A new configuration with other array sizes clears the accumulators. */
+int dqmc_set_td_measurements(dqmc_handle* h, int chain, const dqmc_td_config* cfg);
+/* One measurement of every chain that has them set up, now. */
+int dqmc_td_measure(dqmc_handle* h);
+/* mean / error (may be NULL): 5 * n_slots values, the by-distance arrays of
+ * the charge, spin x, spin y, spin z and on-site pairing correlations, each
+ * (Ndir, B, B) column-major. */
+int dqmc_get_td_measurements(dqmc_handle* h, int chain, dqmc_td_observables* out, double* mean,
+                             double* error);
 
 /* ---- checkpoint state -----------------------------------------------------------
  * Replaces: the parts of a saved simulation that live with the chain

@@ -18,7 +18,7 @@ from .measurements import (LogBinner, double_occupancy as double_occupancy_kerne
                            spin_susceptibility_z, structure_factor, time_displaced_sdc_z,
                            susceptibilities, time_displaced_correlations, CORRELATIONS,
                            current_operator, bilinear_correlation, pair_form_factor,
-                           pair_correlation)
+                           pair_correlation, td_arrays, by_distance)
 from .dqmc import (DQMC, ExitCode, Measurement, double_occupancy, greens_measurement,  # noqa: F401
                    occupation, spin_density_correlation)
 

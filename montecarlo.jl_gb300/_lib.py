@@ -65,6 +65,25 @@ class Observables(C.Structure):
                 ("error_level", C.c_int32 * 4)]
 
 
+class TdConfig(C.Structure):
+    _fields_ = [("enable", C.c_int32), ("measure_rate", C.c_int32), ("n_slots", C.c_int32),
+                ("n_form", C.c_int32 * 2), ("n_current", C.c_int32), ("delta_tau", C.c_double),
+                ("sweep", C.c_int64), ("pair_slot", C.c_void_p), ("q_cos", C.c_void_p),
+                ("q_sin", C.c_void_p), ("form_sites", C.c_void_p), ("form_values", C.c_void_p),
+                ("current_sites", C.c_void_p), ("current_values", C.c_void_p)]
+
+
+class TdObservables(C.Structure):
+    _fields_ = [("count", C.c_int64), ("mean", C.c_double * 8), ("error", C.c_double * 8),
+                ("error_level", C.c_int32 * 8)]
+
+
+# susceptibilities of the device time-displaced measurements (dqmc_td_observables
+# order) and the correlations of its by-distance arrays
+TD_SCALARS = ["charge", "spin_x", "spin_y", "spin_z", "pairing", "pairing_s*", "pairing_d",
+              "current"]
+TD_KINDS = ["charge", "spin_x", "spin_y", "spin_z", "pairing"]
+
 # scalar observables of the device accumulators, in dqmc_observables order
 OBSERVABLES = ["density", "double_occupancy", "interaction_energy", "sz_structure_factor"]
 
@@ -82,8 +101,13 @@ EXPORTS = [
     "dqmc_get_global_stats", "dqmc_calculate_greens_kl", "dqmc_set_checkerboard",
     "dqmc_set_small_chain_kernel", "dqmc_get_greens_batch", "dqmc_get_fields_batch",
     "dqmc_set_fields_batch", "dqmc_checkpoint_doubles", "dqmc_get_checkpoint",
-    "dqmc_set_checkpoint", "dqmc_set_tensor_products",
+    "dqmc_set_checkpoint", "dqmc_set_tensor_products", "dqmc_set_td_measurements",
+    "dqmc_td_measure", "dqmc_get_td_measurements",
 ]
+
+# products on the tensor cores (dqmc_set_tensor_products)
+TC_WRAPS, TC_SLICES, TC_GREENS = 1, 2, 4
+TC_DEFAULT = TC_WRAPS | TC_SLICES | TC_GREENS
 
 GLOBAL_FLIP = 0
 GLOBAL_SHUFFLE = 1
@@ -155,6 +179,10 @@ def load(path: str = LIB_PATH):
                                         C.c_void_p]
     L.dqmc_pool_free_bytes.restype = C.c_int64
     L.dqmc_set_tensor_products.argtypes = [P, C.c_int, C.c_int]
+    L.dqmc_set_td_measurements.argtypes = [P, C.c_int, C.POINTER(TdConfig)]
+    L.dqmc_td_measure.argtypes = [P]
+    L.dqmc_get_td_measurements.argtypes = [P, C.c_int, C.POINTER(TdObservables), C.c_void_p,
+                                           C.c_void_p]
     L.dqmc_checkpoint_doubles.argtypes = [P, C.c_int]
     L.dqmc_checkpoint_doubles.restype = C.c_int64
     L.dqmc_get_checkpoint.argtypes = [P, C.c_int, dp]
@@ -239,8 +267,11 @@ class Handle:
 
     def set_tensor_products(self, enable=True, chain=-1):
         """Tensor-core split-precision products for mixed chains of
-        96 <= n <= 256 (default on) or the double-float FP32-pipe products."""
-        check(load().dqmc_set_tensor_products(self.h, int(chain), int(bool(enable))))
+        96 <= n <= 256: True (the library's default set), False (none: the
+        double-float FP32-pipe products) or a mask of TC_WRAPS, TC_SLICES,
+        TC_GREENS."""
+        mask = TC_DEFAULT if enable is True else (0 if enable is False else int(enable))
+        check(load().dqmc_set_tensor_products(self.h, int(chain), mask))
 
     def set_hopping(self, chain, exps):
         e = [np.asfortranarray(x, dtype=np.float64) for x in exps]
@@ -377,6 +408,47 @@ class Handle:
         for k, name in enumerate(OBSERVABLES):
             out[name] = (o.mean[k], o.error[k])
             out[name + "_level"] = o.error_level[k]
+        return out
+
+    def set_td_measurements(self, chain, arrays, delta_tau, enable=True, rate=1, sweep=-1):
+        """Device time-displaced measurements (dqmc_set_td_measurements);
+        ``arrays`` from measurements.td_arrays (pair slots, q phases, form
+        factors, current operator)."""
+        a = arrays
+        keep = []
+
+        def ptr(x, dt):
+            if x is None:
+                return None
+            v = np.ascontiguousarray(x, dtype=dt)
+            keep.append(v)
+            return v.ctypes.data
+
+        cfg = TdConfig(int(bool(enable)), int(rate), int(a["n_slots"]),
+                       (C.c_int32 * 2)(*a["n_form"]), int(a["n_current"]), float(delta_tau),
+                       int(sweep), ptr(a["pair_slot"], np.int32), ptr(a["q_cos"], np.float64),
+                       ptr(a["q_sin"], np.float64), ptr(a["form_sites"], np.int32),
+                       ptr(a["form_values"], np.float64), ptr(a["current_sites"], np.int32),
+                       ptr(a["current_values"], np.float64))
+        check(load().dqmc_set_td_measurements(self.h, int(chain), C.byref(cfg)))
+
+    def td_measure(self):
+        """One time-displaced measurement of every chain that has them, now."""
+        check(load().dqmc_td_measure(self.h))
+
+    def td_measurements(self, chain, n_slots):
+        """Means and binning errors of the device time-displaced measurements:
+        the susceptibilities and the by-distance arrays (kind, slot)."""
+        o = TdObservables()
+        mean = np.zeros(len(TD_KINDS) * n_slots)
+        err = np.zeros(len(TD_KINDS) * n_slots)
+        check(load().dqmc_get_td_measurements(self.h, chain, C.byref(o), mean.ctypes.data,
+                                              err.ctypes.data))
+        out = {"count": o.count,
+               "by_distance": mean.reshape(len(TD_KINDS), n_slots),
+               "by_distance_error": err.reshape(len(TD_KINDS), n_slots)}
+        for k, name in enumerate(TD_SCALARS):
+            out[name] = (o.mean[k], o.error[k])
         return out
 
     def set_checkerboard(self, chain, data=None, n_parts=-1):

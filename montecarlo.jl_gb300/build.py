@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdqmc_gb300.so")
-SOURCES = ["dqmc_kernels.cu", "dqmc_warp.cu", "dqmc_capi.cu", "dqmc_noalloc.cu"]
+SOURCES = ["dqmc_kernels.cu", "dqmc_kernels_tc.cu", "dqmc_warp.cu", "dqmc_capi.cu",
+           "dqmc_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

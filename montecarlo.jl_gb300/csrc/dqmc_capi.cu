@@ -15,6 +15,7 @@
 #include "dqmc_chain.h"
 #include "dqmc_host_tables.h"
 #include "dqmc_kernels.h"
+#include "dqmc_tc.cuh"
 #include "philox.h"
 
 using dqmc_host::fill_tables;
@@ -95,8 +96,14 @@ struct Layout {
     size_t bytes;
     size_t off_conf, off_hop, off_G, off_Gtmp, off_Ul, off_Ur, off_Tl, off_Tr, off_tmp1, off_tmp2,
         off_currU, off_out, off_ustack, off_tstack, off_dstack, off_Dl, off_Dr, off_tempv,
-        off_pivot, off_meas, off_qcs, off_tconf, off_tempvf, off_hopdf;
+        off_pivot, off_meas, off_qcs, off_tconf, off_tempvf, off_hopdf, off_tcs;
 };
+
+// chains whose products may run on the tensor cores (mm_tc, dqmc_tc.cuh):
+// real, mixed precision, 96 <= n <= 256; they carry its slice scratch
+bool tc_capable(const dqmc_chain_config& c, int prec) {
+    return prec == DQMC_PREC_MIXED && !is_cplx(c) && c.n_sites >= 96 && c.n_sites <= DQMC_TC_NMAX;
+}
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
@@ -123,6 +130,8 @@ Layout layout_of(const dqmc_chain_config& c, int prec) {
     L.off_tconf = o; o = align256(o + nconf);
     L.off_tempvf = o; o = align256(o + nf * n * sizeof(double));
     L.off_hopdf = o; o = align256(o + 2 * n * n * sizeof(float2));
+    L.off_tcs = o;
+    if (tc_capable(c, prec)) o = align256(o + dqmc_tc_scratch_bytes((int)n));
     L.bytes = o;
     return L;
 }
@@ -149,9 +158,11 @@ struct dqmc_handle {
     std::vector<size_t> slot_off, slot_bytes;
     DqmcChain* pinned = nullptr;           // pinned mirror for graph replays
     int n_max = 0;                         // largest n_sites of a fixed handle's chains
+    bool tc = false;                       // launches use the tensor-core kernel build
     bool small_kernel = true;              // sweeps of small chains one warp per chain
     std::vector<double*> ut_mem;           // per-chain unequal-time workspaces (lazy)
     std::vector<double*> cb_mem;           // per-chain checkerboard factors
+    std::vector<double*> td_mem;           // per-chain time-displaced measurement buffers
     cudaGraphExec_t graph = nullptr;
     int graph_budget_us = -1;
 };
@@ -204,7 +215,7 @@ int launch(dqmc_handle* h, int op, int arg0, int arg1, bool sync) {
                  "warp sweep kernel launch");
     else
         CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), op, arg0, arg1,
-                                          h->stream, h->pool ? 0 : h->n_max),
+                                          h->stream, h->pool ? 0 : h->n_max, h->tc),
                  "chain kernel launch");
     if (!sync) {
         h->busy = true;
@@ -271,6 +282,7 @@ void fill_descriptor(DqmcChain& d, const dqmc_chain_config& c, char* b, const La
     d.meas_rate = 1;
     d.temp_conf = (int8_t*)(b + L.off_tconf);
     d.tempvf = (double*)(b + L.off_tempvf);
+    d.tcs = tc_capable(c, precision) ? (unsigned char*)(b + L.off_tcs) : nullptr;
     d.alpha_field = c.alpha;
     d.partner = -1;
     d.global_kind = -1;
@@ -280,7 +292,7 @@ void fill_descriptor(DqmcChain& d, const dqmc_chain_config& c, char* b, const La
         ms[2] = 0.0;
     }
     d.min_tie_gap = INFINITY;
-    d.tc_enable = 0;
+    d.tc_enable = DQMC_TC_DEFAULT;
     d.key = c.seed; d.ctr = 0;
     d.current_slice = 0; d.current_range = 1; d.direction = 1;
     d.active = 1;
@@ -350,7 +362,10 @@ int dqmc_create(int device, const dqmc_chain_config* chains, int n_chains, int p
     h->device = device;
     h->precision = precision;
     h->cfg.assign(chains, chains + n_chains);
-    for (int i = 0; i < n_chains; ++i) h->n_max = std::max(h->n_max, (int)mat_n(chains[i]));
+    for (int i = 0; i < n_chains; ++i) {
+        h->n_max = std::max(h->n_max, (int)mat_n(chains[i]));
+        h->tc = h->tc || tc_capable(chains[i], precision);
+    }
     size_t total = 0;
     std::vector<size_t> base(n_chains);
     for (int i = 0; i < n_chains; ++i) {
@@ -391,6 +406,8 @@ int dqmc_destroy(dqmc_handle* h) {
     if (h->arena) cudaFree(h->arena);
     for (double* p : h->ut_mem)
         if (p) cudaFree(p);
+    for (double* p : h->td_mem)
+        if (p) cudaFree(p);
     for (double* p : h->cb_mem)
         if (p) cudaFree(p);
     if (h->d_chains) cudaFree(h->d_chains);
@@ -408,13 +425,15 @@ int dqmc_set_small_chain_kernel(dqmc_handle* h, int enable) {
     return DQMC_OK;
 }
 
-int dqmc_set_tensor_products(dqmc_handle* h, int chain, int enable) {
+int dqmc_set_tensor_products(dqmc_handle* h, int chain, int mask) {
     if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    if (mask < 0 || mask > (DQMC_TC_WRAPS | DQMC_TC_SLICES | DQMC_TC_GREENS))
+        return fail(DQMC_ERR_INVALID, "dqmc_set_tensor_products: unknown mask");
     int lo = chain, hi = chain + 1;
     if (chain == -1) { lo = 0; hi = (int)h->cfg.size(); }
     else if (int st = check_chain(h, chain)) return st;
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
-    for (int i = lo; i < hi; ++i) h->host[i].tc_enable = enable ? 1 : 0;
+    for (int i = lo; i < hi; ++i) h->host[i].tc_enable = mask;
     h->host_dirty = true;
     return DQMC_OK;
 }
@@ -674,7 +693,7 @@ static int launch_one(dqmc_handle* h, int chain, int op, int arg0, int arg1) {
     CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
     if (h->host_dirty) if (int st = push_descriptors(h)) return st;
     CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains + chain, 1, op, arg0, arg1, h->stream,
-                                      (int)mat_n(h->cfg[chain])),
+                                      (int)mat_n(h->cfg[chain]), h->host[chain].tcs != nullptr),
              "chain kernel launch");
     CUDA_TRY(cudaStreamSynchronize(h->stream), "chain kernel");
     return pull_descriptors(h);
@@ -1201,6 +1220,146 @@ int dqmc_get_global_stats(dqmc_handle* h, int chain, int64_t* accepted, int64_t*
     return DQMC_OK;
 }
 
+/* ---- time-displaced measurements on the device ----------------------------------- */
+
+static int ensure_ut(dqmc_handle* h, int chain) {
+    DqmcChain& d = h->host[chain];
+    if (h->ut_mem.size() < h->host.size()) h->ut_mem.resize(h->host.size(), nullptr);
+    if (!h->ut_mem[chain]) {
+        CUDA_TRY(cudaMalloc((void**)&h->ut_mem[chain],
+                            DQMC_UT_DOUBLES(d.n, d.nf, d.nr) * sizeof(double)),
+                 "allocate the unequal-time stack");
+    }
+    d.ut = h->ut_mem[chain];
+    return DQMC_OK;
+}
+
+int dqmc_set_td_measurements(dqmc_handle* h, int chain, const dqmc_td_config* cfg) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!cfg) return fail(DQMC_ERR_INVALID, "dqmc_set_td_measurements: null config");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    DqmcChain& d = h->host[chain];
+    if (!cfg->enable) {
+        d.td_enable = 0;
+        h->host_dirty = true;
+        return DQMC_OK;
+    }
+    if (d.cplx)
+        return fail(DQMC_ERR_INVALID, "dqmc_set_td_measurements: real chains only (complex G: "
+                                      "use dqmc_calculate_greens_kl)");
+    const int n = d.n, P = cfg->n_slots;
+    const int nf0 = cfg->n_form[0], nf1 = cfg->n_form[1], nc = cfg->n_current;
+    if (cfg->measure_rate < 1 || P < 1 || nf0 < 0 || nf1 < 0 || nc < 0 || !cfg->pair_slot ||
+        !(cfg->delta_tau > 0.0) || ((nf0 + nf1) > 0 && (!cfg->form_sites || !cfg->form_values)) ||
+        (nc > 0 && (!cfg->current_sites || !cfg->current_values)))
+        return fail(DQMC_ERR_INVALID, "dqmc_set_td_measurements: bad configuration");
+    const TdLayout L = td_layout(n, d.nf, P, nf0 + nf1, nc);
+    std::vector<double> buf(L.g, 0.0);  // everything before the Green's functions
+    int32_t* slot = reinterpret_cast<int32_t*>(buf.data() + L.slot);
+    for (size_t e = 0; e < (size_t)n * n; ++e) {
+        const int v = cfg->pair_slot[e];
+        if (v < 0 || v >= P) return fail(DQMC_ERR_INVALID, "dqmc_set_td_measurements: slot out of range");
+        slot[e] = v;
+    }
+    for (int i = 0; i < n; ++i) {
+        buf[L.q + i] = cfg->q_cos ? cfg->q_cos[i] : 1.0;
+        buf[L.q + n + i] = cfg->q_sin ? cfg->q_sin[i] : 0.0;
+    }
+    for (int p = 0; p < nf0 + nf1; ++p) {
+        const int a = cfg->form_sites[2 * p], b = cfg->form_sites[2 * p + 1];
+        if (a < 0 || a >= n || b < 0 || b >= n)
+            return fail(DQMC_ERR_INVALID, "dqmc_set_td_measurements: form-factor site out of range");
+        buf[L.form + 3 * p] = a;
+        buf[L.form + 3 * p + 1] = b;
+        buf[L.form + 3 * p + 2] = cfg->form_values[p];
+    }
+    for (int p = 0; p < nc; ++p) {
+        const int r = cfg->current_sites[2 * p], s2 = cfg->current_sites[2 * p + 1];
+        if (r < 0 || r >= n || s2 < 0 || s2 >= n)
+            return fail(DQMC_ERR_INVALID, "dqmc_set_td_measurements: current site out of range");
+        buf[L.cur + 4 * p] = r;
+        buf[L.cur + 4 * p + 1] = s2;
+        buf[L.cur + 4 * p + 2] = cfg->current_values[2 * p];
+        buf[L.cur + 4 * p + 3] = cfg->current_values[2 * p + 1];
+    }
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    if (int st = ensure_ut(h, chain)) return st;
+    if (h->td_mem.size() < h->host.size()) h->td_mem.resize(h->host.size(), nullptr);
+    // a new layout replaces the buffer and its accumulators
+    const bool same = h->td_mem[chain] && d.td_P == P && d.td_nform0 == nf0 &&
+                      d.td_nform1 == nf1 && d.td_ncur == nc;
+    if (!same) {
+        if (h->td_mem[chain]) cudaFree(h->td_mem[chain]);
+        h->td_mem[chain] = nullptr;
+        CUDA_TRY(cudaMalloc((void**)&h->td_mem[chain], L.total * sizeof(double)),
+                 "allocate the time-displaced measurement buffer");
+        CUDA_TRY(cudaMemsetAsync(h->td_mem[chain], 0, L.total * sizeof(double), h->stream),
+                 "clear the time-displaced accumulators");
+    }
+    CUDA_TRY(cudaMemcpyAsync(h->td_mem[chain], buf.data(), L.g * sizeof(double),
+                             cudaMemcpyHostToDevice, h->stream),
+             "upload the time-displaced configuration");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    d.td = h->td_mem[chain];
+    d.td_enable = 1;
+    d.td_rate = cfg->measure_rate;
+    d.td_P = P;
+    d.td_nform0 = nf0;
+    d.td_nform1 = nf1;
+    d.td_ncur = nc;
+    d.td_dtau = cfg->delta_tau;
+    if (cfg->sweep >= 0) d.sweep = cfg->sweep;
+    h->host_dirty = true;
+    return DQMC_OK;
+}
+
+int dqmc_td_measure(dqmc_handle* h) {
+    if (!h) return fail(DQMC_ERR_INVALID, "null handle");
+    bool any = false;
+    for (const DqmcChain& d : h->host) any = any || (d.active && d.td);
+    if (!any) return fail(DQMC_ERR_INVALID, "dqmc_td_measure: no chain has time-displaced "
+                                            "measurements set up");
+    return launch(h, DQMC_OP_TD_MEASURE, 0, 0, true);
+}
+
+int dqmc_get_td_measurements(dqmc_handle* h, int chain, dqmc_td_observables* out, double* mean,
+                             double* error) {
+    if (int st = check_chain(h, chain)) return st;
+    if (!out) return fail(DQMC_ERR_INVALID, "dqmc_get_td_measurements: null out");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    const DqmcChain& d = h->host[chain];
+    if (!d.td) return fail(DQMC_ERR_INVALID, "dqmc_get_td_measurements: not set up for this chain");
+    CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+    const TdLayout L = td_layout(d.n, d.nf, d.td_P, d.td_nform0 + d.td_nform1, d.td_ncur);
+    std::vector<double> m(L.total - L.acc);
+    CUDA_TRY(cudaMemcpyAsync(m.data(), d.td + L.acc, m.size() * sizeof(double),
+                             cudaMemcpyDeviceToHost, h->stream),
+             "download the time-displaced accumulators");
+    CUDA_TRY(cudaStreamSynchronize(h->stream), "synchronize");
+    out->count = (int64_t)m[0];
+    auto stats = [&](int k, double* mu, double* err, int32_t* lvl) {
+        const double* lv = m.data() + DQMC_MEAS_HEADER + (size_t)k * DQMC_MEAS_LEVELS * DQMC_MEAS_BIN_WORDS;
+        *mu = lv[0] > 0 ? lv[1] : NAN;
+        int use = -1;
+        for (int l = 0; l < DQMC_MEAS_LEVELS; ++l)
+            if (lv[l * DQMC_MEAS_BIN_WORDS] >= 32.0) use = l;
+        if (use < 0) use = 0;
+        const double nb = lv[use * DQMC_MEAS_BIN_WORDS], m2 = lv[use * DQMC_MEAS_BIN_WORDS + 2];
+        *err = nb >= 2.0 ? sqrt(m2 / (nb - 1.0) / nb) : INFINITY;
+        if (lvl) *lvl = use;
+    };
+    for (int k = 0; k < DQMC_TD_SCALARS; ++k)
+        stats(k, &out->mean[k], &out->error[k], &out->error_level[k]);
+    const int nv = DQMC_TD_KINDS * d.td_P;
+    for (int k = 0; k < nv; ++k) {
+        double mu, err;
+        stats(DQMC_TD_SCALARS + k, &mu, &err, nullptr);
+        if (mean) mean[k] = mu;
+        if (error) error[k] = err;
+    }
+    return DQMC_OK;
+}
+
 /* ---- checkpoint state --------------------------------------------------------- */
 
 // Counters of a chain's checkpoint record, in order (integers stored as doubles,
@@ -1302,11 +1461,14 @@ int dqmc_pool_create(int device, int max_slots, int64_t budget_bytes, int precis
         return fail(DQMC_ERR_CUDA, std::string("no CUDA device: ") + cudaGetErrorString(e));
     if (device < 0 || device >= ndev) return fail(DQMC_ERR_INVALID, "dqmc_pool_create: bad device");
     CUDA_TRY(cudaSetDevice(device), "cudaSetDevice");
-    CUDA_TRY(dqmc_prepare_chain_kernel(), "kernel attributes");
+    CUDA_TRY(dqmc_prepare_chain_kernels(), "kernel attributes");
     dqmc_handle* h = new dqmc_handle();
     h->device = device;
     h->precision = precision;
     h->pool = true;
+    // a mixed pool may admit tensor-core-capable chains at any time (its
+    // launch is captured once and replayed)
+    h->tc = precision == DQMC_PREC_MIXED;
     h->budget = align256((size_t)budget_bytes);
     h->cfg.assign(max_slots, dqmc_chain_config{});
     h->lay.assign(max_slots, Layout{});
@@ -1368,6 +1530,10 @@ int dqmc_pool_release(dqmc_handle* h, int slot) {
         cudaFree(h->ut_mem[slot]);
         h->ut_mem[slot] = nullptr;
     }
+    if ((size_t)slot < h->td_mem.size() && h->td_mem[slot]) {
+        cudaFree(h->td_mem[slot]);
+        h->td_mem[slot] = nullptr;
+    }
     if ((size_t)slot < h->cb_mem.size() && h->cb_mem[slot]) {
         cudaFree(h->cb_mem[slot]);
         h->cb_mem[slot] = nullptr;
@@ -1422,7 +1588,7 @@ int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph) {
         CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
         cudaError_t e1 = cudaMemcpyAsync(h->d_chains, h->pinned, bytes, cudaMemcpyHostToDevice, h->stream);
         cudaError_t e2 = dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), DQMC_OP_RUN,
-                                                  budget_us, 0, h->stream, 0);
+                                                  budget_us, 0, h->stream, 0, h->tc);
         cudaError_t e3 = cudaMemcpyAsync(h->pinned, h->d_chains, bytes, cudaMemcpyDeviceToHost, h->stream);
         cudaError_t e4 = cudaStreamEndCapture(h->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {

@@ -117,10 +117,22 @@ struct DqmcChain {
     // the smallest |u - p| of any drawn proposal (+inf before the first)
     long long n_near_tie;
     double min_tie_gap;
-    // mixed chains with 96 <= n <= 256: run the products on the tensor cores
-    // (tcgen05 split-precision products) instead of the FP32 pipe (1 = on)
+    // mixed chains with 96 <= n <= 256: which products run on the tensor
+    // cores (tcgen05 split-precision products) instead of the FP32 pipe, a
+    // mask of DQMC_TC_WRAPS, DQMC_TC_SLICES, DQMC_TC_GREENS
     int tc_enable, pad4;
+    unsigned char* tcs;  // the tensor products' slice scratch (NULL: chain cannot use them)
+    // time-displaced measurements on the device (td_measure in
+    // dqmc_chain_ops.cuh): on/off, sweeps between measurements (on the sweep
+    // counter `sweep`), slots of the by-distance arrays, bonds of the two pair
+    // form factors, entries of the current operator, delta tau, and the buffer
+    // (layout td_layout below)
+    int td_enable, td_rate, td_P, td_nform0, td_nform1, td_ncur;
+    double td_dtau;
+    double* td;
 };
+
+
 // the near-tie window of DqmcChain::n_near_tie
 #define DQMC_NEAR_TIE 1e-12
 #ifdef __CUDACC__
@@ -157,6 +169,37 @@ __device__ __forceinline__ void note_tie(DqmcChain& c, double u, double p) {
 #define DQMC_MEAS_DOUBLES(n, nf) \
     ((size_t)DQMC_MEAS_OCC_OFF + (size_t)(nf) * (n) + (size_t)(nf) * (n) * (n))
 
+// Time-displaced measurements: the susceptibilities (scalars) and the
+// by-distance correlation arrays accumulated per measurement
+#define DQMC_TD_SCALARS 8  // charge, spin x, y, z (at q), s, extended s, d pairing, current
+#define DQMC_TD_KINDS 5    // by-distance arrays: charge, spin x, y, z, on-site pairing
+// Offsets (in doubles) of a chain's time-displaced buffer: pair slots (n^2
+// int32), q phases (cos, sin), form-factor bonds (a, b, F), current entries
+// (r, s, re, im), the four physical Green's functions G(0,0), G(0,l), G(l,0),
+// G(l,l), the by-distance sums of one measurement (5 P), and the log binners
+// (header, then DQMC_TD_SCALARS + 5 P binners of DQMC_MEAS_LEVELS levels).
+struct TdLayout {
+    size_t slot, q, form, cur, g, stage, acc, total;
+};
+#ifdef __CUDACC__
+__host__ __device__
+#endif
+inline TdLayout td_layout(int n, int nf, int P, int nform, int ncur) {
+    TdLayout L;
+    size_t o = 0;
+    L.slot = o; o += ((size_t)n * n + 1) / 2;
+    L.q = o; o += 2 * (size_t)n;
+    L.form = o; o += 3 * (size_t)nform;
+    L.cur = o; o += 4 * (size_t)ncur;
+    L.g = o; o += 4 * (size_t)nf * n * n;
+    L.stage = o; o += (size_t)DQMC_TD_KINDS * P;
+    L.acc = o;
+    o += DQMC_MEAS_HEADER +
+         (size_t)(DQMC_TD_SCALARS + DQMC_TD_KINDS * (size_t)P) * DQMC_MEAS_LEVELS * DQMC_MEAS_BIN_WORDS;
+    L.total = o;
+    return L;
+}
+
 enum { DQMC_PHASE_SWEEP_SPATIAL = 0, DQMC_PHASE_WRAP = 1, DQMC_PHASE_SLICE_CHAIN = 2,
        DQMC_PHASE_UDT = 3, DQMC_PHASE_GREENS = 4, DQMC_PHASE_PROP_CHECK = 5,
        DQMC_PHASE_T_UPDATE = 6, DQMC_PHASE_OTHER = 7 };
@@ -166,7 +209,8 @@ enum { DQMC_OP_SWEEP = 0, DQMC_OP_BUILD = 1, DQMC_OP_GREENS_AT = 2, DQMC_OP_PHYS
        DQMC_OP_RUN = 7 /* time-sliced: arg0 = budget in microseconds */,
        DQMC_OP_GLOBAL = 8 /* arg0: 0 GlobalFlip, 1 GlobalShuffle */,
        DQMC_OP_REPLICA_WEIGHT = 9, DQMC_OP_REPLICA_ACCEPT = 10,
-       DQMC_OP_GREENS_KL = 11 /* arg0 = number of (k, l) pairs */ };
+       DQMC_OP_GREENS_KL = 11 /* arg0 = number of (k, l) pairs */,
+       DQMC_OP_TD_MEASURE = 12 };
 
 // doubles of a chain's unequal-time workspace: forward and backward U, T
 // ((nr + 1) each) and inverse U, T (nr each) of nf*n*n, their D vectors, and

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "../../include/dqmc_gb300.h"
 #include "dqmc_device.cuh"
 #include "dqmc_tc.cuh"
 
@@ -48,9 +49,15 @@ static_assert(sizeof(double) * 2 * 16 * 64 + sizeof(double) * 2 * 64 * 65 >= DQM
 // tensor products are enabled, and the launch has the whole arena (then
 // `tiles` + `arena` hold mm_tc's staging).
 #define DQMC_TC_NMIN 96
+// the tensor-core products are compiled only into the tensor-core build of
+// the chain kernel (dqmc_kernels_tc.cu)
+#ifndef DQMC_TC_BUILD
+#define DQMC_TC_BUILD 0
+#endif
+#define DQMC_TC_COMPILED DQMC_TC_BUILD
 __device__ __forceinline__ bool tc_eligible(const DqmcChain& c, int arena_cap) {
-    return c.prec == DQMC_PREC_MIXED_ID && !c.cplx && !c.cb && c.tc_enable && c.n >= DQMC_TC_NMIN &&
-           c.n <= DQMC_TC_NMAX && arena_cap >= 2 * 64 * 65;
+    return c.prec == DQMC_PREC_MIXED_ID && !c.cplx && !c.cb && c.tc_enable && c.tcs &&
+           c.n >= DQMC_TC_NMIN && c.n <= DQMC_TC_NMAX && arena_cap >= 2 * 64 * 65;
 }
 __device__ __forceinline__ unsigned char* tc_stage(Smem* s) {
     return reinterpret_cast<unsigned char*>(s->tiles);
@@ -78,12 +85,7 @@ __device__ __forceinline__ double* blk(double* p, const Ctx& x, int b) { return 
 __device__ __forceinline__ bool df_mode(const Ctx& x) {
     return x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 32 && !x.c->cb && !x.c->cplx;
 }
-#ifndef DQMC_DF_GLOBAL
-#define DQMC_DF_GLOBAL 0
-#endif
-__device__ __forceinline__ bool df_global_possible(const Ctx& x) {
-    return DQMC_DF_GLOBAL && df_mode(x) && x.n > 64;
-}
+__device__ __forceinline__ bool df_global_possible(const Ctx& x) { return df_mode(x) && x.n > 64; }
 __device__ __forceinline__ bool g_resident_possible(const Ctx& x) {
     return (x.n <= 64 && (size_t)x.nf * x.nn <= (size_t)x.s->arena_cap) || df_global_possible(x);
 }
@@ -185,16 +187,15 @@ __device__ __forceinline__ void tc_failed(const Ctx& x) {
 template <bool TA, bool TB>
 __device__ __forceinline__ void smm(const Ctx& x, bool wrap, double* C, const double* A,
                                     const double* B) {
-    (void)wrap;
     const DqmcChain& c = *x.c;
     if (c.prec == DQMC_PREC_MIXED_ID && x.n >= 48) {
         // the transposed operand is eT2 or eT2inv: take its float-pair split
-        if (x.s->tc_on) {
+        if (DQMC_TC_COMPILED && x.s->tc_on && (c.tc_enable & (wrap ? DQMC_TC_WRAPS : DQMC_TC_SLICES))) {
             const bool ok = TA ? mm_tc<true, false, false>(x.n, C, A == c.eT2 ? c.eT2df : c.eT2invdf,
-                                                          B, tc_stage(x.s), &x.s->tc)
+                                                          B, tc_stage(x.s), &x.s->tc, c.tcs)
                                : mm_tc<false, true, false>(x.n, C, A,
                                                            B == c.eT2 ? c.eT2df : c.eT2invdf,
-                                                           tc_stage(x.s), &x.s->tc);
+                                                           tc_stage(x.s), &x.s->tc, c.tcs);
             if (ok) return;
             tc_failed(x);
         }
@@ -361,8 +362,8 @@ __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* 
 // C = A B for double-float operands and result: tensor cores when the chain
 // has them, else the FP32-pipe product
 __device__ __forceinline__ void mm_df3(const Ctx& x, float2* C, const float2* A, const float2* B) {
-    if (x.s->tc_on) {
-        if (mm_tc<true, true, true>(x.n, C, A, B, tc_stage(x.s), &x.s->tc)) return;
+    if (DQMC_TC_COMPILED && x.s->tc_on && (x.c->tc_enable & DQMC_TC_WRAPS)) {
+        if (mm_tc<true, true, true>(x.n, C, A, B, tc_stage(x.s), &x.s->tc, x.c->tcs)) return;
         tc_failed(x);
     }
     mm_dfx<true, true, true>(x.n, C, A, B, x.s->tiles);
@@ -547,8 +548,9 @@ __device__ __noinline__ void add_slice_sequence_right(const Ctx& x, int idx) {
 template <bool TA, bool TB>
 __device__ __forceinline__ void rmm(const Ctx& x, double* C, const double* A, const double* B) {
     if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48 && !x.c->cplx && !x.c->cb) {
-        if (x.s->tc_on) {
-            if (mm_tc<false, false, false, TA, TB>(x.n, C, A, B, tc_stage(x.s), &x.s->tc)) return;
+        if (DQMC_TC_COMPILED && x.s->tc_on && (x.c->tc_enable & DQMC_TC_GREENS)) {
+            if (mm_tc<false, false, false, TA, TB>(x.n, C, A, B, tc_stage(x.s), &x.s->tc, x.c->tcs))
+                return;
             tc_failed(x);
         }
         mm_dfx<false, false, false, TA, TB>(x.n, C, A, B, x.s->tiles);
@@ -875,6 +877,61 @@ __device__ void flush_delayed(const Ctx& x, int p) {
         }
     }
     __syncthreads();
+}
+
+// flush_delayed for a mixed chain whose global G holds float pairs (n > 64):
+// G -= U W in double-float arithmetic on the FP32 pipe.  W's p rows are split
+// into float pairs once (in the arena, free on such chains), each thread keeps
+// the pairs of -U for its row in registers; per element the p products are
+// summed exactly-rounded in a float pair (TwoProd by fmaf, TwoSum) with the
+// cross terms in FP32, then added to G with one TwoSum: no FP64 instruction
+// beyond the O(p n) splits.
+__device__ void flush_delayed_df(const Ctx& x, int p) {
+    const int n = x.n;
+    float2* wdf = arena_df(x);  // p * n pairs <= 16 * 256 (32 KB of the arena)
+    for (int b = 0; b < x.nf; ++b) {
+        float2* g = gdf_ptr(x) + (size_t)b * x.nn;
+        const double* U = x.c->tmp2 + (size_t)b * x.nn;
+        const double* W = x.c->currU + (size_t)b * x.nn;
+        for (int e = threadIdx.x; e < p * n; e += DQMC_NT) wdf[e] = d_to_df(W[e]);
+        __syncthreads();
+        for (int k = threadIdx.x & 63; k < n; k += 64) {
+            float2 uk[DQMC_DELAY];
+#pragma unroll
+            for (int m = 0; m < DQMC_DELAY; ++m)
+                uk[m] = m < p ? d_to_df(-U[(size_t)m * n + k]) : make_float2(0.f, 0.f);
+            for (int l = threadIdx.x >> 6; l < n; l += DQMC_NT / 64) {
+                float sh = 0.f, sl = 0.f, xx = 0.f;
+#pragma unroll
+                for (int m = 0; m < DQMC_DELAY; ++m) {
+                    if (m < p) {
+                        const float2 w = wdf[(size_t)m * n + l];
+                        const float pr = __fmul_rn(uk[m].x, w.x);
+                        const float pe = __fmaf_rn(uk[m].x, w.x, -pr);
+                        const float t = __fadd_rn(sh, pr);
+                        const float z = __fsub_rn(t, sh);
+                        const float er = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(pr, z));
+                        sh = t;
+                        sl = __fadd_rn(sl, __fadd_rn(er, pe));
+                        xx = __fmaf_rn(uk[m].x, w.y, __fmaf_rn(uk[m].y, w.x, xx));
+                    }
+                }
+                const size_t at = (size_t)k + (size_t)l * n;
+                const float2 gv = g[at];
+                // (gv.x + gv.y) + (sh + (sl + xx)): TwoSum of the leading parts
+                const float s = __fadd_rn(gv.x, sh);
+                const float z = __fsub_rn(s, gv.x);
+                const float er = __fadd_rn(__fsub_rn(gv.x, __fsub_rn(s, z)), __fsub_rn(sh, z));
+                g[at] = df_norm(s, __fadd_rn(__fadd_rn(gv.y, __fadd_rn(sl, xx)), er));
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__device__ __forceinline__ void flush_pending(const Ctx& x, int p, bool df) {
+    if (df) flush_delayed_df(x, p);
+    else flush_delayed(x, p);
 }
 
 // sweep_spatial on a complex chain (local_updates.jl:23-60 with the complex
@@ -1204,7 +1261,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
         const int j = x.s->sxi[2 + (round & 1)];
         ++round;
         if (j >= n) {
-            if (pending > 0) flush_delayed(x, pending);
+            if (pending > 0) flush_pending(x, pending, dfg);
             break;
         }
         acc_count += 1;
@@ -1255,7 +1312,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
             ++pending;
             if (pending == kcap) {
                 __syncthreads();
-                flush_delayed(x, pending);
+                flush_pending(x, pending, dfg);
                 pending = 0;
             }
             i = j + 1;
@@ -1621,11 +1678,21 @@ __device__ __noinline__ void measure(const Ctx& x) {
 }
 
 // end of a sweep: count it and measure at the measurement points
+__device__ void td_measure(const Ctx& x);
+
 __device__ void after_sweep(const Ctx& x) {
     if (threadIdx.x == 0) x.c->sweep += 1;
     __syncthreads();
     if (x.c->meas_enable && x.c->meas && x.c->meas_rate > 0 && x.c->sweep % x.c->meas_rate == 0)
         measure(x);
+    if (x.c->td_enable && x.c->td && x.c->ut && x.c->td_rate > 0 &&
+        x.c->sweep % x.c->td_rate == 0) {
+        // the unequal-time stack factors in the arena (n <= 64): G leaves it
+        const bool was_res = x.s->gres || x.s->gdfg;
+        if (was_res) g_to_global(x);
+        td_measure(x);
+        if (was_res) g_to_arena(x);
+    }
 }
 
 }  // namespace
@@ -1903,6 +1970,203 @@ __device__ __noinline__ void ut_full2(const Ctx& x, const UtView& s, int slice1,
 
 // OP_GREENS_KL: one stack build, then G(k, l) for each requested pair
 // (physical: the _greens! transform of the result, greens.jl:114-125)
+// ---- time-displaced measurements (TimeIntegral, generic.jl:337-366) ----------
+// For l = 0..M with the trapezoid weights w_l = (1/2 at l = 0, M; else 1) dtau,
+// from the physical G(0,0), G(0,l), G(l,0), G(l,l) of the UnequalTimeStack
+// (the reference's CombinedGreensIterator order), the Wick kernels per site
+// pair (i, j), X_b = delta_ij [l = 0] - G0l_b[j, i], Y_b = Gl0_b[i, j],
+// occupations o^l_b(i) = 1 - Gll_b[i, i], o^0_b(j) = 1 - G00_b[j, j]:
+//   charge   full_cdc_kernel   (charge_density.jl:65-112)
+//            sum_ab o^l_a(i) o^0_b(j) + sum_b X_b Y_b
+//   spin x,y full_sdc_x/y_kernel (spin_density.jl:100-169): X_0 Y_1 + X_1 Y_0
+//   spin z   full_sdc_z_kernel (spin_density.jl:182-227):
+//            (o^l_0 - o^l_1)(i) (o^0_0 - o^0_1)(j) + sum_b X_b Y_b
+//   pairing  pc_combined_kernel on site (pairing.jl:95-161): Y_0 Y_1 + X_1 X_0
+// (one flavour block stands for both spins: 4 o^l o^0 + 2 X Y, 2 X Y, Y^2 + X^2),
+// reduced by distance as EachSitePairByDistance does (slot of the pair, sum,
+// divided by the number of sites: lattice_iterators.jl:160-260,
+// generic.jl:434-461, 582-584) and as q-resolved susceptibilities
+// (1/n) sum_l w_l sum_ij (cos q r_i cos q r_j + sin sin) C(i, j); the pairing
+// susceptibility is the q = 0 sum.  Form-factor pairing (extended s, d):
+// (1/n) sum_l w_l [sum F_ab F_cd (Gl0_up[c,a] Gl0_dn[d,b] + X_up[c,a] X_dn[d,b])]
+// over the bonds (a, b), (c, d) of the form factor; current: (1/n) sum_l w_l
+// Re[T_l T_0 + E] with T_l = rep sum_b tr(A (I - Gll_b)), T_0 likewise with
+// G00, E = rep sum_b tr(A Gl0_b A X_b) for the sparse current operator A (rep
+// = 2 for one flavour block).  Each measurement's 8 susceptibilities and 5 P
+// by-distance values go into log binners (the layout of the equal-time ones).
+__device__ __noinline__ void td_contract(const Ctx& x, const TdLayout& L, bool at_zero, double w,
+                                         double* bd, double* sacc) {
+    const DqmcChain& c = *x.c;
+    const int n = x.n, nf = x.nf, P = c.td_P;
+    const size_t nn = x.nn;
+    const int* slot = reinterpret_cast<const int*>(c.td + L.slot);
+    const double* qc = c.td + L.q;
+    const double* qs = qc + n;
+    const double* G00 = c.td + L.g;
+    const double* G0l = G00 + nf * nn;
+    const double* Gl0 = G0l + nf * nn;
+    const double* Gll = Gl0 + nf * nn;
+    const int b1 = nf - 1;
+    for (int e = threadIdx.x; e < n * n; e += DQMC_NT) {
+        const int i = e % n, j = e / n;
+        const double id = (at_zero && i == j) ? 1.0 : 0.0;
+        const double X0 = id - G0l[(size_t)i * n + j], X1 = id - G0l[b1 * nn + (size_t)i * n + j];
+        const double Y0 = Gl0[e], Y1 = Gl0[b1 * nn + e];
+        const double ol0 = 1.0 - Gll[(size_t)i * n + i], ol1 = 1.0 - Gll[b1 * nn + (size_t)i * n + i];
+        const double o00 = 1.0 - G00[(size_t)j * n + j], o01 = 1.0 - G00[b1 * nn + (size_t)j * n + j];
+        double ch, sx, sz, pr;
+        if (nf == 2) {
+            const double ex = X0 * Y0 + X1 * Y1;
+            ch = (ol0 + ol1) * (o00 + o01) + ex;
+            sx = X0 * Y1 + X1 * Y0;
+            sz = (ol0 - ol1) * (o00 - o01) + ex;
+            pr = Y0 * Y1 + X1 * X0;
+        } else {
+            const double ex = X0 * Y0;
+            ch = 4.0 * ol0 * o00 + 2.0 * ex;
+            sx = 2.0 * ex;
+            sz = 2.0 * ex;
+            pr = Y0 * Y0 + X0 * X0;
+        }
+        const double ph = qc[i] * qc[j] + qs[i] * qs[j];
+        sacc[0] += w * ch * ph;
+        sacc[1] += w * sx * ph;
+        sacc[2] += w * sx * ph;
+        sacc[3] += w * sz * ph;
+        sacc[4] += w * pr;
+        const int sl = slot[e];
+        atomicAdd(&bd[sl], w * ch);
+        atomicAdd(&bd[P + sl], w * sx);
+        atomicAdd(&bd[2 * P + sl], w * sx);
+        atomicAdd(&bd[3 * P + sl], w * sz);
+        atomicAdd(&bd[4 * P + sl], w * pr);
+    }
+    // form-factor pairing: bonds of form f are entries [f0, f0 + nb) of the
+    // (a, b, F) list
+    const double* fl = c.td + L.form;
+    const int dn = nf - 1;
+    for (int f = 0; f < 2; ++f) {
+        const int f0 = f == 0 ? 0 : c.td_nform0, nb = f == 0 ? c.td_nform0 : c.td_nform1;
+        double t = 0.0;
+        for (int p = threadIdx.x; p < nb; p += DQMC_NT) {
+            const int a = (int)fl[3 * (f0 + p)], b = (int)fl[3 * (f0 + p) + 1];
+            const double Fab = fl[3 * (f0 + p) + 2];
+            double u = 0.0;
+            for (int q = 0; q < nb; ++q) {
+                const int cc = (int)fl[3 * (f0 + q)], d = (int)fl[3 * (f0 + q) + 1];
+                const double Fcd = fl[3 * (f0 + q) + 2];
+                const double xu = ((at_zero && cc == a) ? 1.0 : 0.0) - G0l[(size_t)a * n + cc];
+                const double xd = ((at_zero && d == b) ? 1.0 : 0.0) - G0l[dn * nn + (size_t)b * n + d];
+                u += Fcd * (Gl0[(size_t)a * n + cc] * Gl0[dn * nn + (size_t)b * n + d] + xu * xd);
+            }
+            t += Fab * u;
+        }
+        sacc[5 + f] += w * t;
+    }
+    // current: the trace terms need the whole sum before their product
+    const double* cl = c.td + L.cur;
+    const int nc = c.td_ncur;
+    const double rep = nf == 1 ? 2.0 : 1.0;
+    double tlr = 0.0, tli = 0.0, t0r = 0.0, t0i = 0.0, er = 0.0;
+    for (int p = threadIdx.x; p < nc; p += DQMC_NT) {
+        const int r = (int)cl[4 * p], s = (int)cl[4 * p + 1];
+        const double ar = cl[4 * p + 2], ai = cl[4 * p + 3];
+        for (int b = 0; b < nf; ++b) {
+            const double il = (r == s ? 1.0 : 0.0) - Gll[b * nn + (size_t)r * n + s];
+            const double i0 = (r == s ? 1.0 : 0.0) - G00[b * nn + (size_t)r * n + s];
+            tlr += ar * il;
+            tli += ai * il;
+            t0r += ar * i0;
+            t0i += ai * i0;
+            // sum_q A_p Gl0[s_p, r_q] A_q X[s_q, r_p]
+            for (int q = 0; q < nc; ++q) {
+                const int r2 = (int)cl[4 * q], s2 = (int)cl[4 * q + 1];
+                const double br = cl[4 * q + 2], bi = cl[4 * q + 3];
+                const double g = Gl0[b * nn + (size_t)r2 * n + s];
+                const double xx = ((at_zero && s2 == r) ? 1.0 : 0.0) - G0l[b * nn + (size_t)r * n + s2];
+                // Re[(ar + i ai)(br + i bi)] * g * xx
+                er += (ar * br - ai * bi) * g * xx;
+            }
+        }
+    }
+    // block sums of the trace terms (tiles are free here)
+    double* red = x.s->tiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double v4[4] = {tlr, tli, t0r, t0i};
+    for (int q = 0; q < 4; ++q) {
+        const double v = warp_sum(v4[q]);
+        if (lane == 0) red[q * DQMC_NW + warp] = v;
+    }
+    __syncthreads();
+    double T[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int q = 0; q < 4; ++q)
+        for (int ww = 0; ww < DQMC_NW; ++ww) T[q] += red[q * DQMC_NW + ww];
+    __syncthreads();
+    // Re[T_l T_0] once (thread 0), the exchange term from every thread
+    double cur = rep * er;
+    if (threadIdx.x == 0) cur += rep * rep * (T[0] * T[2] - T[1] * T[3]);
+    sacc[7] += w * cur;
+}
+
+__device__ __noinline__ void td_measure(const Ctx& x) {
+    DqmcChain& c = *x.c;
+    const int n = x.n, nf = x.nf, M = c.M, P = c.td_P;
+    const TdLayout L = td_layout(n, nf, P, c.td_nform0 + c.td_nform1, c.td_ncur);
+    const size_t ms = (size_t)nf * x.nn;
+    double* G00 = c.td + L.g;
+    double* G0l = G00 + ms;
+    double* Gl0 = G0l + ms;
+    double* Gll = Gl0 + ms;
+    const UtView s = ut_view(x);
+    ut_build(x, s);
+    ut_full1(x, s, 0, 0);
+    greens_physical(x, s.G, G00);
+    // by-distance sums of this measurement (global: the arena holds the
+    // unequal-time QR factorisations of small chains)
+    double* bd = c.td + L.stage;
+    fill(DQMC_TD_KINDS * P, bd, 0.0);
+    double sacc[DQMC_TD_SCALARS];
+    for (int q = 0; q < DQMC_TD_SCALARS; ++q) sacc[q] = 0.0;
+    __syncthreads();
+    for (int l = 0; l <= M; ++l) {
+        const double w = ((l == 0 || l == M) ? 0.5 : 1.0) * c.td_dtau;
+        if (l == 0) ut_full1(x, s, 0, 0);
+        else ut_full2(x, s, 0, l);
+        greens_physical(x, s.G, G0l);
+        ut_full1(x, s, l, 0);
+        greens_physical(x, s.G, Gl0);
+        ut_full1(x, s, l, l);
+        greens_physical(x, s.G, Gll);
+        __syncthreads();
+        td_contract(x, L, l == 0, w, bd, sacc);
+        __syncthreads();
+    }
+    // block sums of the susceptibilities
+    double* red = x.s->tiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int q = 0; q < DQMC_TD_SCALARS; ++q) {
+        const double v = warp_sum(sacc[q]);
+        if (lane == 0) red[q * DQMC_NW + warp] = v;
+    }
+    __syncthreads();
+    double* acc = c.td + L.acc;
+    const double inv_n = 1.0 / n;
+    // one binner per thread: the scalars first, then the by-distance values
+    for (int k = threadIdx.x; k < DQMC_TD_SCALARS + DQMC_TD_KINDS * P; k += DQMC_NT) {
+        double v;
+        if (k < DQMC_TD_SCALARS) {
+            v = 0.0;
+            for (int ww = 0; ww < DQMC_NW; ++ww) v += red[k * DQMC_NW + ww];
+        } else {
+            v = bd[k - DQMC_TD_SCALARS];
+        }
+        binner_push(acc, k, v * inv_n);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) acc[0] += 1.0;
+    __syncthreads();
+}
+
 __device__ __noinline__ void greens_kl(const Ctx& x, int npairs, bool physical) {
     const DqmcChain& c = *x.c;
     const UtView s = ut_view(x);

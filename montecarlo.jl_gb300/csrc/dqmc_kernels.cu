@@ -3,13 +3,31 @@
 // Green's function updates, wraps, slice-matrix chains, UDT stabilisation and
 // Green's function reconstruction -- for as many sweeps as requested, so a
 // whole batch of chains advances in one launch.
+//
+// The file is compiled twice: as is (DQMC_TC_BUILD 0, no tensor-core code:
+// the occupancy calculation of a kernel that contains tcgen05 instructions
+// allows one CTA per SM, while these kernels are built for two), and by
+// dqmc_kernels_tc.cu with DQMC_TC_BUILD 1, whose kernels run the products of
+// tensor-core-capable mixed chains on the tensor cores.  Each build's kernels
+// have internal linkage; the host entry points carry a _tc suffix in the
+// second.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#ifndef DQMC_TC_BUILD
+#define DQMC_TC_BUILD 0
+#endif
 #include "dqmc_chain_ops.cuh"
 #include "dqmc_kernels.h"
 
+#if DQMC_TC_BUILD
+#define DQMC_KERNEL_ENTRY(name) name##_tc
+#else
+#define DQMC_KERNEL_ENTRY(name) name
+#endif
+
 namespace dqmc {
+namespace {
 
 // MINB CTAs per SM: 2 in general (128 registers a thread); 4 for ensembles of
 // small lattices (n <= 32), whose chains are latency-bound and leave the
@@ -49,13 +67,24 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     // tensor-core products: one warp allocates the accumulators' TMEM columns
     // (two CTAs per SM at most, 2 x 256 of the SM's 512 columns) and thread 0
     // sets up the mbarriers; released after the operation
-    const bool use_tc = tc_eligible(s->c, arena_cap);
+    const bool use_tc = DQMC_TC_BUILD && tc_eligible(s->c, arena_cap);
+#if DQMC_TC_BUILD
+    // a CTA of this build that will not allocate TMEM gives up its allocation
+    // permit at once: an SM admits the next CTA of a kernel that may allocate
+    // TMEM only after the resident one has allocated or relinquished
+    if (!use_tc && (threadIdx.x >> 5) == 0)
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+#endif
     if (use_tc) {
+#if DQMC_TC_BUILD
         if ((threadIdx.x >> 5) == 0) tc_alloc(&s->tc.tmem, DQMC_TC_COLS);
+#endif
         if (threadIdx.x == 0) {
-            mbar_init(&s->tc.bar[0], 1);
-            mbar_init(&s->tc.bar[1], 1);
-            s->tc.phase[0] = s->tc.phase[1] = 0;
+            for (int b = 0; b < 2; ++b) {
+                mbar_init(&s->tc.full[b], 1);
+                mbar_init(&s->tc.mma[b], 1);
+                s->tc.ph_full[b] = s->tc.ph_mma[b] = 0;
+            }
             s->tc.status = 0;
             asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
         }
@@ -155,6 +184,9 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     case DQMC_OP_REPLICA_ACCEPT:
         if (s->c.partner >= 0) replica_accept(x, chains, (int)blockIdx.x);
         break;
+    case DQMC_OP_TD_MEASURE:  // chains without time-displaced measurements skip
+        if (s->c.td && s->c.ut) td_measure(x);
+        break;
     case DQMC_OP_GREENS_KL:
         if (s->c.ut && s->c.ut_pairs && s->c.ut_out) greens_kl(x, arg0, arg1 != 0);
         else if (threadIdx.x == 0) s->c.status = 1;
@@ -168,7 +200,9 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
         tc_fence_before();
         __syncthreads();
         tc_fence_after();
+#if DQMC_TC_BUILD
         if ((threadIdx.x >> 5) == 0) tc_dealloc(s->tc.tmem, DQMC_TC_COLS);
+#endif
     }
     // write back the mutable state
     if (threadIdx.x == 0) {
@@ -208,13 +242,16 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     }
 }
 
+}  // namespace
 }  // namespace dqmc
 
+#if !DQMC_TC_BUILD
 size_t dqmc_chain_kernel_smem() { return sizeof(dqmc::Smem); }
+#endif
 
 static bool g_attr_set[64] = {};
 
-cudaError_t dqmc_prepare_chain_kernel() {
+cudaError_t DQMC_KERNEL_ENTRY(dqmc_prepare_chain_kernel)() {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
@@ -226,15 +263,26 @@ cudaError_t dqmc_prepare_chain_kernel() {
             e = cudaFuncSetAttribute(dqmc::chain_kernel<4>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)sizeof(dqmc::Smem));
+        // the whole unified L1 / shared array as shared memory: two CTAs of
+        // ~97 KB per SM need more than the smaller carve-outs leave
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dqmc::chain_kernel<2>,
+                                     cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(dqmc::chain_kernel<4>,
+                                     cudaFuncAttributePreferredSharedMemoryCarveout,
+                                     cudaSharedmemCarveoutMaxShared);
         if (e != cudaSuccess) return e;
         g_attr_set[dev] = true;
     }
     return cudaSuccess;
 }
 
-cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
-                                     cudaStream_t stream, int n_max) {
-    cudaError_t e = dqmc_prepare_chain_kernel();
+cudaError_t DQMC_KERNEL_ENTRY(dqmc_launch_chain_kernel)(DqmcChain* d_chains, int nchains, int op,
+                                                        int arg0, int arg1, cudaStream_t stream,
+                                                        int n_max) {
+    cudaError_t e = DQMC_KERNEL_ENTRY(dqmc_prepare_chain_kernel)();
     if (e != cudaSuccess) return e;
     // arena the chains need: 2 n (n + 1) doubles for the largest n <= 64
     // (n_max <= 0: unknown, e.g. a pool whose chains change between replays:
@@ -250,3 +298,15 @@ cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, i
                                                                   arg1, cap);
     return cudaGetLastError();
 }
+
+#if !DQMC_TC_BUILD
+cudaError_t dqmc_prepare_chain_kernels() {
+    cudaError_t e = dqmc_prepare_chain_kernel();
+    return e == cudaSuccess ? dqmc_prepare_chain_kernel_tc() : e;
+}
+cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
+                                     cudaStream_t stream, int n_max, bool tc) {
+    return tc ? dqmc_launch_chain_kernel_tc(d_chains, nchains, op, arg0, arg1, stream, n_max)
+              : dqmc_launch_chain_kernel(d_chains, nchains, op, arg0, arg1, stream, n_max);
+}
+#endif

@@ -844,7 +844,7 @@ __global__ void __launch_bounds__(32 * WPC, MINB)
 
 bool dqmc_warp_kernel_eligible(const DqmcChain& d) {
     return !d.active || (d.n <= 32 && d.prec == DQMC_PREC_FP64_ID && !d.cplx && !d.cb &&
-                         d.global_kind < 0 && !d.meas_enable);
+                         d.global_kind < 0 && !d.meas_enable && !d.td_enable);
 }
 
 cudaError_t dqmc_launch_warp_kernel(DqmcChain* d_chains, int nchains, int nsweeps,

@@ -45,13 +45,20 @@ class DQMC:
     ``recording_rate``, which defaults to ``measure_rate``; ``False``: record
     nothing, the reference's Discarder) receives the field configuration after
     every recorded sweep past thermalisation (DQMC.jl:41, 216).
+    ``time_displaced`` (default False) adds the TimeIntegral measurements on
+    the device after every ``measure_rate``-th sweep past thermalisation:
+    charge, spin x / y / z (at ``structure_factor_q``) and pairing (on site,
+    extended s, d) susceptibilities, the current-current susceptibility along
+    ``current_direction``, and the by-distance correlation arrays (see
+    ``time_displaced_observables``).
     """
 
     def __init__(self, model, *, seed: int = -1, field=None, measurements=None,
                  thermalization_measurements=None, last_sweep: int = 0, measure_rate: int = 10,
                  precision: str = "fp64", device: int = 0, device_measurements: bool = True,
                  structure_factor_q=None, global_update=None, recorder=None,
-                 recording_rate: int = None, **kwargs):
+                 recording_rate: int = None, time_displaced: bool = False,
+                 current_direction=None, **kwargs):
         self.model = model
         self.parameters = DQMCParameters.make(measure_rate=measure_rate, **kwargs)
         fcls = field if field is not None else model.choose_field()
@@ -100,6 +107,12 @@ class DQMC:
         # an empty recorder is falsy (len 0): test for the Discarder spelling
         self.recorder = None if recorder is False else recorder
         self._restore_record = None
+        self.time_displaced = time_displaced and not self.field.is_complex
+        self._td_arrays = None
+        if self.time_displaced:
+            from .measurements import td_arrays
+            self._td_arrays = td_arrays(model, q=structure_factor_q,
+                                        current_direction=current_direction)
 
     # -- stack --------------------------------------------------------------
     def init(self):
@@ -213,7 +226,7 @@ class DQMC:
                     stops.append(self.recorder.rate - (self.last_sweep % self.recorder.rate))
                 k = min(stops)
             k = max(1, min(k, total - self.last_sweep, self.max_sweeps_per_launch))
-            if self.device_measurements:
+            if self.device_measurements or self.time_displaced:
                 self._device_measure(self.last_sweep >= th)
             self.handle.sweep(k)
             self.last_sweep += k
@@ -263,10 +276,25 @@ class DQMC:
         multiple of ``measure_rate`` while on."""
         if self._dev_meas_on is on:
             return
-        self.handle.set_measurements(0, enable=on, rate=self.parameters.measure_rate,
-                                     greens=True, sweep=self.last_sweep, U=self.model.U,
-                                     q=self._q_phases)
+        if self.device_measurements:
+            self.handle.set_measurements(0, enable=on, rate=self.parameters.measure_rate,
+                                         greens=True, sweep=self.last_sweep, U=self.model.U,
+                                         q=self._q_phases)
+        if self.time_displaced:
+            self.handle.set_td_measurements(0, self._td_arrays, self.parameters.delta_tau,
+                                            enable=on, rate=self.parameters.measure_rate,
+                                            sweep=self.last_sweep)
         self._dev_meas_on = on
+
+    def time_displaced_observables(self):
+        """The device time-displaced measurements (``time_displaced=True``):
+        ``(mean, error)`` per susceptibility, ``by_distance`` (kind, slot)
+        means and errors of the charge, spin x / y / z and on-site pairing
+        correlations (the reference's EachSitePairByDistance arrays,
+        (Ndir, B, B) column-major per kind), and the number of measurements."""
+        if not self.time_displaced:
+            raise ValueError("time-displaced measurements were not requested (time_displaced=True)")
+        return self.handle.td_measurements(0, self._td_arrays["n_slots"])
 
     def observables(self):
         """The on-device equal-time measurements: ``(mean, error)`` of the

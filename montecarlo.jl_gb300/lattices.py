@@ -80,6 +80,38 @@ class Lattice:
             self._bonds = out
         return self._bonds
 
+    def n_bravais(self) -> int:
+        return int(math.prod(self.Ls))
+
+    def pair_distance_index(self):
+        """Slot of every site pair (src, trg) in the by-distance arrays of the
+        reference's EachSitePairByDistance (lattice_iterators.jl:160-168,
+        generic.jl:434-461): output shape (Ndir, B, B) column-major with
+        Ndir = Bravais sites, B = basis sites; the direction of a pair is the
+        Bravais shift from src's cell to trg's, per dimension (trg - src) mod L
+        flattened like _sub2ind (the Bravais dir2srctrg, lattice_cache.jl:
+        226-242).  Returns an (n, n) int array, 0-based slots, [src, trg]."""
+        import numpy as np
+
+        nb, B = self.n_bravais(), len(self.unitcell.sites)
+        n = nb * B
+        coords = np.zeros((nb, len(self.Ls)), dtype=np.int64)
+        for idx in range(nb):
+            rem = idx
+            for d, L in enumerate(self.Ls):
+                coords[idx, d] = rem % L
+                rem //= L
+        shift = np.zeros((nb, nb), dtype=np.int64)
+        stride = 1
+        for d, L in enumerate(self.Ls):
+            shift += ((coords[None, :, d] - coords[:, None, d]) % L) * stride
+            stride *= L
+        out = np.zeros((n, n), dtype=np.int32)
+        for b1 in range(B):
+            for b2 in range(B):
+                out[b1 * nb:(b1 + 1) * nb, b2 * nb:(b2 + 1) * nb] = shift + nb * (b1 + B * b2)
+        return out
+
     def positions(self):
         """Real-space site positions (n x dim), used for Fourier sums."""
         import numpy as np

@@ -250,6 +250,48 @@ def bilinear_correlation(A, B, G00, G0l, Gl0, Gll, at_zero):
     return t1 * t2 + ex
 
 
+def td_arrays(model, q=None, current_direction=None):
+    """Inputs of the device time-displaced measurements for ``model``'s
+    lattice: the by-distance slot of every site pair (src + n trg order, the
+    reference's EachSitePairByDistance), cos / sin (q . r_i) (q defaults to
+    (pi, pi, ...)), the extended-s and d pair form factors as (a, b, F) bond
+    lists (lattices with at least two lattice vectors) and the uniform
+    current operator along ``current_direction`` as (r, s, A_rs) entries."""
+    lat = model.l
+    n = len(lat)
+    slot = lat.pair_distance_index()
+    pos = lat.positions()
+    qv = np.full(pos.shape[1], np.pi) if q is None else np.asarray(q, dtype=float)
+    ph = pos @ qv
+    sites, vals, nform = [], [], [0, 0]
+    if len(lat.unitcell.lattice_vectors) >= 2:
+        for f, kind in enumerate(("s*", "d")):
+            F = pair_form_factor(lat, kind)
+            a, b = np.nonzero(F)
+            sites += [np.stack([a, b], axis=1).ravel()]
+            vals += [F[a, b]]
+            nform[f] = len(a)
+    A = current_operator(model.hopping_matrix(), lat, current_direction)
+    r, c = np.nonzero(A)
+    return {"n_slots": int(slot.max()) + 1, "pair_slot": slot.ravel(order="F"),
+            "q_cos": np.cos(ph), "q_sin": np.sin(ph), "n_form": nform,
+            "form_sites": np.concatenate(sites) if sites else None,
+            "form_values": np.concatenate(vals) if vals else None,
+            "n_current": len(r),
+            "current_sites": np.stack([r, c], axis=1).ravel() if len(r) else None,
+            "current_values": np.stack([A[r, c].real, A[r, c].imag], axis=1).ravel()
+            if len(r) else None, "n_sites": n}
+
+
+def by_distance(C, slot, n_slots):
+    """The reference's EachSitePairByDistance reduction of a correlation
+    matrix C[src, trg]: sum over the pairs of every slot, divided by the
+    number of sites (generic.jl:434-461, 582-584)."""
+    out = np.zeros(n_slots)
+    np.add.at(out, np.asarray(slot).ravel(), np.asarray(C).ravel())
+    return out / C.shape[0]
+
+
 def susceptibilities(greens_by_l, phases, delta_tau, kinds=CORRELATIONS, current=None,
                      pair_fields=None):
     """chi_K(q) = (1/n) sum_l w_l sum_ij e^{i q (r_i - r_j)} C_K(i, j; l dtau)

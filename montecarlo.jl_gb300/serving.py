@@ -62,10 +62,20 @@ class Result:
     block_latencies: List[float] = field(default_factory=list)
 
 
-def request_config(req: Request):
-    """Chain configuration and hopping exponentials of a request."""
+def request_config(req: Request, precision=None, tol=None):
+    """Chain configuration and hopping exponentials of a request.  With a
+    propagation-error bound ``tol``, a safe_mult the autotuner already chose
+    for this kind of chain (same sites, slices, |U|, mu, field, precision and
+    bound) replaces the request's own."""
     model = req.model()
-    param = DQMCParameters.make(beta=req.beta, delta_tau=req.delta_tau, safe_mult=req.safe_mult)
+    k = req.safe_mult
+    if tol is not None and precision is not None:
+        from . import autotune
+        hit = autotune.cached(model, model.choose_field(), req.beta, req.delta_tau,
+                              precision=precision, tol=tol)
+        if hit is not None:
+            k = hit
+    param = DQMCParameters.make(beta=req.beta, delta_tau=req.delta_tau, safe_mult=k)
     fld = model.choose_field()(param, model)
     cfg = _lib.ChainConfig(len(model.l), fld.unique_flavors, param.slices, param.safe_mult,
                            fld.kind, 1, fld.alpha, req.seed)
@@ -92,11 +102,14 @@ class Server:
     """Serves requests from one pool with time-sliced launches."""
 
     def __init__(self, max_slots=304, budget_bytes=8 << 30, precision=_lib.PREC_FP64,
-                 quantum_us=20000, use_graph=True, device=0):
+                 quantum_us=20000, use_graph=True, device=0, tol=None):
         self.pool = _lib.Pool(max_slots, budget_bytes, precision=precision, device=device)
         self.quantum_us = quantum_us
         self.use_graph = use_graph
         self.precision = precision
+        # propagation-error bound: requests of kinds the autotuner has seen
+        # run at its safe_mult (autotune's cache)
+        self.tol = tol
 
     def close(self):
         self.pool.close()
@@ -118,7 +131,7 @@ class Server:
             # admission: every queued request that fits the slots and budget
             still = []
             for req in queue:
-                cfg, exps = request_config(req)
+                cfg, exps = request_config(req, self.precision, self.tol)
                 slot = self.pool.admit(cfg)
                 if slot is None:
                     still.append(req)

@@ -1,0 +1,85 @@
+"""Host-side logic without a GPU: the autotuner's cache and back-off, the
+serving path's reuse of cached choices, and the by-distance slots of the
+time-displaced measurements (the reference's EachSitePairByDistance)."""
+import numpy as np
+
+
+def test_autotune_back_off_and_cache(pkg):
+    from montecarlo_gb300 import autotune, _lib
+    m = pkg.HubbardModel(pkg.SquareLattice(6), U=5.5)
+    spec = [(m, m.choose_field(), 8.0, 0.1, 1)]
+    key = autotune.cache_key(m, m.choose_field(), 8.0, 0.1, _lib.PREC_MIXED, 1e-6)
+    autotune._CACHE.pop(key, None)
+    assert autotune.cached(m, m.choose_field(), 8.0, 0.1, _lib.PREC_MIXED, 1e-6) is None
+    ks, nb = autotune.back_off(spec, [10], [2e-6], tol=1e-6, precision=_lib.PREC_MIXED)
+    assert ks == [8] and nb == 1
+    assert autotune.cached(m, m.choose_field(), 8.0, 0.1, _lib.PREC_MIXED, 1e-6) == 8
+    # under the bound: unchanged
+    assert autotune.back_off(spec, [8], [5e-7], tol=1e-6, precision=_lib.PREC_MIXED) == ([8], 0)
+    assert autotune.lower(2) == 2 and autotune.lower(15) == 12
+    # a cached kind skips the probes entirely (no device needed)
+    ks, errs = autotune.tune_safe_mult(spec, tol=1e-6, precision=_lib.PREC_MIXED)
+    assert ks == [8] and np.isnan(errs[0])
+    autotune._CACHE.pop(key, None)
+
+
+def test_serving_reuses_cached_safe_mult(pkg):
+    from montecarlo_gb300 import autotune, serving, _lib
+    req = serving.Request(0, "square", 6, -4.0, 4.0, 100, 7)  # physics U = -4: U_ref = 4
+    m = req.model()
+    key = autotune.cache_key(m, m.choose_field(), 4.0, 0.1, _lib.PREC_MIXED, 1e-6)
+    autotune._CACHE[key] = 5
+    cfg, _ = serving.request_config(req, _lib.PREC_MIXED, 1e-6)
+    assert cfg.safe_mult == 5
+    cfg, _ = serving.request_config(req)  # no bound: the request's own
+    assert cfg.safe_mult == req.safe_mult
+    autotune._CACHE.pop(key, None)
+
+
+def _brute_slots(lat):
+    """Slot of (src, trg): Bravais shift of trg's cell from src's, per
+    dimension mod L, flattened like _sub2ind, plus the basis pair."""
+    nb, B = lat.n_bravais(), len(lat.unitcell.sites)
+    n = nb * B
+    out = np.zeros((n, n), dtype=int)
+    for src in range(n):
+        for trg in range(n):
+            b1, i1 = divmod(src, nb)
+            b2, i2 = divmod(trg, nb)
+            shift, stride, r1, r2 = 0, 1, i1, i2
+            for L in lat.Ls:
+                shift += ((r2 % L - r1 % L) % L) * stride
+                stride *= L
+                r1 //= L
+                r2 //= L
+            out[src, trg] = shift + nb * (b1 + B * b2)
+    return out
+
+
+def test_pair_distance_index(pkg):
+    for lat in (pkg.SquareLattice(4), pkg.Honeycomb(3), pkg.Chain(5), pkg.CubicLattice(2)):
+        P = lat.pair_distance_index()
+        assert np.array_equal(P, _brute_slots(lat))
+        # every slot of a Bravais shift and basis pair holds one pair per cell
+        counts = np.bincount(P.ravel())
+        assert np.all(counts == lat.n_bravais())
+
+
+def test_by_distance_sums_translation_invariant_correlation(pkg):
+    lat = pkg.SquareLattice(4)
+    P = lat.pair_distance_index()
+    rng = np.random.default_rng(3)
+    f = rng.normal(size=P.max() + 1)
+    C = f[P]  # a correlation that depends on the displacement only
+    bd = pkg.by_distance(C, P, P.max() + 1)
+    assert np.allclose(bd, f)  # sum over n pairs / n sites
+
+
+def test_td_arrays_square(pkg):
+    m = pkg.HubbardModel(pkg.SquareLattice(4), U=-4.0)
+    a = pkg.td_arrays(m)
+    n = len(m.l)
+    assert a["n_slots"] == 16 and a["pair_slot"].shape == (n * n,)
+    assert a["n_form"] == [64, 64]  # directed nearest-neighbour bonds
+    assert a["n_current"] == 32     # bonds along +x, two entries each
+    assert np.allclose(a["q_cos"] ** 2 + a["q_sin"] ** 2, 1.0)
