@@ -10,7 +10,7 @@ One step = one sweep (2M slice visits x N proposals, with wraps and
 stabilisations) of every chain in one launch; ``value`` is aggregate sweeps/s.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                  [--workload c2|c1|c4] [--chains B]
+                  [--workload c2|c1|c4|l12] [--chains B]
 
 ``--impl reference`` times the CPU restatement of the reference's algorithm
 (the oracle; the reference itself is Julia, which this machine cannot run) on
@@ -46,6 +46,9 @@ WORKLOADS = {
     "c1": (4, 4.0, 4.0, 10, "DensityHirschField",
            "4x4 square attractive Hubbard U=-4 (physics), mu=0, DensityHirschField, beta=4, "
            "dtau=0.1 (M=40), safe_mult=10, FP64"),
+    "l12": (12, -4.0, 8.0, 10, "MagneticHirschField",
+            "12x12 square repulsive Hubbard U=4 (physics), mu=0, MagneticHirschField, beta=8, "
+            "dtau=0.1 (M=80), safe_mult=10"),
     "c4": (16, -4.0, 10.0, 10, "MagneticHirschField",
            "16x16 square repulsive Hubbard U=4 (physics), mu=0, MagneticHirschField, beta=10, "
            "dtau=0.1 (M=100), safe_mult=10, FP64"),

@@ -102,6 +102,7 @@ __device__ __forceinline__ float2* gdf_ptr(const Ctx& x) {
 // the resident G (either form) as FP64 into dst (dst may be G's own global
 // buffer: element e is read before it is written, by the same thread)
 __device__ void g_resident_to(const Ctx& x, double* dst) {
+    if (!x.s->gres && !x.s->gdfg) return;  // G is in global memory as FP64 already
     if (df_mode(x)) {
         const float2* a = gdf_ptr(x);
         for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) dst[e] = df_to_d(a[e]);
@@ -145,7 +146,7 @@ __device__ __forceinline__ void udt_one(const Ctx& x, double* U, double* D, doub
                      x.s->arena, x.s->arena + x.n * (x.n + 1), x.s->sv, x.s->sxd);
     else
         udt_pivot(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
-                  blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->sxi);
+                  blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->sxi, x.s->tiles);
 }
 
 
@@ -372,13 +373,14 @@ __device__ __forceinline__ void mm_df3(const Ctx& x, float2* C, const float2* A,
 // wrap_greens! of the resident double-float G of a mixed chain: the same
 // four slice-matrix steps with double-float diagonals (exact float pairs of
 // the interaction exponentials) and double-float products; tmp1 holds the
-// float-pair intermediate.
+// float-pair intermediate.  The pairs of one flavour block's diagonal go into
+// `sv` (n <= DQMC_NMAX pairs; `sv` is used only by the stabilisations).
 __device__ __noinline__ void wrap_greens_df(const Ctx& x, int curr_slice, int direction) {
     const DqmcChain& c = *x.c;
     const int n = x.n;
     float2* G = gdf_ptr(x);
     float2* T = reinterpret_cast<float2*>(c.tmp1);
-    float2* ev = reinterpret_cast<float2*>(x.s->ev + DQMC_NMAX);  // beyond the nf*n FP64 entries
+    float2* d = reinterpret_cast<float2*>(x.s->sv);
     const int slice = direction == -1 ? curr_slice - 1 : curr_slice;
     for (int half = 0; half < 2; ++half) {
         // direction +1: B(l) G B(l)^-1 = eT2 (eV (G eV^-1)) eT2inv, as
@@ -386,13 +388,13 @@ __device__ __noinline__ void wrap_greens_df(const Ctx& x, int curr_slice, int di
         //   slice_inv_left then slice_right (stack.jl:319-357)
         const bool inverse = (direction == 1) ? (half == 1) : (half == 0);
         interaction_exp(x, slice, inverse);
-        for (int e = threadIdx.x; e < x.nf * n; e += DQMC_NT) ev[e] = d_to_df(x.s->ev[e]);
-        __syncthreads();
         const float2* hop = inverse ? c.eT2invdf : c.eT2df;
         for (int b = 0; b < x.nf; ++b) {
             float2* g = G + (size_t)b * x.nn;
             float2* t = T + (size_t)b * x.nn;
-            const float2* d = ev + b * n;
+            __syncthreads();  // the previous block's last reads of d are done
+            for (int i = threadIdx.x; i < n; i += DQMC_NT) d[i] = d_to_df(x.s->ev[b * n + i]);
+            __syncthreads();
             if (half == 0) {
                 if (direction == 1) {  // G <- eT2 * (eV * G)
                     dleft_df(n, t, d, g);

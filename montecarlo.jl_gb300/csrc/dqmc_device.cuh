@@ -314,108 +314,179 @@ __device__ __noinline__ void mm_dfx(int n, void* __restrict__ Cv, const void* __
     }
 }
 
-// udt_AVX_pivot! (UDT.jl:216-334) on one n x n block: Householder QR with
-// column pivoting (column norms recomputed every step, as indmaxcolumn does),
-// explicit Q by backward accumulation, D = |diag R| (0 -> 1), T = D^-1 R
-// pivoted (apply = true) or left unpivoted with the reflectors below the
-// diagonal (apply = false, consumed by rdivp).  scr: n*n scratch (apply only);
-// sv: n doubles of shared memory; sx: 2 shared doubles / ints.
+// udt_AVX_pivot! (UDT.jl:216-334) on one n x n block in global memory (the
+// blocks of n > 64 that do not fit shared memory): Householder QR with
+// column pivoting, explicit Q by backward accumulation, D = |diag R| (0 -> 1),
+// T = D^-1 R pivoted (apply = true) or left unpivoted with the reflectors
+// below the diagonal (apply = false, consumed by rdivp).  The column norms
+// that the reference recomputes every step (indmaxcolumn) are recomputed in
+// the reflector-application pass, which already holds every updated column
+// (the initial norms in a pass of their own), so each step reads the
+// trailing matrix once; the reflector is cached in shared memory (xs, n
+// doubles); a warp updates two columns per pass, their dot products and
+// norms reduced together.  scr: n*n scratch (apply only); sv: n doubles of
+// shared memory; sxd, sxi: 2 shared doubles / ints.
+__device__ __forceinline__ void warp_sum2(double& a, double& b) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+}
+
 __device__ __noinline__ void udt_pivot(int n, double* __restrict__ U, double* __restrict__ D,
                           double* __restrict__ In, int* __restrict__ piv, double* __restrict__ tau,
-                          bool apply, double* __restrict__ scr, double* sv, double* sxd, int* sxi) {
+                          bool apply, double* __restrict__ scr, double* sv, double* sxd, int* sxi,
+                          double* xs) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     for (int i = tid; i < n; i += DQMC_NT) piv[i] = i + 1;
+    // initial squared column norms
+    for (int col = warp; col < n; col += DQMC_NW) {
+        const double* x = In + (size_t)col * n;
+        double s0 = 0.0, s1 = 0.0;
+        int r = lane;
+        for (; r + 32 < n; r += 64) {
+            s0 = fma(x[r], x[r], s0);
+            s1 = fma(x[r + 32], x[r + 32], s1);
+        }
+        if (r < n) s0 = fma(x[r], x[r], s0);
+        const double v = warp_sum(s0 + s1);
+        if (lane == 0) sv[col] = v;
+    }
     __syncthreads();
     for (int j = 0; j < n; ++j) {
-        for (int col = j + warp; col < n; col += DQMC_NW) {
-            const double* x = In + (size_t)col * n;
-            double s = 0.0;
-            for (int r = j + lane; r < n; r += 32) s = fma(x[r], x[r], s);
-            s = warp_sum(s);
-            if (lane == 0) sv[col] = s;
-        }
-        __syncthreads();
         if (warp == 0) {
+            // indmaxcolumn: first column of maximal norm among j..n-1
             double best = -1.0;
             int bi = j;  // never out of range, also when every norm is NaN
             for (int col = j + lane; col < n; col += 32) {
-                double v = sv[col];
+                const double v = sv[col];
                 if (v > best) { best = v; bi = col; }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                double ob = __shfl_down_sync(0xffffffffu, best, o);
-                int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                const double ob = __shfl_down_sync(0xffffffffu, best, o);
+                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
             if (lane == 0) sxi[0] = bi;
         }
         __syncthreads();
         const int jm = sxi[0];
-        const double normu = sv[jm];
         if (jm != j) {
             double* a = In + (size_t)jm * n;
             double* b = In + (size_t)j * n;
             for (int r = tid; r < n; r += DQMC_NT) {
-                double t = a[r];
+                const double t = a[r];
                 a[r] = b[r];
                 b[r] = t;
             }
             if (tid == 0) {
-                int tp = piv[jm];
+                const int tp = piv[jm];
                 piv[jm] = piv[j];
                 piv[j] = tp;
+                const double tn = sv[jm];
+                sv[jm] = sv[j];
+                sv[j] = tn;
             }
             __syncthreads();
         }
-        // reflector! (UDT.jl:157-172)
+        // reflector! (UDT.jl:157-172); the scaled reflector into xs
         if (warp == 0) {
             double* x = In + (size_t)j * n;
+            const double normu = sv[j];
             double xi1 = x[j];
             double t = 0.0;
             if (normu != 0.0) {
-                double nu = copysign(sqrt(normu), xi1);
+                const double nu = copysign(sqrt(normu), xi1);
                 xi1 += nu;
-                __syncwarp();
-                for (int r = j + 1 + lane; r < n; r += 32) x[r] = x[r] / xi1;
+                for (int r = j + 1 + lane; r < n; r += 32) {
+                    const double v = x[r] / xi1;
+                    x[r] = v;
+                    xs[r] = v;
+                }
                 if (lane == 0) x[j] = -nu;
                 t = xi1 / nu;
+            } else {
+                for (int r = j + 1 + lane; r < n; r += 32) xs[r] = x[r];
             }
             if (lane == 0) { tau[j] = t; sxd[0] = t; }
         }
         __syncthreads();
-        // reflectorApply! (UDT.jl:53-70)
+        // reflectorApply! (UDT.jl:53-70) to columns j+1.., two per warp pass,
+        // and their squared norms below row j for the next step's pivot
         const double t = sxd[0];
-        const double* x = In + (size_t)j * n;
-        for (int col = j + 1 + warp; col < n; col += DQMC_NW) {
-            double* a = In + (size_t)col * n;
-            double aj = a[j];
-            double s = 0.0;
-            for (int r = j + 1 + lane; r < n; r += 32) s = fma(x[r], a[r], s);
-            s = warp_sum(s);
-            double vAj = t * (aj + s);
-            if (lane == 0) a[j] = aj - vAj;
-            for (int r = j + 1 + lane; r < n; r += 32) a[r] = fma(-x[r], vAj, a[r]);
+        for (int c0 = j + 1 + 2 * warp; c0 < n; c0 += 2 * DQMC_NW) {
+            const int c1 = c0 + 1;
+            const bool two = c1 < n;
+            double* a = In + (size_t)c0 * n;
+            double* b = In + (size_t)(two ? c1 : c0) * n;
+            double sa = 0.0, sb = 0.0;
+            for (int r = j + 1 + lane; r < n; r += 32) {
+                const double xr = xs[r];
+                sa = fma(xr, a[r], sa);
+                sb = fma(xr, b[r], sb);
+            }
+            warp_sum2(sa, sb);
+            const double aj = a[j], bj = b[j];
+            const double va = t * (aj + sa), vb = t * (bj + sb);
+            double qa = 0.0, qb = 0.0;
+            for (int r = j + 1 + lane; r < n; r += 32) {
+                const double xr = xs[r];
+                const double an = fma(-xr, va, a[r]);
+                a[r] = an;
+                qa = fma(an, an, qa);
+                if (two) {
+                    const double bn = fma(-xr, vb, b[r]);
+                    b[r] = bn;
+                    qb = fma(bn, bn, qb);
+                }
+            }
+            warp_sum2(qa, qb);
+            if (lane == 0) {
+                a[j] = aj - va;
+                sv[c0] = qa;
+                if (two) {
+                    b[j] = bj - vb;
+                    sv[c1] = qb;
+                }
+            }
         }
         __syncthreads();
     }
-    // Calculate Q (UDT.jl:272-289)
+    // Calculate Q (UDT.jl:272-289): U = H_0 ... H_{n-1} applied to I backwards
     ident(n, U);
     __syncthreads();
     if (tid == 0) U[(size_t)(n - 1) * n + (n - 1)] -= tau[n - 1];
     __syncthreads();
     for (int k = n - 2; k >= 0; --k) {
         const double* v = In + (size_t)k * n;
+        for (int r = k + 1 + tid; r < n; r += DQMC_NT) xs[r] = v[r];
+        __syncthreads();
         const double t = tau[k];
-        for (int col = k + warp; col < n; col += DQMC_NW) {
-            double* u = U + (size_t)col * n;
-            double uk = u[k];
-            double s = 0.0;
-            for (int r = k + 1 + lane; r < n; r += 32) s = fma(v[r], u[r], s);
-            s = warp_sum(s);
-            double vB = t * (uk + s);
-            if (lane == 0) u[k] = uk - vB;
-            for (int r = k + 1 + lane; r < n; r += 32) u[r] = fma(-v[r], vB, u[r]);
+        for (int c0 = k + 2 * warp; c0 < n; c0 += 2 * DQMC_NW) {
+            const int c1 = c0 + 1;
+            const bool two = c1 < n;
+            double* a = U + (size_t)c0 * n;
+            double* b = U + (size_t)(two ? c1 : c0) * n;
+            double sa = 0.0, sb = 0.0;
+            for (int r = k + 1 + lane; r < n; r += 32) {
+                const double xr = xs[r];
+                sa = fma(xr, a[r], sa);
+                sb = fma(xr, b[r], sb);
+            }
+            warp_sum2(sa, sb);
+            const double ak = a[k], bk = b[k];
+            const double va = t * (ak + sa), vb = t * (bk + sb);
+            for (int r = k + 1 + lane; r < n; r += 32) {
+                const double xr = xs[r];
+                a[r] = fma(-xr, va, a[r]);
+                if (two) b[r] = fma(-xr, vb, b[r]);
+            }
+            if (lane == 0) {
+                a[k] = ak - va;
+                if (two) b[k] = bk - vb;
+            }
         }
         __syncthreads();
     }

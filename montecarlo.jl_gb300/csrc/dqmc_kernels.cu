@@ -56,6 +56,8 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     if (threadIdx.x == 0) {
         s->Gglob = s->c.G;
         s->gres = 0;
+        s->gdfg = 0;
+        s->tc_on = 0;
         s->arena_cap = arena_cap;
     }
     __syncthreads();

@@ -60,6 +60,13 @@ __global__ void __launch_bounds__(DQMC_NT, 2)
         uint32_t* dst = reinterpret_cast<uint32_t*>(&s->c);
         for (int e = threadIdx.x; e < words; e += DQMC_NT) dst[e] = src[e];
     }
+    if (threadIdx.x == 0) {  // G stays in global memory; no tensor products here
+        s->Gglob = s->c.G;
+        s->gres = 0;
+        s->gdfg = 0;
+        s->tc_on = 0;
+        s->arena_cap = (int)(sizeof(s->arena) / sizeof(double));
+    }
     __syncthreads();
     dqmc::Ctx x;
     x.s = s;

@@ -111,3 +111,32 @@ def test_mixed_16x16_beta10_every_stabilisation(pkg, lib, oracle):
           f"vs FP64 GPU at every stabilisation {worst_fp64:.2e}")
     assert worst_oracle <= TOL_MIXED
     assert worst_fp64 <= TOL_MIXED
+
+
+@pytest.mark.parametrize("L", [12, 16])
+def test_mixed_two_flavour_honeycomb_large(pkg, lib, L):
+    """Two-flavour mixed chains with nf * n above 512 (honeycomb, n = 288 and
+    512; the largest lattices of the served stream): the double-float wraps
+    stage one flavour block's diagonal at a time.  A free sweep keeps the
+    propagation error and G within the bound of the FP64 path (itself pinned
+    to the oracle at 1e-10) for the chain's own configuration."""
+    model, param, fld, exps = make_setup(pkg, L=L, lattice="honeycomb", U=-4.0, beta=1.0,
+                                         safe_mult=5, field=pkg.MagneticHirschField)
+    assert fld.unique_flavors == 2 and len(model.l) == 2 * L * L
+    cfg = [chain_config(lib, model, param, fld, 9)]
+    hm = lib.Handle(cfg, precision=lib.PREC_MIXED)
+    hd = lib.Handle(cfg, precision=lib.PREC_FP64)
+    for h in (hm, hd):
+        h.set_hopping(-1, exps)
+        h.init_random_field(0)
+    hm.initialize_run()
+    st = hm.sweep(1)[0]
+    assert st["status"] == 0
+    assert st["max_propagation_error"] <= TOL_MIXED
+    assert st["accepted"] > 0
+    hd.set_field(0, hm.get_field(0))
+    d = maxdiff(hm.greens(0), hd.calculate_greens(0, st["current_slice"] - 1))
+    print(f"honeycomb L={L} (n={len(model.l)}) mixed vs FP64 max |dG| {d:.2e}")
+    assert d <= TOL_MIXED
+    hm.close()
+    hd.close()
