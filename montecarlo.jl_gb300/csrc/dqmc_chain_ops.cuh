@@ -144,9 +144,12 @@ __device__ __forceinline__ void udt_one(const Ctx& x, double* U, double* D, doub
     if (x.n <= 64)
         udt_pivot_sm(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
                      x.s->arena, x.s->arena + x.n * (x.n + 1), x.s->sv, x.s->sxd);
+    else if (x.c->prec == DQMC_PREC_MIXED_ID)  // norms downdated (see udt_pivot_g)
+        udt_pivot_g<true>(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
+                          blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->tiles);
     else
-        udt_pivot(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
-                  blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->sxi, x.s->tiles);
+        udt_pivot_g<false>(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
+                           blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->tiles);
 }
 
 

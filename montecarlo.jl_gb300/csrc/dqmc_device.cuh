@@ -315,179 +315,272 @@ __device__ __noinline__ void mm_dfx(int n, void* __restrict__ Cv, const void* __
 }
 
 // udt_AVX_pivot! (UDT.jl:216-334) on one n x n block in global memory (the
-// blocks of n > 64 that do not fit shared memory): Householder QR with
-// column pivoting, explicit Q by backward accumulation, D = |diag R| (0 -> 1),
-// T = D^-1 R pivoted (apply = true) or left unpivoted with the reflectors
-// below the diagonal (apply = false, consumed by rdivp).  The column norms
-// that the reference recomputes every step (indmaxcolumn) are recomputed in
-// the reflector-application pass, which already holds every updated column
-// (the initial norms in a pass of their own), so each step reads the
-// trailing matrix once; the reflector is cached in shared memory (xs, n
-// doubles); a warp updates two columns per pass, their dot products and
-// norms reduced together.  scr: n*n scratch (apply only); sv: n doubles of
-// shared memory; sxd, sxi: 2 shared doubles / ints.
-__device__ __forceinline__ void warp_sum2(double& a, double& b) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
+// blocks of n > 64 that do not fit shared memory; L2-resident): Householder
+// QR with column pivoting, explicit Q by backward accumulation, D = |diag R|
+// (0 -> 1), T = D^-1 R pivoted (apply = true) or left unpivoted with the
+// reflectors below the diagonal (apply = false, consumed by rdivp).
+//
+// Organised for GB300's narrow FP64 pipe (a warp's FP64 instruction costs the
+// pipe the same however few of its lanes do useful work):
+//  * per step, warp 0 alone finds the pivot (bit patterns of the squared
+//    norms compared on the integer pipe), swaps it in and forms the reflector
+//    (scaled by the reciprocal of xi1, a rounding-level difference from the
+//    division), staged in shared memory `xs`; one barrier;
+//  * every warp then applies it to eight trailing columns at a time with four
+//    lanes per column (rows interleaved by four from a 4-aligned start, so a
+//    warp's load of one row quartet of eight columns touches eight whole
+//    32-byte sectors; two shuffles combine a column's dot product); second
+//    barrier.  Per column and row one FMA for the dot product, one for the
+//    update, and one for the next step's squared norm;
+//  * DOWNDATE (mixed-precision chains): the norms are downdated instead,
+//    ||a(j+1:n)||^2 = ||a(j:n)||^2 - a_j^2 (LAPACK xGEQP3 / xLAQPS, Quintana-
+//    Orti, Sun and Bischof 1998), and recomputed in the update pass only for
+//    columns where cancellation has reduced the downdated value below
+//    sqrt(eps) of the last recomputed one (warp-uniform: a pass recomputes
+//    when one of its eight columns needs it); the reflector's own norm is
+//    recomputed from its column.  Without DOWNDATE the norms are recomputed
+//    every step as the reference's indmaxcolumn does;
+//  * Q accumulates backwards with the same mapping; the next reflector is
+//    staged in the second half of `xs` during the current step, one barrier
+//    per step.
+// scr: n*n scratch (apply only); sv: n doubles of shared memory (squared
+// norms); sxd, sxi: shared scalars; xs: 2048 doubles of shared memory
+// (reflector buffers at 0 and 512, DOWNDATE reference norms at 1024).
+// Strided column kernels of udt_pivot_g: rows r, r + 4, r + 8, ... < n of a
+// column in global memory (L2), eight loads in flight per lane (four
+// accumulation chains), which the L2 latency of the two-die part needs to
+// keep the FP64 pipe fed.
+__device__ __forceinline__ double dot_s4(const double* __restrict__ x, const double* a, int r,
+                                         int n) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    for (; r + 28 < n; r += 32) {
+        const double a0 = a[r], a1 = a[r + 4], a2 = a[r + 8], a3 = a[r + 12];
+        const double a4 = a[r + 16], a5 = a[r + 20], a6 = a[r + 24], a7 = a[r + 28];
+        s0 = fma(x[r], a0, s0);
+        s1 = fma(x[r + 4], a1, s1);
+        s2 = fma(x[r + 8], a2, s2);
+        s3 = fma(x[r + 12], a3, s3);
+        s0 = fma(x[r + 16], a4, s0);
+        s1 = fma(x[r + 20], a5, s1);
+        s2 = fma(x[r + 24], a6, s2);
+        s3 = fma(x[r + 28], a7, s3);
     }
+    for (; r < n; r += 4) s0 = fma(x[r], a[r], s0);
+    return (s0 + s1) + (s2 + s3);
+}
+// a[r'] -= x[r'] v for the strided rows; with SQ, returns the sum of the new
+// values' squares
+template <bool SQ>
+__device__ __forceinline__ double axpy_s4(double* a, const double* __restrict__ x, double v, int r,
+                                          int n) {
+    double q0 = 0.0, q1 = 0.0, q2 = 0.0, q3 = 0.0;
+    for (; r + 28 < n; r += 32) {
+        double b[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) b[u] = a[r + 4 * u];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            b[u] = fma(-x[r + 4 * u], v, b[u]);
+            a[r + 4 * u] = b[u];
+        }
+        if (SQ) {
+            q0 = fma(b[0], b[0], q0);
+            q1 = fma(b[1], b[1], q1);
+            q2 = fma(b[2], b[2], q2);
+            q3 = fma(b[3], b[3], q3);
+            q0 = fma(b[4], b[4], q0);
+            q1 = fma(b[5], b[5], q1);
+            q2 = fma(b[6], b[6], q2);
+            q3 = fma(b[7], b[7], q3);
+        }
+    }
+    for (; r < n; r += 4) {
+        const double b = fma(-x[r], v, a[r]);
+        a[r] = b;
+        if (SQ) q0 = fma(b, b, q0);
+    }
+    return (q0 + q1) + (q2 + q3);
 }
 
-__device__ __noinline__ void udt_pivot(int n, double* __restrict__ U, double* __restrict__ D,
-                          double* __restrict__ In, int* __restrict__ piv, double* __restrict__ tau,
-                          bool apply, double* __restrict__ scr, double* sv, double* sxd, int* sxi,
-                          double* xs) {
+template <bool DOWNDATE>
+__device__ __noinline__ void udt_pivot_g(int n, double* __restrict__ U, double* __restrict__ D,
+                                         double* __restrict__ In, int* __restrict__ piv,
+                                         double* __restrict__ tau, bool apply,
+                                         double* __restrict__ scr, double* sv, double* sxd,
+                                         double* xs) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int h = lane >> 3, cl = lane & 7;  // row quarter, column within the group of eight
+    const double tol3z = 1.4901161193847656e-08;  // sqrt(2^-52)
+    double* sv2 = xs + 1024;
     for (int i = tid; i < n; i += DQMC_NT) piv[i] = i + 1;
     // initial squared column norms
-    for (int col = warp; col < n; col += DQMC_NW) {
-        const double* x = In + (size_t)col * n;
-        double s0 = 0.0, s1 = 0.0;
-        int r = lane;
-        for (; r + 32 < n; r += 64) {
-            s0 = fma(x[r], x[r], s0);
-            s1 = fma(x[r + 32], x[r + 32], s1);
+    for (int g = warp * 8; g < n; g += 8 * DQMC_NW) {
+        const int c = g + cl;
+        const bool act = c < n;
+        const double* a = In + (size_t)(act ? c : g) * n;
+        double q = act ? dot_s4(a, a, h, n) : 0.0;
+        q += __shfl_xor_sync(0xffffffffu, q, 8);
+        q += __shfl_xor_sync(0xffffffffu, q, 16);
+        if (act && h == 0) {
+            sv[c] = q;
+            if (DOWNDATE) sv2[c] = q;
         }
-        if (r < n) s0 = fma(x[r], x[r], s0);
-        const double v = warp_sum(s0 + s1);
-        if (lane == 0) sv[col] = v;
     }
     __syncthreads();
     for (int j = 0; j < n; ++j) {
+        const int rb = (j + 1) & ~3;  // first row of the aligned quartets below row j
         if (warp == 0) {
             // indmaxcolumn: first column of maximal norm among j..n-1
-            double best = -1.0;
+            long long best = -1;
             int bi = j;  // never out of range, also when every norm is NaN
             for (int col = j + lane; col < n; col += 32) {
-                const double v = sv[col];
+                const long long v = __double_as_longlong(sv[col]);
                 if (v > best) { best = v; bi = col; }
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
-                const double ob = __shfl_down_sync(0xffffffffu, best, o);
-                const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+                const long long ob = __shfl_xor_sync(0xffffffffu, best, o);
+                const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
                 if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
             }
-            if (lane == 0) sxi[0] = bi;
-        }
-        __syncthreads();
-        const int jm = sxi[0];
-        if (jm != j) {
-            double* a = In + (size_t)jm * n;
-            double* b = In + (size_t)j * n;
-            for (int r = tid; r < n; r += DQMC_NT) {
-                const double t = a[r];
-                a[r] = b[r];
-                b[r] = t;
-            }
-            if (tid == 0) {
-                const int tp = piv[jm];
-                piv[jm] = piv[j];
-                piv[j] = tp;
-                const double tn = sv[jm];
-                sv[jm] = sv[j];
-                sv[j] = tn;
-            }
-            __syncthreads();
-        }
-        // reflector! (UDT.jl:157-172); the scaled reflector into xs
-        if (warp == 0) {
+            const int jm = bi;
             double* x = In + (size_t)j * n;
-            const double normu = sv[j];
-            double xi1 = x[j];
+            if (jm != j) {
+                double* a = In + (size_t)jm * n;
+                for (int r = lane; r < n; r += 32) {
+                    const double t = a[r];
+                    a[r] = x[r];
+                    x[r] = t;
+                }
+                if (lane == 0) {
+                    const int tp = piv[jm];
+                    piv[jm] = piv[j];
+                    piv[j] = tp;
+                    sv[jm] = sv[j];
+                    if (DOWNDATE) sv2[jm] = sv2[j];
+                }
+            }
+            __syncwarp();
+            // reflector! (UDT.jl:157-172)
+            double normu = __longlong_as_double(best);
+            if (DOWNDATE) {
+                double s0 = 0.0, s1 = 0.0;
+                int r = j + lane;
+                for (; r + 32 < n; r += 64) {
+                    s0 = fma(x[r], x[r], s0);
+                    s1 = fma(x[r + 32], x[r + 32], s1);
+                }
+                if (r < n) s0 = fma(x[r], x[r], s0);
+                normu = warp_sum(s0 + s1);
+            }
+            const double xi1 = x[j];
             double t = 0.0;
             if (normu != 0.0) {
                 const double nu = copysign(sqrt(normu), xi1);
-                xi1 += nu;
+                const double xi = xi1 + nu;
+                const double inv = 1.0 / xi;
                 for (int r = j + 1 + lane; r < n; r += 32) {
-                    const double v = x[r] / xi1;
+                    const double v = x[r] * inv;
                     x[r] = v;
                     xs[r] = v;
                 }
                 if (lane == 0) x[j] = -nu;
-                t = xi1 / nu;
+                t = xi / nu;
             } else {
                 for (int r = j + 1 + lane; r < n; r += 32) xs[r] = x[r];
             }
+            // rows of the first quartet at or above row j take no part
+            if (lane < 4 && rb + lane <= j) xs[rb + lane] = 0.0;
             if (lane == 0) { tau[j] = t; sxd[0] = t; }
         }
         __syncthreads();
-        // reflectorApply! (UDT.jl:53-70) to columns j+1.., two per warp pass,
-        // and their squared norms below row j for the next step's pivot
+        // reflectorApply! (UDT.jl:53-70) to columns j+1..n-1 and their norms
         const double t = sxd[0];
-        for (int c0 = j + 1 + 2 * warp; c0 < n; c0 += 2 * DQMC_NW) {
-            const int c1 = c0 + 1;
-            const bool two = c1 < n;
-            double* a = In + (size_t)c0 * n;
-            double* b = In + (size_t)(two ? c1 : c0) * n;
-            double sa = 0.0, sb = 0.0;
-            for (int r = j + 1 + lane; r < n; r += 32) {
-                const double xr = xs[r];
-                sa = fma(xr, a[r], sa);
-                sb = fma(xr, b[r], sb);
+        for (int g = j + 1 + warp * 8; g < n; g += 8 * DQMC_NW) {
+            const int c = g + cl;
+            const bool act = c < n;
+            double* a = In + (size_t)(act ? c : g) * n;
+            double sdot = act ? dot_s4(xs, a, rb + h, n) : 0.0;
+            sdot += __shfl_xor_sync(0xffffffffu, sdot, 8);
+            sdot += __shfl_xor_sync(0xffffffffu, sdot, 16);
+            const double aj = act ? a[j] : 0.0;
+            const double vA = t * (aj + sdot);
+            const double ajn = aj - vA;
+            bool need = true;
+            double down = 0.0;
+            if (DOWNDATE) {
+                const double s1v = act ? sv[c] : 0.0;
+                down = fma(-ajn, ajn, s1v);
+                need = act && s1v != 0.0 && down <= tol3z * sv2[c];
+                if (s1v == 0.0) down = 0.0;
             }
-            warp_sum2(sa, sb);
-            const double aj = a[j], bj = b[j];
-            const double va = t * (aj + sa), vb = t * (bj + sb);
-            double qa = 0.0, qb = 0.0;
-            for (int r = j + 1 + lane; r < n; r += 32) {
-                const double xr = xs[r];
-                const double an = fma(-xr, va, a[r]);
-                a[r] = an;
-                qa = fma(an, an, qa);
-                if (two) {
-                    const double bn = fma(-xr, vb, b[r]);
-                    b[r] = bn;
-                    qb = fma(bn, bn, qb);
+            const bool norms = DOWNDATE ? __any_sync(0xffffffffu, need) : true;
+            double q = 0.0;
+            if (act) {
+                // first quartet: rows at or above j stay
+                const int r = rb + h;
+                if (r > j && r < n) {
+                    const double an = fma(-xs[r], vA, a[r]);
+                    a[r] = an;
+                    q = an * an;
                 }
+                if (norms) q += axpy_s4<true>(a, xs, vA, r + 4, n);
+                else axpy_s4<false>(a, xs, vA, r + 4, n);
             }
-            warp_sum2(qa, qb);
-            if (lane == 0) {
-                a[j] = aj - va;
-                sv[c0] = qa;
-                if (two) {
-                    b[j] = bj - vb;
-                    sv[c1] = qb;
+            if (norms) {
+                q += __shfl_xor_sync(0xffffffffu, q, 8);
+                q += __shfl_xor_sync(0xffffffffu, q, 16);
+            }
+            __syncwarp();  // every lane has read a[j] and sv[c]
+            if (act && h == 0) {
+                a[j] = ajn;
+                if (!DOWNDATE) {
+                    sv[c] = q;
+                } else if (need) {
+                    sv[c] = q;
+                    sv2[c] = q;
+                } else {
+                    sv[c] = down;
                 }
             }
         }
         __syncthreads();
     }
-    // Calculate Q (UDT.jl:272-289): U = H_0 ... H_{n-1} applied to I backwards
+    // Calculate Q (UDT.jl:272-289): U = H_0 ... H_{n-1} applied to I backwards;
+    // the reflector of step k is staged in xs + 512 (k & 1), zero in the rows
+    // of its first quartet at or above row k
+    auto stage = [&](int k) {
+        double* dst = xs + 512 * (k & 1);
+        const double* v = In + (size_t)k * n;
+        for (int r = (k & ~3) + tid; r < n; r += DQMC_NT) dst[r] = r > k ? v[r] : 0.0;
+    };
     ident(n, U);
+    if (n >= 2) stage(n - 2);
     __syncthreads();
     if (tid == 0) U[(size_t)(n - 1) * n + (n - 1)] -= tau[n - 1];
     __syncthreads();
     for (int k = n - 2; k >= 0; --k) {
-        const double* v = In + (size_t)k * n;
-        for (int r = k + 1 + tid; r < n; r += DQMC_NT) xs[r] = v[r];
-        __syncthreads();
+        const double* xv = xs + 512 * (k & 1);
+        const int rb = (k + 1) & ~3;
         const double t = tau[k];
-        for (int c0 = k + 2 * warp; c0 < n; c0 += 2 * DQMC_NW) {
-            const int c1 = c0 + 1;
-            const bool two = c1 < n;
-            double* a = U + (size_t)c0 * n;
-            double* b = U + (size_t)(two ? c1 : c0) * n;
-            double sa = 0.0, sb = 0.0;
-            for (int r = k + 1 + lane; r < n; r += 32) {
-                const double xr = xs[r];
-                sa = fma(xr, a[r], sa);
-                sb = fma(xr, b[r], sb);
+        for (int g = k + warp * 8; g < n; g += 8 * DQMC_NW) {
+            const int c = g + cl;
+            const bool act = c < n;
+            double* u = U + (size_t)(act ? c : g) * n;
+            double sdot = act ? dot_s4(xv, u, rb + h, n) : 0.0;
+            sdot += __shfl_xor_sync(0xffffffffu, sdot, 8);
+            sdot += __shfl_xor_sync(0xffffffffu, sdot, 16);
+            const double uk = act ? u[k] : 0.0;
+            const double vB = t * (uk + sdot);
+            if (act) {
+                const int r = rb + h;
+                if (r > k && r < n) u[r] = fma(-xv[r], vB, u[r]);
+                axpy_s4<false>(u, xv, vB, r + 4, n);
             }
-            warp_sum2(sa, sb);
-            const double ak = a[k], bk = b[k];
-            const double va = t * (ak + sa), vb = t * (bk + sb);
-            for (int r = k + 1 + lane; r < n; r += 32) {
-                const double xr = xs[r];
-                a[r] = fma(-xr, va, a[r]);
-                if (two) b[r] = fma(-xr, vb, b[r]);
-            }
-            if (lane == 0) {
-                a[k] = ak - va;
-                if (two) b[k] = bk - vb;
-            }
+            __syncwarp();  // every lane has read u[k]
+            if (act && h == 0) u[k] = uk - vB;
         }
+        if (k >= 1) stage(k - 1);
         __syncthreads();
     }
     // D (UDT.jl:293-301)
@@ -984,14 +1077,25 @@ __device__ __noinline__ void rdivp(int n, double* __restrict__ A, const double* 
         for (int j = 0; j < n; ++j) {
             const double* tj = T + (size_t)j * n;
             // two independent accumulation chains halve the dependent-FMA latency
-            double x0 = O[i + (size_t)j * n], x1 = 0.0;
+            // (eight loads of the row in flight, four accumulation chains)
+            double x0 = O[i + (size_t)j * n], x1 = 0.0, x2 = 0.0, x3 = 0.0;
+            const double* ai = A + i;
             int k = 0;
-            for (; k + 1 < j; k += 2) {
-                x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
-                x1 = fma(-A[i + (size_t)(k + 1) * n], tj[k + 1], x1);
+            for (; k + 7 < j; k += 8) {
+                double b[8];
+#pragma unroll
+                for (int u = 0; u < 8; ++u) b[u] = ai[(size_t)(k + u) * n];
+                x0 = fma(-b[0], tj[k], x0);
+                x1 = fma(-b[1], tj[k + 1], x1);
+                x2 = fma(-b[2], tj[k + 2], x2);
+                x3 = fma(-b[3], tj[k + 3], x3);
+                x0 = fma(-b[4], tj[k + 4], x0);
+                x1 = fma(-b[5], tj[k + 5], x1);
+                x2 = fma(-b[6], tj[k + 6], x2);
+                x3 = fma(-b[7], tj[k + 7], x3);
             }
-            if (k < j) x0 = fma(-A[i + (size_t)k * n], tj[k], x0);
-            A[i + (size_t)j * n] = (x0 + x1) * rcp[j];
+            for (; k < j; ++k) x0 = fma(-ai[(size_t)k * n], tj[k], x0);
+            A[i + (size_t)j * n] = ((x0 + x1) + (x2 + x3)) * rcp[j];
         }
     }
     __syncthreads();
