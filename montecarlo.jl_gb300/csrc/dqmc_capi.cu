@@ -157,6 +157,7 @@ struct dqmc_handle {
     std::map<size_t, size_t> free_blocks;  // offset -> bytes
     std::vector<size_t> slot_off, slot_bytes;
     DqmcChain* pinned = nullptr;           // pinned mirror for graph replays
+    unsigned int* d_sync = nullptr;        // pools: the launch's visit counters (DqmcChain::run_sync)
     int n_max = 0;                         // largest n_sites of a fixed handle's chains
     bool tc = false;                       // launches use the tensor-core kernel build
     bool small_kernel = true;              // sweeps of small chains one warp per chain
@@ -413,6 +414,7 @@ int dqmc_destroy(dqmc_handle* h) {
     if (h->d_chains) cudaFree(h->d_chains);
     if (h->graph) cudaGraphExecDestroy(h->graph);
     if (h->pinned) cudaFreeHost(h->pinned);
+    if (h->d_sync) cudaFree(h->d_sync);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
     delete h;
     return DQMC_OK;
@@ -1481,6 +1483,8 @@ int dqmc_pool_create(int device, int max_slots, int64_t budget_bytes, int precis
     e = cudaMalloc((void**)&h->arena, h->budget);
     if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_chains, sizeof(DqmcChain) * max_slots);
     if (e == cudaSuccess) e = cudaHostAlloc((void**)&h->pinned, sizeof(DqmcChain) * max_slots, 0);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&h->d_sync, 4 * sizeof(unsigned int));
+    if (e == cudaSuccess) e = cudaMemset(h->d_sync, 0, 4 * sizeof(unsigned int));
     if (e != cudaSuccess) {
         int st = cuda_fail(e, "dqmc_pool_create: allocation of the pool");
         dqmc_destroy(h);
@@ -1512,6 +1516,7 @@ int dqmc_pool_admit(dqmc_handle* h, const dqmc_chain_config* cfg, int* slot) {
     CUDA_TRY(cudaMemsetAsync(h->arena + off, 0, L.bytes, h->stream), "clear chain workspace");
     fill_descriptor(h->host[free_slot], *cfg, h->arena + off, L, h->precision);
     h->host[free_slot].needs_build = 1;
+    h->host[free_slot].run_sync = h->d_sync;
     h->cfg[free_slot] = *cfg;
     h->lay[free_slot] = L;
     h->slot_off[free_slot] = off;
@@ -1577,7 +1582,13 @@ int64_t dqmc_pool_free_bytes(dqmc_handle* h) {
 int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph) {
     if (!h || !h->pool) return fail(DQMC_ERR_INVALID, "dqmc_pool_run: not a pool");
     if (budget_us <= 0) return fail(DQMC_ERR_INVALID, "dqmc_pool_run: budget_us <= 0");
-    if (!use_graph) return launch(h, DQMC_OP_RUN, budget_us, 0, true);
+    if (!use_graph) {
+        if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+        CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
+        CUDA_TRY(cudaMemsetAsync(h->d_sync, 0, 4 * sizeof(unsigned int), h->stream),
+                 "reset visit counters");
+        return launch(h, DQMC_OP_RUN, budget_us, 0, true);
+    }
     if (h->busy) if (int st = dqmc_synchronize(h)) return st;
     CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
     const size_t bytes = sizeof(DqmcChain) * h->host.size();
@@ -1586,7 +1597,9 @@ int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph) {
         // one replayable step: upload descriptors, time-sliced launch, download
         cudaGraph_t g = nullptr;
         CUDA_TRY(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+        cudaError_t e0 = cudaMemsetAsync(h->d_sync, 0, 4 * sizeof(unsigned int), h->stream);
         cudaError_t e1 = cudaMemcpyAsync(h->d_chains, h->pinned, bytes, cudaMemcpyHostToDevice, h->stream);
+        if (e1 == cudaSuccess) e1 = e0;
         cudaError_t e2 = dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), DQMC_OP_RUN,
                                                   budget_us, 0, h->stream, 0, h->tc);
         cudaError_t e3 = cudaMemcpyAsync(h->pinned, h->d_chains, bytes, cudaMemcpyDeviceToHost, h->stream);

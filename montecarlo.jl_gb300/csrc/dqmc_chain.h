@@ -130,6 +130,10 @@ struct DqmcChain {
     int td_enable, td_rate, td_P, td_nform0, td_nform1, td_ncur;
     double td_dtau;
     double* td;
+    // pool launches: {chains that started visiting, chains past their time
+    // budget} of the current launch (shared by the pool's chains, zeroed
+    // before every launch); NULL outside pools
+    unsigned int* run_sync;
 };
 
 

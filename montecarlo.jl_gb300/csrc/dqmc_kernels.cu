@@ -99,10 +99,18 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     case DQMC_OP_RUN: {
         // time slice of a pool: build the stack of a newly admitted chain,
         // then run slice visits (sweep_spatial + propagate) until the chain's
-        // quota is used up or the budget (arg0 microseconds) has elapsed; the
-        // chain's state carries over to the next slice
+        // quota is used up or the time slice is over; the chain's state
+        // carries over to the next slice.  The slice is work-conserving: a
+        // chain past its budget (arg0 microseconds) keeps visiting until every
+        // chain of the launch is past its own (the pool's visit counters), so
+        // no SM idles while the launch waits for a chain with long visits.
+        // No chain waits for another: each only reads the counters.
         const unsigned long long t_start = global_ns();
         const unsigned long long budget = 1000ull * (unsigned long long)arg0;
+        unsigned int* sync = s->c.run_sync;
+        bool counted = false;  // thread 0: this chain is counted as past its budget
+        const bool works = s->c.needs_build || s->c.visits_quota > 0;
+        if (threadIdx.x == 0 && sync && works) atomicAdd(&sync[0], 1u);
         if (s->c.needs_build) {
             reverse_build_stack(x);
             propagate(x);
@@ -120,12 +128,24 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
             if (threadIdx.x == 0) {
                 s->c.visits_quota -= 1;
                 s->c.visits_done += 1;
-                s->sxi[1] = (global_ns() - t_start) >= budget;
+                const bool over = (global_ns() - t_start) >= budget;
+                bool stop = over;
+                if (sync) {
+                    if (over && !counted) {
+                        atomicAdd(&sync[1], 1u);
+                        counted = true;
+                    }
+                    const volatile unsigned int* vs = sync;
+                    stop = counted && vs[1] >= vs[0];
+                }
+                s->sxi[1] = stop;
             }
             __syncthreads();
             if (s->c.visits_done % (2 * s->c.M) == 0) after_sweep(x);
             if (s->sxi[1]) break;
         }
+        // a chain that stops early (quota used up) no longer holds the others
+        if (threadIdx.x == 0 && sync && works && !counted) atomicAdd(&sync[1], 1u);
         if (in_arena) g_to_global(x);
         break;
     }

@@ -90,3 +90,37 @@ def test_uneven_ensemble_time_sliced(pkg, lib):
     # smaller chains do more sweeps in the same slices
     assert out["per_chain"][3] > out["per_chain"][2]
     assert out["max_propagation_error"] < 1e-6
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_pool_time_slice_is_work_conserving(pkg, lib, use_graph):
+    """A chain past its time budget keeps visiting while another chain of the
+    launch is not (here: a 12 x 12 chain still building its stack), instead
+    of leaving its SM idle; alone, a chain stops at the first visit past the
+    budget (1 microsecond: exactly one visit)."""
+    small = make_setup(pkg, L=4, U=4.0, beta=1.0, safe_mult=5)
+    big = make_setup(pkg, L=12, U=4.0, beta=2.0, safe_mult=5)
+
+    def admit(pool, setup, seed):
+        model, param, fld, exps = setup
+        s = pool.admit(chain_config(lib, model, param, fld, seed))
+        pool.set_hopping(s, exps)
+        pool.init_random_field(s)
+        pool.set_quota(s, 1000)
+        return s
+
+    alone = lib.Pool(2, 64 << 20)
+    s0 = admit(alone, small, 3)
+    alone.run(1, use_graph)
+    assert alone.stats(s0)["proposals"] == 16  # one visit of the 16 sites
+    alone.close()
+
+    pool = lib.Pool(2, 1 << 30)
+    sb = admit(pool, big, 4)
+    ss = admit(pool, small, 3)
+    pool.run(1, use_graph)
+    visits_big = pool.stats(sb)["proposals"] // 144
+    visits_small = pool.stats(ss)["proposals"] // 16
+    assert visits_big >= 1
+    assert visits_small >= 10, (visits_small, visits_big)
+    pool.close()
