@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define DQMC_GB300_ABI_VERSION 8
+#define DQMC_GB300_ABI_VERSION 9
 
 /* status codes */
 #define DQMC_OK 0
@@ -393,9 +393,17 @@ int dqmc_pool_release(dqmc_handle* h, int slot);
 int dqmc_pool_set_quota(dqmc_handle* h, int slot, int64_t n_sweeps);
 /* One time slice of every admitted chain: each runs slice visits until its
  * quota is used up or budget_us microseconds have passed (a chain finishes the
- * visit it is in).  use_graph = 1 replays the step (descriptor upload, launch,
+ * visit it is in); a chain past its budget keeps visiting while another chain
+ * of the slice is not past its own (no SM idles waiting for a chain with long
+ * visits).  use_graph = 1 replays the step (descriptor upload, launch,
  * download) as one captured CUDA graph. */
 int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph);
+/* enable = 1: a two-flavour chain of the pool (real field, dense hopping, no
+ * device measurements, global updates or replica exchange) runs its two
+ * flavour blocks on two CTAs of a two-CTA cluster, i.e. on two SMs, which
+ * roughly halves its time per sweep when SMs are free (served streams at light
+ * load).  Results are bit-identical to the chain on one CTA.  Default 0. */
+int dqmc_pool_set_flavour_split(dqmc_handle* h, int enable);
 int dqmc_pool_slot(dqmc_handle* h, int slot, int64_t* sweeps_done, int64_t* sweeps_left,
                    int32_t* active);
 int64_t dqmc_pool_free_bytes(dqmc_handle* h);

@@ -95,7 +95,7 @@ EXPORTS = [
     "dqmc_get_stats", "dqmc_get_greens", "dqmc_set_greens", "dqmc_calculate_greens",
     "dqmc_get_stack", "dqmc_set_stream", "dqmc_get_timers", "dqmc_calculate_greens_noalloc",
     "dqmc_pool_create", "dqmc_pool_admit", "dqmc_pool_release", "dqmc_pool_set_quota",
-    "dqmc_pool_run", "dqmc_pool_slot", "dqmc_pool_free_bytes",
+    "dqmc_pool_run", "dqmc_pool_slot", "dqmc_pool_free_bytes", "dqmc_pool_set_flavour_split",
     "dqmc_set_measurements", "dqmc_reset_measurements", "dqmc_get_measurements",
     "dqmc_global_update", "dqmc_set_global_schedule", "dqmc_replica_exchange",
     "dqmc_get_global_stats", "dqmc_calculate_greens_kl", "dqmc_set_checkerboard",
@@ -163,6 +163,7 @@ def load(path: str = LIB_PATH):
     L.dqmc_pool_release.argtypes = [P, C.c_int]
     L.dqmc_pool_set_quota.argtypes = [P, C.c_int, C.c_int64]
     L.dqmc_pool_run.argtypes = [P, C.c_int, C.c_int]
+    L.dqmc_pool_set_flavour_split.argtypes = [P, C.c_int]
     L.dqmc_pool_slot.argtypes = [P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                  C.POINTER(C.c_int32)]
     L.dqmc_pool_free_bytes.argtypes = [P]
@@ -557,6 +558,11 @@ class Pool(Handle):
 
     def run(self, budget_us, use_graph=True):
         check(load().dqmc_pool_run(self.h, int(budget_us), int(bool(use_graph))))
+
+    def set_flavour_split(self, enable=True):
+        """Two-flavour chains run their flavour blocks on two CTAs (two SMs)
+        of a two-CTA cluster; results are bit-identical."""
+        check(load().dqmc_pool_set_flavour_split(self.h, int(bool(enable))))
 
     def slot(self, slot):
         d, l, a = C.c_int64(), C.c_int64(), C.c_int32()

@@ -131,7 +131,7 @@ Layout layout_of(const dqmc_chain_config& c, int prec) {
     L.off_tempvf = o; o = align256(o + nf * n * sizeof(double));
     L.off_hopdf = o; o = align256(o + 2 * n * n * sizeof(float2));
     L.off_tcs = o;
-    if (tc_capable(c, prec)) o = align256(o + dqmc_tc_scratch_bytes((int)n));
+    if (tc_capable(c, prec)) o = align256(o + nf * dqmc_tc_scratch_stride((int)n));
     L.bytes = o;
     return L;
 }
@@ -158,6 +158,7 @@ struct dqmc_handle {
     std::vector<size_t> slot_off, slot_bytes;
     DqmcChain* pinned = nullptr;           // pinned mirror for graph replays
     unsigned int* d_sync = nullptr;        // pools: the launch's visit counters (DqmcChain::run_sync)
+    bool flavour_split = false;            // pools: two-flavour chains on two CTAs (dqmc_pool_set_flavour_split)
     int n_max = 0;                         // largest n_sites of a fixed handle's chains
     bool tc = false;                       // launches use the tensor-core kernel build
     bool small_kernel = true;              // sweeps of small chains one warp per chain
@@ -216,7 +217,8 @@ int launch(dqmc_handle* h, int op, int arg0, int arg1, bool sync) {
                  "warp sweep kernel launch");
     else
         CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), op, arg0, arg1,
-                                          h->stream, h->pool ? 0 : h->n_max, h->tc),
+                                          h->stream, h->pool ? 0 : h->n_max, h->tc,
+                                          h->pool && h->flavour_split && op == DQMC_OP_RUN),
                  "chain kernel launch");
     if (!sync) {
         h->busy = true;
@@ -695,7 +697,8 @@ static int launch_one(dqmc_handle* h, int chain, int op, int arg0, int arg1) {
     CUDA_TRY(cudaSetDevice(h->device), "cudaSetDevice");
     if (h->host_dirty) if (int st = push_descriptors(h)) return st;
     CUDA_TRY(dqmc_launch_chain_kernel(h->d_chains + chain, 1, op, arg0, arg1, h->stream,
-                                      (int)mat_n(h->cfg[chain]), h->host[chain].tcs != nullptr),
+                                      (int)mat_n(h->cfg[chain]), h->host[chain].tcs != nullptr,
+                                      false),
              "chain kernel launch");
     CUDA_TRY(cudaStreamSynchronize(h->stream), "chain kernel");
     return pull_descriptors(h);
@@ -1550,6 +1553,18 @@ int dqmc_pool_release(dqmc_handle* h, int slot) {
     return DQMC_OK;
 }
 
+int dqmc_pool_set_flavour_split(dqmc_handle* h, int enable) {
+    if (!h || !h->pool) return fail(DQMC_ERR_INVALID, "dqmc_pool_set_flavour_split: not a pool");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    const bool on = enable != 0;
+    if (on != h->flavour_split && h->graph) {  // the captured launch changes shape
+        cudaGraphExecDestroy(h->graph);
+        h->graph = nullptr;
+    }
+    h->flavour_split = on;
+    return DQMC_OK;
+}
+
 int dqmc_pool_set_quota(dqmc_handle* h, int slot, int64_t n_sweeps) {
     if (int st = check_chain(h, slot)) return st;
     if (n_sweeps < 0) return fail(DQMC_ERR_INVALID, "dqmc_pool_set_quota: n_sweeps < 0");
@@ -1601,7 +1616,8 @@ int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph) {
         cudaError_t e1 = cudaMemcpyAsync(h->d_chains, h->pinned, bytes, cudaMemcpyHostToDevice, h->stream);
         if (e1 == cudaSuccess) e1 = e0;
         cudaError_t e2 = dqmc_launch_chain_kernel(h->d_chains, (int)h->host.size(), DQMC_OP_RUN,
-                                                  budget_us, 0, h->stream, 0, h->tc);
+                                                  budget_us, 0, h->stream, 0, h->tc,
+                                                  h->flavour_split);
         cudaError_t e3 = cudaMemcpyAsync(h->pinned, h->d_chains, bytes, cudaMemcpyDeviceToHost, h->stream);
         cudaError_t e4 = cudaStreamEndCapture(h->stream, &g);
         if (e1 != cudaSuccess || e2 != cudaSuccess || e3 != cudaSuccess || e4 != cudaSuccess) {

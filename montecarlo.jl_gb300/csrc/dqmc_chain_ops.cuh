@@ -25,6 +25,15 @@ struct Smem {
     int arena_cap;               // doubles of `arena` this launch allocated
     int tc_on;                   // this chain's products run on the tensor cores (mm_tc)
     int gdfg;                    // G stays in global memory but holds float pairs (n > 64)
+    // flavour-split chains (one flavour block per CTA of a two-CTA cluster):
+    // this CTA's exchange counter as its partner reads it, the epochs it has
+    // published, a partner that stopped answering, values for the partner,
+    // and a configuration flip published after the partner has read the site
+    unsigned int xflag;
+    unsigned int xepoch;
+    int xdead;
+    int xflip_val;
+    double xval[2];
     TcState tc;                  // TMEM base and mbarriers of mm_tc (16-byte aligned)
     // `tiles` and `arena` are adjacent and 16-byte aligned: mm_tc stages its
     // operand slices in both (chains with n > 64 use neither otherwise)
@@ -68,9 +77,117 @@ struct Ctx {
     DqmcChain* c;  // == &s->c
     int n, nf;
     size_t nn;
+    // flavour blocks this CTA owns: [0, nf), or block `b0` alone on a
+    // flavour-split chain, whose other block the cluster partner (`peer`,
+    // its rank; -1: none) owns
+    int b0, b1, peer;
 };
 
 __device__ __forceinline__ double* blk(double* p, const Ctx& x, int b) { return p + (size_t)b * x.nn; }
+__device__ __forceinline__ bool split(const Ctx& x) { return x.peer >= 0; }
+// the tensor products' operand scratch of this CTA (one area per flavour
+// block; a CTA that owns both blocks uses the first)
+__device__ __forceinline__ unsigned char* tc_scratch(const Ctx& x) {
+    return x.c->tcs + (size_t)x.b0 * dqmc_tc_scratch_stride(x.n);
+}
+// A chain whose two flavour blocks can run on two CTAs: real field, dense
+// hopping, and nothing coupling the blocks besides the local updates'
+// determinant ratio and the propagation error (no device measurements,
+// global updates or replica exchange).
+__device__ __forceinline__ bool flavour_split_ok(const DqmcChain& c) {
+    return c.nf == 2 && !c.cplx && !c.cb && !c.meas_enable && !c.td_enable && c.global_kind < 0 &&
+           c.partner < 0;
+}
+// the owned blocks' part of an nf x (n x n) matrix / an nf x n vector
+__device__ __forceinline__ void copy_mats(const Ctx& x, double* dst, const double* src) {
+    const size_t o = (size_t)x.b0 * x.nn;
+    copy((x.b1 - x.b0) * (int)x.nn, dst + o, src + o);
+}
+__device__ __forceinline__ void copy_vecs(const Ctx& x, double* dst, const double* src) {
+    const int o = x.b0 * x.n;
+    copy((x.b1 - x.b0) * x.n, dst + o, src + o);
+}
+
+// The field of site j of a slice row; `fresh`: read past L1 (on a
+// flavour-split chain the partner CTA's SM writes the configuration).
+__device__ __forceinline__ int conf_at(const int8_t* s, int j, bool fresh) {
+    return fresh ? *reinterpret_cast<const volatile int8_t*>(s + j) : s[j];
+}
+
+// ---- exchanges between the two CTAs of a flavour-split chain ---------------
+__device__ __forceinline__ unsigned int cluster_ncta() {
+    unsigned int r;
+    asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ unsigned int cluster_rank() {
+    unsigned int r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// all threads of the cluster (every CTA has started; its prior writes visible)
+__device__ __forceinline__ void cluster_barrier() {
+    asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;"
+                 ::: "memory");
+}
+// the address of `p` (this CTA's shared memory) in CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t peer_addr(const void* p, int rank) {
+    const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
+    uint32_t r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ double peer_ld(uint32_t a) {
+    double v;
+    asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ int peer_ld_s32(uint32_t a) {
+    int v;
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ unsigned int peer_ld_acquire(uint32_t a) {
+    unsigned int v;
+    asm volatile("ld.acquire.cluster.shared::cluster.u32 %0, [%1];" : "=r"(v) : "r"(a) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_cluster(uint32_t a, unsigned int v) {
+    asm volatile("st.release.cluster.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+#define DQMC_STATUS_PEER 9  // the partner CTA of a flavour-split chain stopped answering
+// Rendezvous of the two CTAs of a flavour-split chain: every write either CTA
+// made before it is visible to the other after it.  Thread 0 publishes its
+// epoch with a cluster-scope release and waits (bounded: 2 s of the global
+// timer or 2^28 polls) until the partner has published the same epoch; after
+// a time-out the chain's status is set, further rendezvous return at once
+// and false, and the callers skip the partner's data (no read of a CTA that
+// may have left).  Executed by all threads of both CTAs the same number of
+// times (both run the same control flow: the decisions are identical).
+__device__ bool xsync(const Ctx& x) {
+    __syncthreads();
+    if (threadIdx.x == 0 && !x.s->xdead) {
+        const unsigned int e = ++x.s->xepoch;
+        st_release_cluster(peer_addr(&x.s->xflag, (int)cluster_rank()), e);
+        const uint32_t pa = peer_addr(&x.s->xflag, x.peer);
+        unsigned long long t0;
+        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));
+        for (unsigned int spin = 0;; ++spin) {
+            if ((int)(peer_ld_acquire(pa) - e) >= 0) break;
+            if ((spin & 1023) == 1023) {
+                unsigned long long t;
+                asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+                if (t - t0 > 2000000000ull || spin > (1u << 28)) {
+                    x.s->xdead = 1;
+                    x.c->status = DQMC_STATUS_PEER;
+                    break;
+                }
+            }
+        }
+    }
+    __syncthreads();
+    return !x.s->xdead;
+}
 
 // G-resident mode (n <= 64): during sweeps G stays in shared memory for the
 // rank-1 updates and wraps, and moves to global memory while a stabilisation
@@ -103,18 +220,20 @@ __device__ __forceinline__ float2* gdf_ptr(const Ctx& x) {
 // buffer: element e is read before it is written, by the same thread)
 __device__ void g_resident_to(const Ctx& x, double* dst) {
     if (!x.s->gres && !x.s->gdfg) return;  // G is in global memory as FP64 already
+    const int e0 = x.b0 * (int)x.nn, e1 = x.b1 * (int)x.nn;
     if (df_mode(x)) {
         const float2* a = gdf_ptr(x);
-        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) dst[e] = df_to_d(a[e]);
+        for (int e = e0 + threadIdx.x; e < e1; e += DQMC_NT) dst[e] = df_to_d(a[e]);
     } else {
-        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) dst[e] = x.s->arena[e];
+        for (int e = e0 + threadIdx.x; e < e1; e += DQMC_NT) dst[e] = x.s->arena[e];
     }
 }
 __device__ void g_to_arena(const Ctx& x) {
     __syncthreads();
+    const int e0 = x.b0 * (int)x.nn, e1 = x.b1 * (int)x.nn;
     if (x.n > 64) {  // in place, float pairs in the global buffer
         float2* a = reinterpret_cast<float2*>(x.s->Gglob);
-        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) a[e] = d_to_df(x.s->Gglob[e]);
+        for (int e = e0 + threadIdx.x; e < e1; e += DQMC_NT) a[e] = d_to_df(x.s->Gglob[e]);
         __syncthreads();
         if (threadIdx.x == 0) x.s->gdfg = 1;
         __syncthreads();
@@ -122,9 +241,9 @@ __device__ void g_to_arena(const Ctx& x) {
     }
     if (df_mode(x)) {
         float2* a = arena_df(x);
-        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) a[e] = d_to_df(x.s->Gglob[e]);
+        for (int e = e0 + threadIdx.x; e < e1; e += DQMC_NT) a[e] = d_to_df(x.s->Gglob[e]);
     } else {
-        for (int e = threadIdx.x; e < x.nf * (int)x.nn; e += DQMC_NT) x.s->arena[e] = x.s->Gglob[e];
+        for (int e = e0 + threadIdx.x; e < e1; e += DQMC_NT) x.s->arena[e] = x.s->Gglob[e];
     }
     __syncthreads();
     if (threadIdx.x == 0) { x.c->G = x.s->arena; x.s->gres = 1; }
@@ -196,10 +315,10 @@ __device__ __forceinline__ void smm(const Ctx& x, bool wrap, double* C, const do
         // the transposed operand is eT2 or eT2inv: take its float-pair split
         if (DQMC_TC_COMPILED && x.s->tc_on && (c.tc_enable & (wrap ? DQMC_TC_WRAPS : DQMC_TC_SLICES))) {
             const bool ok = TA ? mm_tc<true, false, false>(x.n, C, A == c.eT2 ? c.eT2df : c.eT2invdf,
-                                                          B, tc_stage(x.s), &x.s->tc, c.tcs)
+                                                          B, tc_stage(x.s), &x.s->tc, tc_scratch(x))
                                : mm_tc<false, true, false>(x.n, C, A,
                                                            B == c.eT2 ? c.eT2df : c.eT2invdf,
-                                                           tc_stage(x.s), &x.s->tc, c.tcs);
+                                                           tc_stage(x.s), &x.s->tc, tc_scratch(x));
             if (ok) return;
             tc_failed(x);
         }
@@ -279,7 +398,8 @@ __device__ __noinline__ void interaction_exp(const Ctx& x, int slice, bool inver
     const bool ghq = (c.kind >= 2);
     for (int e = threadIdx.x; e < x.nf * ns; e += DQMC_NT) {
         int b = e / ns, i = e % ns;
-        int v = ghq ? (int)s[i] - 1 : (s[i] > 0 ? 1 : 0);
+        const int f = conf_at(s, i, x.peer >= 0);
+        int v = ghq ? f - 1 : (f > 0 ? 1 : 0);
         x.s->ev[b * x.n + i] = inverse ? c.evinv[b][v] : c.ev[b][v];
         if (c.cplx) x.s->ev[b * x.n + ns + i] = inverse ? c.evinvi[b][v] : c.evi[b][v];
     }
@@ -300,7 +420,7 @@ __device__ __forceinline__ void ev_right(const Ctx& x, double* C, const double* 
 // multiply_slice_matrix_left!: M <- eT2 * eV * M  (stack.jl:319-327)
 __device__ __noinline__ void slice_left(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, false);
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         ev_left(x, blk(x.c->tmp1, x, b), x.s->ev + b * x.n, blk(M, x, b));
         __syncthreads();
         if (x.c->cb)
@@ -313,7 +433,7 @@ __device__ __noinline__ void slice_left(const Ctx& x, int slice, double* M, bool
 // multiply_slice_matrix_right!: M <- M * eT2 * eV  (stack.jl:329-337)
 __device__ __noinline__ void slice_right(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, false);
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         if (x.c->cb)
             cb_apply(x, 0, 1, blk(x.c->tmp1, x, b), blk(M, x, b), blk(x.c->tmp2, x, b));
         else
@@ -326,7 +446,7 @@ __device__ __noinline__ void slice_right(const Ctx& x, int slice, double* M, boo
 // multiply_slice_matrix_inv_right!: M <- M * eV^-1 * eT2^-1  (stack.jl:339-347)
 __device__ __noinline__ void slice_inv_right(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, true);
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         ev_right(x, blk(x.c->tmp1, x, b), blk(M, x, b), x.s->ev + b * x.n);
         __syncthreads();
         if (x.c->cb)
@@ -339,7 +459,7 @@ __device__ __noinline__ void slice_inv_right(const Ctx& x, int slice, double* M,
 // multiply_slice_matrix_inv_left!: M <- eV^-1 * eT2^-1 * M  (stack.jl:349-357)
 __device__ __noinline__ void slice_inv_left(const Ctx& x, int slice, double* M, bool wrap = false) {
     interaction_exp(x, slice, true);
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         if (x.c->cb)
             cb_apply(x, 1, 0, blk(x.c->tmp1, x, b), blk(M, x, b), blk(x.c->tmp2, x, b));
         else
@@ -352,7 +472,7 @@ __device__ __noinline__ void slice_inv_left(const Ctx& x, int slice, double* M, 
 // multiply_daggered_slice_matrix_left!: M <- eV * eT2 * M (stack.jl:359-367)
 __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* M) {
     interaction_exp(x, slice, false);
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         if (x.c->cb)
             cb_apply(x, 0, 2, blk(x.c->tmp1, x, b), blk(M, x, b), blk(x.c->tmp2, x, b));
         else
@@ -367,7 +487,7 @@ __device__ __noinline__ void slice_dagger_left(const Ctx& x, int slice, double* 
 // has them, else the FP32-pipe product
 __device__ __forceinline__ void mm_df3(const Ctx& x, float2* C, const float2* A, const float2* B) {
     if (DQMC_TC_COMPILED && x.s->tc_on && (x.c->tc_enable & DQMC_TC_WRAPS)) {
-        if (mm_tc<true, true, true>(x.n, C, A, B, tc_stage(x.s), &x.s->tc, x.c->tcs)) return;
+        if (mm_tc<true, true, true>(x.n, C, A, B, tc_stage(x.s), &x.s->tc, tc_scratch(x))) return;
         tc_failed(x);
     }
     mm_dfx<true, true, true>(x.n, C, A, B, x.s->tiles);
@@ -392,7 +512,7 @@ __device__ __noinline__ void wrap_greens_df(const Ctx& x, int curr_slice, int di
         const bool inverse = (direction == 1) ? (half == 1) : (half == 0);
         interaction_exp(x, slice, inverse);
         const float2* hop = inverse ? c.eT2invdf : c.eT2df;
-        for (int b = 0; b < x.nf; ++b) {
+        for (int b = x.b0; b < x.b1; ++b) {
             float2* g = G + (size_t)b * x.nn;
             float2* t = T + (size_t)b * x.nn;
             __syncthreads();  // the previous block's last reads of d are done
@@ -471,7 +591,7 @@ __device__ __forceinline__ double* dstk(const Ctx& x, int idx) {
 }
 
 __device__ void mat_ident(const Ctx& x, double* A) {
-    for (int b = 0; b < x.nf; ++b) ident(x.n, blk(A, x, b));
+    for (int b = x.b0; b < x.b1; ++b) ident(x.n, blk(A, x, b));
 }
 
 // two flavour blocks that fit the shared-memory QR: factor them together
@@ -480,12 +600,24 @@ __device__ __forceinline__ UdtJob udt_job(const Ctx& x, double* U, double* D, do
     return UdtJob{blk(U, x, b), D + b * x.n, blk(In, x, b), x.c->pivot + b * x.n,
                   x.c->tempv + b * x.n};
 }
+// (a flavour-split chain factors its own block with the pair's arithmetic)
 __device__ __forceinline__ void udt_pair(const Ctx& x, double* U, double* D, double* In, bool apply) {
+    if (split(x)) {
+        const UdtJob j = udt_job(x, U, D, In, x.b0);
+        udt_pivot_sm2(x.n, j, j, apply, x.s->arena, x.s->sv, x.s->sxd, true);
+        return;
+    }
     udt_pivot_sm2(x.n, udt_job(x, U, D, In, 0), udt_job(x, U, D, In, 1), apply, x.s->arena,
                   x.s->sv, x.s->sxd);
 }
 __device__ __forceinline__ void rdivp_pair(const Ctx& x, double* A, double* T, double* O) {
     const int n = x.n;
+    if (split(x)) {
+        const int b = x.b0;
+        rdivp2(n, blk(A, x, b), blk(T, x, b), blk(O, x, b), x.c->pivot + b * n, nullptr, nullptr,
+               nullptr, nullptr, x.s->sv, 1);
+        return;
+    }
     rdivp2(n, A, T, O, x.c->pivot, blk(A, x, 1), blk(T, x, 1), blk(O, x, 1), x.c->pivot + n,
            x.s->sv);
 }
@@ -495,23 +627,23 @@ __device__ __noinline__ void udt_blocks(const Ctx& x, double* U, double* D, doub
         udt_pair(x, U, D, In, apply);
         return;
     }
-    for (int b = 0; b < x.nf; ++b) udt_one(x, blk(U, x, b), D + b * x.n, blk(In, x, b), b, apply);
+    for (int b = x.b0; b < x.b1; ++b) udt_one(x, blk(U, x, b), D + b * x.n, blk(In, x, b), b, apply);
 }
 __device__ __noinline__ void mm_blocks(const Ctx& x, double* C, double* A, double* B) {
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         mm<false, false>(x.n, blk(C, x, b), blk(A, x, b), blk(B, x, b), x.s->tiles);
     }
     __syncthreads();
 }
 __device__ void dright_blocks(const Ctx& x, double* C, double* A, const double* d) {
-    for (int b = 0; b < x.nf; ++b) dright(x.n, blk(C, x, b), blk(A, x, b), d + b * x.n);
+    for (int b = x.b0; b < x.b1; ++b) dright(x.n, blk(C, x, b), blk(A, x, b), d + b * x.n);
     __syncthreads();
 }
 
 // add_slice_sequence_left (stack.jl:377-393)
 __device__ __noinline__ void add_slice_sequence_left(const Ctx& x, int idx) {
     DqmcChain& c = *x.c;
-    copy(x.nf * (int)x.nn, c.currU, ustk(x, idx));
+    copy_mats(x, c.currU, ustk(x, idx));
     __syncthreads();
     long long t0 = phase_start();
     for (int s = c.rfirst[idx - 1]; s <= c.rlast[idx - 1]; ++s) slice_left(x, s, c.currU);
@@ -527,7 +659,7 @@ __device__ __noinline__ void add_slice_sequence_left(const Ctx& x, int idx) {
 // add_slice_sequence_right (stack.jl:402-416)
 __device__ __noinline__ void add_slice_sequence_right(const Ctx& x, int idx) {
     DqmcChain& c = *x.c;
-    copy(x.nf * (int)x.nn, c.currU, ustk(x, idx + 1));
+    copy_mats(x, c.currU, ustk(x, idx + 1));
     __syncthreads();
     long long t0 = phase_start();
     for (int s = c.rlast[idx - 1]; s >= c.rfirst[idx - 1]; --s) slice_dagger_left(x, s, c.currU);
@@ -554,7 +686,7 @@ template <bool TA, bool TB>
 __device__ __forceinline__ void rmm(const Ctx& x, double* C, const double* A, const double* B) {
     if (x.c->prec == DQMC_PREC_MIXED_ID && x.n >= 48 && !x.c->cplx && !x.c->cb) {
         if (DQMC_TC_COMPILED && x.s->tc_on && (x.c->tc_enable & DQMC_TC_GREENS)) {
-            if (mm_tc<false, false, false, TA, TB>(x.n, C, A, B, tc_stage(x.s), &x.s->tc, x.c->tcs))
+            if (mm_tc<false, false, false, TA, TB>(x.n, C, A, B, tc_stage(x.s), &x.s->tc, tc_scratch(x)))
                 return;
             tc_failed(x);
         }
@@ -567,19 +699,19 @@ __device__ __forceinline__ void rmm(const Ctx& x, double* C, const double* A, co
 __device__ __noinline__ void calculate_greens_pair(const Ctx& x, double* Gout, bool finish) {
     DqmcChain& c = *x.c;
     const int n = x.n;
-    for (int b = 0; b < 2; ++b) rmm<false, true>(x, blk(Gout, x, b), blk(c.Tl, x, b), blk(c.Tr, x, b));
+    for (int b = x.b0; b < x.b1; ++b) rmm<false, true>(x, blk(Gout, x, b), blk(c.Tl, x, b), blk(c.Tr, x, b));
     __syncthreads();
-    for (int b = 0; b < 2; ++b) dright(n, blk(c.Tr, x, b), blk(Gout, x, b), c.Dr + b * n);
+    for (int b = x.b0; b < x.b1; ++b) dright(n, blk(c.Tr, x, b), blk(Gout, x, b), c.Dr + b * n);
     __syncthreads();
-    for (int b = 0; b < 2; ++b) dleft(n, blk(Gout, x, b), c.Dl + b * n, blk(c.Tr, x, b));
+    for (int b = x.b0; b < x.b1; ++b) dleft(n, blk(Gout, x, b), c.Dl + b * n, blk(c.Tr, x, b));
     __syncthreads();
     udt_pair(x, c.Tr, c.Dr, Gout, false);
-    for (int b = 0; b < 2; ++b) rmm<false, false>(x, blk(c.Tl, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b));
+    for (int b = x.b0; b < x.b1; ++b) rmm<false, false>(x, blk(c.Tl, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b));
     __syncthreads();
     rdivp_pair(x, c.Ur, Gout, c.Ul);
-    for (int b = 0; b < 2; ++b) rmm<true, false>(x, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ur, x, b));
+    for (int b = x.b0; b < x.b1; ++b) rmm<true, false>(x, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ur, x, b));
     __syncthreads();
-    for (int e = threadIdx.x; e < 2 * n; e += DQMC_NT) {
+    for (int e = x.b0 * n + threadIdx.x; e < x.b1 * n; e += DQMC_NT) {
         const int b = e / n, i = e % n;
         blk(c.Tr, x, b)[(size_t)i * n + i] += c.Dr[b * n + i];
     }
@@ -587,12 +719,12 @@ __device__ __noinline__ void calculate_greens_pair(const Ctx& x, double* Gout, b
     udt_pair(x, c.Ul, c.Dr, c.Tr, false);
     if (!finish) return;
     rdivp_pair(x, c.Ur, c.Tr, Gout);
-    for (int b = 0; b < 2; ++b) rmm<false, false>(x, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ul, x, b));
-    for (int e = threadIdx.x; e < 2 * n; e += DQMC_NT) c.Dl[e] = 1.0 / c.Dr[e];
+    for (int b = x.b0; b < x.b1; ++b) rmm<false, false>(x, blk(c.Tr, x, b), blk(c.Tl, x, b), blk(c.Ul, x, b));
+    for (int e = x.b0 * n + threadIdx.x; e < x.b1 * n; e += DQMC_NT) c.Dl[e] = 1.0 / c.Dr[e];
     __syncthreads();
-    for (int b = 0; b < 2; ++b) dright(n, blk(c.Ul, x, b), blk(c.Ur, x, b), c.Dl + b * n);
+    for (int b = x.b0; b < x.b1; ++b) dright(n, blk(c.Ul, x, b), blk(c.Ur, x, b), c.Dl + b * n);
     __syncthreads();
-    for (int b = 0; b < 2; ++b) rmm<false, true>(x, blk(Gout, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b));
+    for (int b = x.b0; b < x.b1; ++b) rmm<false, true>(x, blk(Gout, x, b), blk(c.Ul, x, b), blk(c.Tr, x, b));
     __syncthreads();
 }
 
@@ -609,7 +741,7 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout, bool f
     DqmcChain& c = *x.c;
     const int n = x.n;
     const bool bf = x.nf > 1;
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         double *ul = blk(c.Ul, x, b), *tl = blk(c.Tl, x, b), *ur = blk(c.Ur, x, b),
                *tr = blk(c.Tr, x, b), *g = blk(Gout, x, b);
         double *dl = c.Dl + b * n, *dr = c.Dr + b * n;
@@ -643,7 +775,7 @@ __device__ __noinline__ void calculate_greens(const Ctx& x, double* Gout, bool f
 }
 
 __device__ void set_ones(const Ctx& x, double* d) {
-    fill(x.nf * x.n, d, 1.0);
+    fill((x.b1 - x.b0) * x.n, d + x.b0 * x.n, 1.0);
 }
 
 // reverse_build_stack (stack.jl:284-308)
@@ -658,9 +790,9 @@ __device__ __noinline__ void reverse_build_stack(const Ctx& x) {
     mat_ident(x, c.Ul);
     set_ones(x, c.Dl);
     mat_ident(x, c.Tl);
-    copy(x.nf * (int)x.nn, c.Ur, ustk(x, 1));
-    copy(x.nf * x.n, c.Dr, dstk(x, 1));
-    copy(x.nf * (int)x.nn, c.Tr, tstk(x, 1));
+    copy_mats(x, c.Ur, ustk(x, 1));
+    copy_vecs(x, c.Dr, dstk(x, 1));
+    copy_mats(x, c.Tr, tstk(x, 1));
     __syncthreads();
     calculate_greens(x, c.G);
     if (threadIdx.x == 0) {
@@ -680,9 +812,9 @@ __device__ __noinline__ void build_stack(const Ctx& x) {
     mat_ident(x, tstk(x, 1));
     __syncthreads();
     for (int i = 1; i <= nr; ++i) add_slice_sequence_left(x, i);
-    copy(x.nf * (int)x.nn, c.Ul, ustk(x, nr + 1));
-    copy(x.nf * x.n, c.Dl, dstk(x, nr + 1));
-    copy(x.nf * (int)x.nn, c.Tl, tstk(x, nr + 1));
+    copy_mats(x, c.Ul, ustk(x, nr + 1));
+    copy_vecs(x, c.Dl, dstk(x, nr + 1));
+    copy_mats(x, c.Tl, tstk(x, nr + 1));
     mat_ident(x, c.Ur);
     set_ones(x, c.Dr);
     mat_ident(x, c.Tr);
@@ -711,8 +843,7 @@ __device__ __noinline__ void record_prop_error(const Ctx& x) {
             if (d > m || d != d) m = d;
         }
     } else {
-        const int cnt = x.nf * (int)x.nn;
-        for (int e = threadIdx.x; e < cnt; e += DQMC_NT) {
+        for (int e = x.b0 * (int)x.nn + threadIdx.x; e < x.b1 * (int)x.nn; e += DQMC_NT) {
             double d = fabs(c.Gtmp[e] - c.G[e]);
             if (d > m || d != d) m = d;
         }
@@ -730,6 +861,20 @@ __device__ __noinline__ void record_prop_error(const Ctx& x) {
             double v = x.s->red[w];
             if (v > mx || v != v) mx = v;
         }
+        x.s->xval[0] = mx;
+    }
+    if (split(x) && xsync(x)) {
+        // the chain's error is the larger of the two blocks' (both CTAs
+        // record the same value); the partner reads xval[0] before the
+        // next rendezvous, which precedes the next write of it
+        if (threadIdx.x == 0) {
+            const double v = peer_ld(peer_addr(&x.s->xval[0], x.peer));
+            if (v > x.s->xval[0] || v != v) x.s->xval[0] = v;
+        }
+        xsync(x);
+    }
+    if (threadIdx.x == 0) {
+        const double mx = x.s->xval[0];
         if (mx > c.prop_err_max || mx != mx) c.prop_err_max = mx;
         // a non-finite Green's function is reported to the host as a
         // numerical error (status 2) instead of propagating silently
@@ -765,16 +910,16 @@ __device__ __noinline__ void propagate(const Ctx& x) {
                 const int idx = cr;
                 const bool was_res = x.s->gres || x.s->gdfg;
                 if (was_res) g_to_global(x);
-                copy(x.nf * (int)x.nn, c.Ur, ustk(x, idx + 1));
-                copy(x.nf * x.n, c.Dr, dstk(x, idx + 1));
-                copy(x.nf * (int)x.nn, c.Tr, tstk(x, idx + 1));
+                copy_mats(x, c.Ur, ustk(x, idx + 1));
+                copy_vecs(x, c.Dr, dstk(x, idx + 1));
+                copy_mats(x, c.Tr, tstk(x, idx + 1));
                 __syncthreads();
                 add_slice_sequence_left(x, idx);
-                copy(x.nf * (int)x.nn, c.Ul, ustk(x, idx + 1));
-                copy(x.nf * x.n, c.Dl, dstk(x, idx + 1));
-                copy(x.nf * (int)x.nn, c.Tl, tstk(x, idx + 1));
+                copy_mats(x, c.Ul, ustk(x, idx + 1));
+                copy_vecs(x, c.Dl, dstk(x, idx + 1));
+                copy_mats(x, c.Tl, tstk(x, idx + 1));
                 long long t0 = phase_start();
-                if (c.check_prop) copy(x.nf * (int)x.nn, c.Gtmp, c.G);
+                if (c.check_prop) copy_mats(x, c.Gtmp, c.G);
                 __syncthreads();
                 wrap_greens(x, c.Gtmp, cs - 1, 1);
                 phase_stop(x, DQMC_PHASE_PROP_CHECK, t0);
@@ -813,16 +958,16 @@ __device__ __noinline__ void propagate(const Ctx& x) {
                 const int idx = cr;
                 const bool was_res = x.s->gres || x.s->gdfg;
                 if (was_res) g_to_global(x);
-                copy(x.nf * (int)x.nn, c.Ul, ustk(x, idx));
-                copy(x.nf * x.n, c.Dl, dstk(x, idx));
-                copy(x.nf * (int)x.nn, c.Tl, tstk(x, idx));
+                copy_mats(x, c.Ul, ustk(x, idx));
+                copy_vecs(x, c.Dl, dstk(x, idx));
+                copy_mats(x, c.Tl, tstk(x, idx));
                 __syncthreads();
                 add_slice_sequence_right(x, idx);
-                copy(x.nf * (int)x.nn, c.Ur, ustk(x, idx));
-                copy(x.nf * x.n, c.Dr, dstk(x, idx));
-                copy(x.nf * (int)x.nn, c.Tr, tstk(x, idx));
+                copy_mats(x, c.Ur, ustk(x, idx));
+                copy_vecs(x, c.Dr, dstk(x, idx));
+                copy_mats(x, c.Tr, tstk(x, idx));
                 long long t0 = phase_start();
-                if (c.check_prop) copy(x.nf * (int)x.nn, c.Gtmp, c.G);
+                if (c.check_prop) copy_mats(x, c.Gtmp, c.G);
                 __syncthreads();
                 phase_stop(x, DQMC_PHASE_PROP_CHECK, t0);
                 t0 = phase_start();
@@ -864,7 +1009,7 @@ __device__ __noinline__ void propagate(const Ctx& x) {
 // of U in registers.
 __device__ void flush_delayed(const Ctx& x, int p) {
     const int n = x.n;
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         double* g = x.c->G + (size_t)b * x.nn;
         const double* U = x.c->tmp2 + (size_t)b * x.nn;
         const double* W = x.c->currU + (size_t)b * x.nn;
@@ -894,7 +1039,7 @@ __device__ void flush_delayed(const Ctx& x, int p) {
 __device__ void flush_delayed_df(const Ctx& x, int p) {
     const int n = x.n;
     float2* wdf = arena_df(x);  // p * n pairs <= 16 * 256 (32 KB of the arena)
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         float2* g = gdf_ptr(x) + (size_t)b * x.nn;
         const double* U = x.c->tmp2 + (size_t)b * x.nn;
         const double* W = x.c->currU + (size_t)b * x.nn;
@@ -937,6 +1082,21 @@ __device__ void flush_delayed_df(const Ctx& x, int p) {
 __device__ __forceinline__ void flush_pending(const Ctx& x, int p, bool df) {
     if (df) flush_delayed_df(x, p);
     else flush_delayed(x, p);
+}
+
+// Flavour-split chain: bring the partner's block of the diagonal mirror into
+// this CTA's after a rendezvous (accepted site j >= 0: rank 0 first writes
+// the site's new field, `xflip_val`, now that both have read the old one);
+// a second rendezvous keeps the partner from changing its mirror before this
+// CTA has read it.
+__device__ void pull_peer_diag(const Ctx& x, double* diag, int j) {
+    if (!xsync(x)) return;
+    if (j >= 0 && x.b0 == 0 && threadIdx.x == 0)
+        x.c->conf[(size_t)(x.c->current_slice - 1) * x.n + j] = (int8_t)x.s->xflip_val;
+    const int pb = 1 - x.b0, n = x.n;
+    const uint32_t base = peer_addr(diag + pb * n, x.peer);
+    for (int k = threadIdx.x; k < n; k += DQMC_NT) diag[pb * n + k] = peer_ld(base + 8u * k);
+    xsync(x);
 }
 
 // sweep_spatial on a complex chain (local_updates.jl:23-60 with the complex
@@ -1189,12 +1349,14 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     // n x n rank-1 update runs in double-float on the FP32 pipe
     const bool dfg = df_resident(x);
     const float2* gdf = gdf_ptr(x);
-    for (int e = tid; e < nf * n; e += DQMC_NT) {
+    const int e0 = x.b0 * n, e1 = x.b1 * n;  // the owned blocks' entries
+    for (int e = e0 + tid; e < e1; e += DQMC_NT) {
         const int b = e / n, k = e % n;
         const size_t at = (size_t)b * x.nn + (size_t)k * n + k;
         diag[e] = dfg ? df_to_d(gdf[at]) : c.G[at];
     }
     __syncthreads();
+    if (split(x)) pull_peer_diag(x, diag, -1);
     long long acc_count = 0;
     int i = 0, round = 0;
     // G in global memory: delay the rank-1 updates and apply them DQMC_DELAY
@@ -1212,7 +1374,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 int xnew = 0;
                 double gr = 1.0, gq = 1.0;
                 if (ghq) {
-                    const int xold = s[j];
+                    const int xold = conf_at(s, j, split(x));
                     const uint64_t w = dqmc_philox_word(c.key, c.ctr);
                     c.ctr += 1;
                     const int r = dqmc_word_to_choice3(w);
@@ -1221,7 +1383,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                     gr = c.gam[xnew - 1];
                     gq = c.gam[xold - 1];
                 } else {
-                    t = s[j] > 0 ? 1 : 0;
+                    t = conf_at(s, j, split(x)) > 0 ? 1 : 0;
                 }
                 const double d0 = c.delta0[t], d1 = c.delta1[t];
                 const double R0 = __dadd_rn(1.0, __dmul_rn(d0, __dsub_rn(1.0, g0)));
@@ -1253,7 +1415,11 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 if (accept) {
                     x.s->sxd[0] = __ddiv_rn(d0, R0);
                     x.s->sxd[1] = twoflv ? __ddiv_rn(d1, R1) : 0.0;
-                    s[j] = ghq ? (int8_t)xnew : (int8_t)(-s[j]);
+                    const int8_t flipped = ghq ? (int8_t)xnew : (int8_t)(-conf_at(s, j, split(x)));
+                    // a flavour-split chain flips after the partner has read
+                    // the site (rank 0 alone writes the configuration)
+                    if (split(x)) x.s->xflip_val = (int)flipped;
+                    else s[j] = flipped;
                     c.accepted += 1;
                     break;
                 }
@@ -1270,7 +1436,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
             break;
         }
         acc_count += 1;
-        for (int e = tid; e < nf * n; e += DQMC_NT) {
+        for (int e = e0 + tid; e < e1; e += DQMC_NT) {
             const int b = e / n, k = e % n;
             const double* g = c.G + (size_t)b * x.nn;
             double gkj, gjk;
@@ -1308,7 +1474,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
         __syncthreads();
         if (delayed) {
             if (warp == 0) {
-                for (int e = lane; e < nf * n; e += 32) {
+                for (int e = e0 + lane; e < e1; e += 32) {
                     const int b = e / n, k = e % n;
                     diag[e] = fma(-x.s->r1.col[b][k], x.s->r1.row[b][k], diag[e]);
                 }
@@ -1320,18 +1486,19 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 flush_pending(x, pending, dfg);
                 pending = 0;
             }
+            if (split(x)) pull_peer_diag(x, diag, j);
             i = j + 1;
             continue;
         }
         if (warp == 0) {
-            for (int e = lane; e < nf * n; e += 32) {
+            for (int e = e0 + lane; e < e1; e += 32) {
                 const int b = e / n, k = e % n;
                 diag[e] = fma(-x.s->r1.col[b][k], x.s->r1.row[b][k], diag[e]);
             }
             __syncwarp();
         } else if (dfg) {
             const int w = tid - 32, nw = DQMC_NT / 32 - 1;
-            for (int b = 0; b < nf; ++b) {
+            for (int b = x.b0; b < x.b1; ++b) {
                 float2* g = arena_df(x) + (size_t)b * x.nn;
                 const float2* cl = reinterpret_cast<const float2*>(x.s->r1.col[b] + 256);
                 const float2* rw = reinterpret_cast<const float2*>(x.s->r1.row[b] + 256);
@@ -1343,7 +1510,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
             }
         } else {
             const int w = tid - 32, nw = DQMC_NT / 32 - 1;
-            for (int b = 0; b < nf; ++b) {
+            for (int b = x.b0; b < x.b1; ++b) {
                 double* g = c.G + (size_t)b * x.nn;
                 const double* cl = x.s->r1.col[b];
                 const double* rw = x.s->r1.row[b];
@@ -1354,6 +1521,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 }
             }
         }
+        if (split(x)) pull_peer_diag(x, diag, j);
         i = j + 1;
     }
     return acc_count;
@@ -1566,7 +1734,7 @@ __device__ __noinline__ void replica_accept(const Ctx& x, const DqmcChain* all, 
 // _greens! (greens.jl:114-125): out = eThalfplus * (G * eThalfminus)
 __device__ __noinline__ void greens_physical(const Ctx& x, const double* src, double* out) {
     DqmcChain& c = *x.c;
-    for (int b = 0; b < x.nf; ++b) {
+    for (int b = x.b0; b < x.b1; ++b) {
         if (c.cb) {
             cb_apply(x, 2, 1, blk(c.tmp1, x, b), src + (size_t)b * x.nn, blk(c.tmp2, x, b));
             cb_apply(x, 3, 0, blk(out, x, b), blk(c.tmp1, x, b), blk(c.tmp2, x, b));
@@ -1747,15 +1915,15 @@ __device__ __forceinline__ double* utv(const Ctx& x, double* p, int idx) {
 }
 
 __device__ void mm_nt_blocks(const Ctx& x, double* C, double* A, double* B) {
-    for (int b = 0; b < x.nf; ++b) mm<false, true>(x.n, blk(C, x, b), blk(A, x, b), blk(B, x, b), x.s->tiles);
+    for (int b = x.b0; b < x.b1; ++b) mm<false, true>(x.n, blk(C, x, b), blk(A, x, b), blk(B, x, b), x.s->tiles);
     __syncthreads();
 }
 __device__ void mm_tn_blocks(const Ctx& x, double* C, double* A, double* B) {
-    for (int b = 0; b < x.nf; ++b) mm<true, false>(x.n, blk(C, x, b), blk(A, x, b), blk(B, x, b), x.s->tiles);
+    for (int b = x.b0; b < x.b1; ++b) mm<true, false>(x.n, blk(C, x, b), blk(A, x, b), blk(B, x, b), x.s->tiles);
     __syncthreads();
 }
 __device__ void dleft_blocks(const Ctx& x, double* C, const double* d, double* B) {
-    for (int b = 0; b < x.nf; ++b) dleft(x.n, blk(C, x, b), d + b * x.n, blk(B, x, b));
+    for (int b = x.b0; b < x.b1; ++b) dleft(x.n, blk(C, x, b), d + b * x.n, blk(B, x, b));
     __syncthreads();
 }
 __device__ void rdivp_blocks(const Ctx& x, double* A, double* T, double* O) {
@@ -1763,7 +1931,7 @@ __device__ void rdivp_blocks(const Ctx& x, double* A, double* T, double* O) {
         rdivp_pair(x, A, T, O);
         return;
     }
-    for (int b = 0; b < x.nf; ++b)
+    for (int b = x.b0; b < x.b1; ++b)
         rdivp(x.n, blk(A, x, b), blk(T, x, b), blk(O, x, b), x.c->pivot + b * x.n, x.nf > 1, x.s->sv);
 }
 // vmaxinv! / vmin! (real.jl:143-170), rvadd! (:123-127), copyto!(A, Diagonal(d))
@@ -1877,7 +2045,7 @@ __device__ __noinline__ void ut_inverse_block(const Ctx& x, const UtView& s, int
 __device__ __noinline__ void ut_forward_block(const Ctx& x, const UtView& s, int slice) {
     DqmcChain& c = *x.c;
     const int idx = max(0, find_range(x, slice) - 1);
-    copy(x.nf * (int)x.nn, c.Tl, utm(x, s.fu, idx + 1));
+    copy_mats(x, c.Tl, utm(x, s.fu, idx + 1));
     __syncthreads();
     const int target = idx > 0 ? c.rlast[idx - 1] + 1 : 1;
     for (int l = target; l <= slice; ++l) slice_left(x, l, c.Tl);
@@ -1890,7 +2058,7 @@ __device__ __noinline__ void ut_forward_block(const Ctx& x, const UtView& s, int
 __device__ __noinline__ void ut_backward_block(const Ctx& x, const UtView& s, int slice) {
     DqmcChain& c = *x.c;
     const int idx = find_range(x, slice) + 1;
-    copy(x.nf * (int)x.nn, c.Ur, utm(x, s.bu, idx));
+    copy_mats(x, c.Ur, utm(x, s.bu, idx));
     __syncthreads();
     const int target = idx <= c.nr ? c.rfirst[idx - 1] - 1 : c.rlast[c.nr - 1];
     for (int l = target; l >= slice + 1; --l) slice_dagger_left(x, l, c.Ur);

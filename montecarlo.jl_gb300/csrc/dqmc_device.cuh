@@ -832,12 +832,16 @@ struct UdtJob {
 // sv: 2 * 64 doubles (block g at g * 64); sxd: 2 doubles.  Same algorithm and
 // pivot rule as udt_pivot_sm.
 __device__ __noinline__ void udt_pivot_sm2(int n, UdtJob j0, UdtJob j1, bool apply,
-                                           double* arena, double* sv, double* sxd) {
+                                           double* arena, double* sv, double* sxd,
+                                           bool one = false) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     // block 1 numbers its warps backwards (warp 7 first): when a late step
     // keeps only the first warps of each block busy, the two blocks' warps
     // sit on different SM sub-partitions
-    const int g = tid >> 7, gwarp = g ? 7 - warp : warp, gtid = gwarp * 32 + lane;
+    const int g = tid >> 7, gwarp = g ? 7 - warp : warp;
+    // one: block j0 alone (threads 128-255 only keep the barriers), with the
+    // same arithmetic per block as the pair
+    const int gtid = (one && g) ? (1 << 20) : gwarp * 32 + lane;
     const UdtJob J = g ? j1 : j0;
     const int ld = n + 1;
     double* sIn = arena + (size_t)g * n * ld;
@@ -865,7 +869,7 @@ __device__ __noinline__ void udt_pivot_sm2(int n, UdtJob j0, UdtJob j1, bool app
     }
     __syncthreads();
     for (int j = 0; j < n; ++j) {
-        if (gwarp == 0) {  // warp 0 for block 0, warp 7 for block 1
+        if (gwarp == 0 && !(one && g)) {  // warp 0 for block 0, warp 7 for block 1
             long long best = -1;
             int bi = j;  // never out of range, also when every norm is NaN
             for (int col = j + lane; col < n; col += 32) {
@@ -1018,14 +1022,15 @@ __device__ __noinline__ void udt_pivot_sm2(int n, UdtJob j0, UdtJob j1, bool app
 // doubles.  Same arithmetic per row as rdivp.
 __device__ __noinline__ void rdivp2(int n, double* A0, const double* T0, double* O0, const int* p0,
                                     double* A1, const double* T1, double* O1, const int* p1,
-                                    double* rcp) {
+                                    double* rcp, int nb = 2) {
+    // nb = 1: block 0 alone, the same arithmetic per row
     const int tid = threadIdx.x;
-    for (int e = tid; e < 2 * n; e += DQMC_NT) {
+    for (int e = tid; e < nb * n; e += DQMC_NT) {
         const int b = e / n, j = e % n;
         const double* T = b ? T1 : T0;
         rcp[b * 64 + j] = 1.0 / T[(size_t)j * n + j];
     }
-    for (int e = tid; e < 2 * n * n; e += DQMC_NT) {
+    for (int e = tid; e < nb * n * n; e += DQMC_NT) {
         const int b = e / (n * n), f = e % (n * n);
         const int i = f % n, j = f / n;
         const double* A = b ? A1 : A0;
@@ -1033,7 +1038,7 @@ __device__ __noinline__ void rdivp2(int n, double* A0, const double* T0, double*
         (b ? O1 : O0)[f] = A[i + (size_t)(piv[j] - 1) * n];
     }
     __syncthreads();
-    if (tid < 128) {
+    if (tid < 64 * nb) {
         const int b = tid >> 6, i = tid & 63;
         if (i < n) {
             double* A = b ? A1 : A0;

@@ -38,11 +38,25 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
                                                            int arena_cap) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     Smem* s = reinterpret_cast<Smem*>(smem_raw);
-    if ((int)blockIdx.x >= nchains) return;
+    // launched in two-CTA clusters (a pool with flavour-split chains): both
+    // CTAs of a cluster take the same slot; a two-flavour chain that can be
+    // split runs one flavour block on each, any other chain on rank 0 alone
+    const bool pair = cluster_ncta() == 2;
+    const int slot = pair ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;
+    const int rank = pair ? (int)cluster_rank() : 0;
+    if (pair) {
+        if (threadIdx.x == 0) {
+            s->xflag = 0;
+            s->xepoch = 0;
+            s->xdead = 0;
+        }
+        cluster_barrier();  // both CTAs have started and cleared their exchange counters
+    }
+    if (slot >= nchains) return;
     // stage this chain's descriptor in shared memory
     {
         const int words = (int)(sizeof(DqmcChain) / 4);
-        const uint32_t* src = reinterpret_cast<const uint32_t*>(chains + blockIdx.x);
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(chains + slot);
         uint32_t* dst = reinterpret_cast<uint32_t*>(&s->c);
         for (int e = threadIdx.x; e < words; e += DQMC_NT) dst[e] = src[e];
     }
@@ -53,6 +67,9 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     x.n = s->c.n;
     x.nf = s->c.nf;
     x.nn = (size_t)x.n * x.n;
+    x.b0 = 0;
+    x.b1 = x.nf;
+    x.peer = -1;
     if (threadIdx.x == 0) {
         s->Gglob = s->c.G;
         s->gres = 0;
@@ -63,8 +80,15 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     __syncthreads();
     if (!s->c.active) return;  // free pool slot
     if (x.n > DQMC_NMAX || x.nf < 1 || x.nf > 2) {
-        if (threadIdx.x == 0) chains[blockIdx.x].status = 1;
+        if (threadIdx.x == 0 && rank == 0) chains[slot].status = 1;
         return;
+    }
+    const bool fsplit = pair && op == DQMC_OP_RUN && flavour_split_ok(s->c);
+    if (pair && rank == 1 && !fsplit) return;
+    if (fsplit) {
+        x.b0 = rank;
+        x.b1 = rank + 1;
+        x.peer = rank ^ 1;
     }
     // tensor-core products: one warp allocates the accumulators' TMEM columns
     // (two CTAs per SM at most, 2 x 256 of the SM's 512 columns) and thread 0
@@ -107,7 +131,9 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
         // No chain waits for another: each only reads the counters.
         const unsigned long long t_start = global_ns();
         const unsigned long long budget = 1000ull * (unsigned long long)arg0;
-        unsigned int* sync = s->c.run_sync;
+        // (a flavour-split chain counts once, on rank 0, which also decides
+        // when the chain stops and tells its partner)
+        unsigned int* sync = rank == 0 ? s->c.run_sync : nullptr;
         bool counted = false;  // thread 0: this chain is counted as past its budget
         const bool works = s->c.needs_build || s->c.visits_quota > 0;
         if (threadIdx.x == 0 && sync && works) atomicAdd(&sync[0], 1u);
@@ -139,6 +165,12 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
                     stop = counted && vs[1] >= vs[0];
                 }
                 s->sxi[1] = stop;
+                s->xval[1] = stop ? 1.0 : 0.0;
+            }
+            if (fsplit) {  // rank 1 follows rank 0 (a partner gone: stop)
+                const bool ok = xsync(x);
+                if (threadIdx.x == 0 && rank == 1)
+                    s->sxi[1] = !ok || peer_ld(peer_addr(&s->xval[1], x.peer)) != 0.0;
             }
             __syncthreads();
             if (s->c.visits_done % (2 * s->c.M) == 0) after_sweep(x);
@@ -226,9 +258,21 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
         if ((threadIdx.x >> 5) == 0) tc_dealloc(s->tc.tmem, DQMC_TC_COLS);
 #endif
     }
+    if (fsplit) {
+        // rank 0 takes over its partner's status; then both leave (no CTA
+        // reads the shared memory of one that has left)
+        if (xsync(x)) {
+            if (threadIdx.x == 0 && rank == 0) {
+                const int st = peer_ld_s32(peer_addr(&s->c.status, x.peer));
+                if (st != 0 && s->c.status == 0) s->c.status = st;
+            }
+            xsync(x);
+        }
+        if (rank == 1) return;
+    }
     // write back the mutable state
     if (threadIdx.x == 0) {
-        DqmcChain& g = chains[blockIdx.x];
+        DqmcChain& g = chains[slot];
         g.ctr = s->c.ctr;
         g.current_slice = s->c.current_slice;
         g.current_range = s->c.current_range;
@@ -303,7 +347,7 @@ cudaError_t DQMC_KERNEL_ENTRY(dqmc_prepare_chain_kernel)() {
 
 cudaError_t DQMC_KERNEL_ENTRY(dqmc_launch_chain_kernel)(DqmcChain* d_chains, int nchains, int op,
                                                         int arg0, int arg1, cudaStream_t stream,
-                                                        int n_max) {
+                                                        int n_max, bool pairs) {
     cudaError_t e = DQMC_KERNEL_ENTRY(dqmc_prepare_chain_kernel)();
     if (e != cudaSuccess) return e;
     // arena the chains need: 2 n (n + 1) doubles for the largest n <= 64
@@ -312,6 +356,23 @@ cudaError_t DQMC_KERNEL_ENTRY(dqmc_launch_chain_kernel)(DqmcChain* d_chains, int
     const int na = (n_max <= 0 || n_max > 64) ? 64 : n_max;
     const int cap = 2 * na * (na + 1);
     const size_t smem = offsetof(dqmc::Smem, arena) + (size_t)cap * sizeof(double);
+    if (pairs) {
+        // two CTAs per chain in two-CTA clusters (flavour-split chains)
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(2u * (unsigned)nchains);
+        cfg.blockDim = dim3(DQMC_NT);
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = stream;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 2;
+        attr[0].val.clusterDim.y = 1;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, dqmc::chain_kernel<2>, d_chains, nchains, op, arg0, arg1,
+                                  cap);
+    }
     if (n_max > 0 && n_max <= 32)
         dqmc::chain_kernel<4><<<nchains, DQMC_NT, smem, stream>>>(d_chains, nchains, op, arg0,
                                                                   arg1, cap);
@@ -327,8 +388,8 @@ cudaError_t dqmc_prepare_chain_kernels() {
     return e == cudaSuccess ? dqmc_prepare_chain_kernel_tc() : e;
 }
 cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
-                                     cudaStream_t stream, int n_max, bool tc) {
-    return tc ? dqmc_launch_chain_kernel_tc(d_chains, nchains, op, arg0, arg1, stream, n_max)
-              : dqmc_launch_chain_kernel(d_chains, nchains, op, arg0, arg1, stream, n_max);
+                                     cudaStream_t stream, int n_max, bool tc, bool pairs) {
+    return tc ? dqmc_launch_chain_kernel_tc(d_chains, nchains, op, arg0, arg1, stream, n_max, pairs)
+              : dqmc_launch_chain_kernel(d_chains, nchains, op, arg0, arg1, stream, n_max, pairs);
 }
 #endif

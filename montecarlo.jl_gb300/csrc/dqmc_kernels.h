@@ -15,13 +15,14 @@ cudaError_t dqmc_prepare_chain_kernels();  // both builds
 // variant); <= 0 when the chains may change between replays of a captured
 // launch (pools): the full arena.  The first two take one build; the third
 // picks the tensor-core build when tc (the launch holds chains whose
-// products may run on the tensor cores).
+// products may run on the tensor cores).  pairs: two CTAs per chain in
+// two-CTA clusters (DQMC_OP_RUN of a pool with flavour-split chains).
 cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
-                                     cudaStream_t stream, int n_max);
+                                     cudaStream_t stream, int n_max, bool pairs);
 cudaError_t dqmc_launch_chain_kernel_tc(DqmcChain* d_chains, int nchains, int op, int arg0,
-                                        int arg1, cudaStream_t stream, int n_max);
+                                        int arg1, cudaStream_t stream, int n_max, bool pairs);
 cudaError_t dqmc_launch_chain_kernel(DqmcChain* d_chains, int nchains, int op, int arg0, int arg1,
-                                     cudaStream_t stream, int n_max, bool tc);
+                                     cudaStream_t stream, int n_max, bool tc, bool pairs);
 
 // The sweep of chains with n <= 32 sites, one warp per chain (dqmc_warp.cu):
 // nsweeps sweeps of every chain.  n_max: the largest n of the launch (<= 32).

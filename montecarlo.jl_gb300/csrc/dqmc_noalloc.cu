@@ -74,6 +74,9 @@ __global__ void __launch_bounds__(DQMC_NT, 2)
     x.n = s->c.n;
     x.nf = s->c.nf;
     x.nn = (size_t)x.n * x.n;
+    x.b0 = 0;
+    x.b1 = x.nf;
+    x.peer = -1;
     dqmc::calculate_greens_at(x, slice, safe_mult, out);
 }
 

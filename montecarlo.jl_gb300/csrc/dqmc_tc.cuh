@@ -76,6 +76,11 @@ __host__ __device__ inline size_t dqmc_tc_scratch_bytes(int n) {
     const size_t nk = (size_t)(n + DQMC_TC_KB - 1) / DQMC_TC_KB;
     return dqmc_tc_scratch_a(n) + (size_t)((n + DQMC_TC_TN - 1) / DQMC_TC_TN) * nk * DQMC_TC_BSTEP;
 }
+// a chain's scratch holds one such area per flavour block (256-byte aligned),
+// so that the two CTAs of a flavour-split chain split their products apart
+__host__ __device__ inline size_t dqmc_tc_scratch_stride(int n) {
+    return (dqmc_tc_scratch_bytes(n) + 255) & ~(size_t)255;
+}
 
 namespace dqmc {
 

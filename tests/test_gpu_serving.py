@@ -124,3 +124,45 @@ def test_pool_time_slice_is_work_conserving(pkg, lib, use_graph):
     assert visits_big >= 1
     assert visits_small >= 10, (visits_small, visits_big)
     pool.close()
+
+
+@pytest.mark.parametrize("prec,L", [("fp64", 4), ("fp64", 8), ("fp64", 10), ("mixed", 8),
+                                    ("mixed", 12)])
+def test_flavour_split_chain_equals_one_cta(pkg, lib, prec, L):
+    """A two-flavour chain whose flavour blocks run on the two CTAs of a
+    two-CTA cluster (n = 16 and 64: shared-memory QR and G; n = 100: G in
+    global memory with delayed updates; mixed n = 144: tensor-core products
+    and float-pair G) gives bit-identical fields, Green's function and
+    counters to the chain on one CTA; a one-flavour chain in the same pool
+    runs on one CTA of its pair."""
+    precision = lib.PREC_MIXED if prec == "mixed" else lib.PREC_FP64
+    two = make_setup(pkg, L=L, U=-4.0, beta=2.0 if L <= 8 else 1.0, safe_mult=5,
+                     field=pkg.MagneticHirschField)
+    one = make_setup(pkg, L=4, U=4.0, beta=1.0, safe_mult=5, field=pkg.DensityHirschField)
+    assert two[2].unique_flavors == 2 and one[2].unique_flavors == 1
+    out = []
+    for fsplit in (False, True):
+        pool = lib.Pool(4, 1 << 30, precision=precision)
+        pool.set_flavour_split(fsplit)
+        slots = []
+        for (model, param, fld, exps), seed in ((two, 21), (one, 22)):
+            s = pool.admit(chain_config(lib, model, param, fld, seed))
+            pool.set_hopping(s, exps)
+            pool.init_random_field(s)
+            pool.set_quota(s, 2)
+            slots.append(s)
+        pool.run(30_000_000, True)  # one slice covers both sweeps of both chains
+        res = []
+        for s in slots:
+            done, left, _ = pool.slot(s)
+            assert (done, left) == (2, 0)
+            st = pool.stats(s)
+            assert st["status"] == 0
+            res.append((pool.get_field(s), pool.greens(s), st))
+        out.append(res)
+        pool.close()
+    for (f0, g0, s0), (f1, g1, s1) in zip(out[0], out[1]):
+        assert np.array_equal(f0, f1)
+        assert np.array_equal(g0, g1)
+        for k in ("accepted", "proposals", "near_ties", "max_propagation_error"):
+            assert s0[k] == s1[k], k
