@@ -224,6 +224,9 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, stream, seed=3):
         # runs is far above its value on a few probe sweeps
         ks, errs = autotune.tune_safe_mult(specs, tol=1e-6, precision=prec, confs=confs,
                                            safety=0.005)
+        tensor, tc_ratio = None, None
+        if prec == _lib.PREC_MIXED:  # tensor-core or double-float products, timed per kind
+            tensor, tc_ratio = autotune.tune_tensor(specs, ks=ks, confs=confs)
         tune_s = time.perf_counter() - t
         backoffs, attempts = 0, 0
         while True:
@@ -236,7 +239,7 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, stream, seed=3):
                                             fld.alpha, s),
                            pkg.hopping_exponentials(model.hopping_matrix(), dt)))
             r = pkg.run_ensemble(ce, seconds=seconds, quantum_us=100000, precision=prec,
-                                 confs=confs)
+                                 confs=confs, tensor=tensor)
             pe = np.array(r["per_chain_propagation_error"])
             if not np.any(pe > 1e-6) or attempts == 3:
                 break
@@ -252,6 +255,15 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, stream, seed=3):
                      "safe_mult_histogram": {str(k): ks.count(k) for k in sorted(set(ks))},
                      "autotune_s": tune_s, "backoffs": backoffs, "timed_runs": attempts,
                      "timed_s": r["wall"], "launches": r["launches"]}
+        if tensor is not None:
+            by_n = {}
+            for (model, _f, beta, _dt, _s), on, q in zip(specs, tensor, tc_ratio):
+                n = len(model.l)
+                if 96 <= n <= 256:
+                    by_n.setdefault(f"n={n},beta={beta:g}", {"tensor_products": bool(on),
+                                             "double_float_over_tensor_cycles":
+                                                 None if q != q else round(q, 3)})
+            out[name]["product_choice"] = by_n
     out["unbatched_plain_fp64"] = unbatched_plain(pkg, _lib, specs, chosen["plain_fp64"], confs,
                                                   stream)
     out["mixed_vs_plain"] = out["mixed"]["sweeps_per_s"] / out["plain_fp64"]["sweeps_per_s"]

@@ -21,6 +21,12 @@ reuses the choice without probing, and ``back_off`` lowers the interval of
 chains whose propagation error exceeded the bound over a longer run (the
 error's tail over many sweeps lies above its value on a few probe sweeps) and
 records the lowered choice.
+
+``tune_tensor`` chooses, per kind of mixed-precision chain with
+96 <= n <= 256, between the tensor-core split-precision products and the
+double-float FP32-pipe products by timing both on the device (the per-chain
+phase timers of one probe launch, both variants side by side), cached by
+(sites, flavours, slices, field).
 """
 from __future__ import annotations
 
@@ -133,3 +139,62 @@ def tune_safe_mult(specs, tol=1e-6, precision=_lib.PREC_FP64, candidates=CANDIDA
         chosen.append(k)
         err_at.append(e[k])
     return chosen, err_at
+
+
+# (n, nf, slices, field kind) -> tensor products faster (True / False)
+_TC_CACHE = {}
+
+
+def tensor_key(model, field_cls, beta, delta_tau):
+    param = DQMCParameters.make(beta=beta, delta_tau=delta_tau)
+    fld = field_cls(param, model)
+    return (len(model.l), fld.unique_flavors, param.slices, fld.kind)
+
+
+def tune_tensor(specs, ks=None, confs=None, sweeps=1, device=0, use_cache=True):
+    """Per spec: True when its chain sweeps faster with the tensor-core
+    products than with the double-float products (mixed precision; always
+    False outside 96 <= n <= 256), and the probe's cycle ratio (NaN for a
+    cached or ineligible kind).  `ks`: the specs' safe_mult (default 10)."""
+    keys = [tensor_key(m, f, b, dt) for m, f, b, dt, s in specs]
+    ratio = [float("nan")] * len(specs)
+    todo = {}
+    for j, (m, f, b, dt, s) in enumerate(specs):
+        n = len(m.l)
+        if not (96 <= n <= 256) or (use_cache and keys[j] in _TC_CACHE):
+            continue
+        todo.setdefault(keys[j], j)
+    if todo:
+        cfgs, owner = [], []
+        for key, j in todo.items():
+            m, f, b, dt, s = specs[j]
+            k = 10 if ks is None else ks[j]
+            for tc in (True, False):
+                cfgs.append(_cfg(m, f, b, dt, k, s))
+                owner.append((key, j, tc))
+        h = _lib.Handle(cfgs, precision=_lib.PREC_MIXED, device=device)
+        for r, (key, j, tc) in enumerate(owner):
+            m, f, b, dt, s = specs[j]
+            h.set_hopping(r, hopping_exponentials(m.hopping_matrix(), dt))
+            h.init_random_field(r)
+            if confs is not None:
+                h.set_field(r, confs[j])
+            h.set_tensor_products(tc, chain=r)
+        h.initialize_run()
+        t0 = [sum(h.timers(r).values()) for r in range(len(cfgs))]
+        h.sweep(sweeps)
+        cyc = [sum(h.timers(r).values()) - t0[r] for r in range(len(cfgs))]
+        h.close()
+        per = {}
+        for r, (key, j, tc) in enumerate(owner):
+            per.setdefault(key, {})[tc] = cyc[r]
+        for key, d in per.items():
+            _TC_CACHE[key] = d[True] < d[False]
+            for jj, kk in enumerate(keys):
+                if kk == key:
+                    ratio[jj] = d[False] / d[True] if d[True] > 0 else float("nan")
+    choice = []
+    for j, (m, f, b, dt, s) in enumerate(specs):
+        n = len(m.l)
+        choice.append(bool(96 <= n <= 256 and _TC_CACHE.get(keys[j], True)))
+    return choice, ratio

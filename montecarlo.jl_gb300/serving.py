@@ -185,11 +185,13 @@ class Server:
 
 
 def run_ensemble(configs_and_exps, seconds: float, quantum_us=50000, precision=_lib.PREC_FP64,
-                 use_graph=True, device=0, budget_bytes=None, confs=None):
+                 use_graph=True, device=0, budget_bytes=None, confs=None, tensor=None):
     """Advance an uneven ensemble of chains for about `seconds` of device time
     in time-sliced launches; returns aggregate sweeps/s and per-chain sweeps.
     ``confs`` (optional): starting field configurations (e.g. thermalised
-    ones) in place of the seeded random ones; the streams stay seeded."""
+    ones) in place of the seeded random ones; the streams stay seeded.
+    ``tensor`` (optional, mixed precision): per chain, tensor-core products
+    on or off (``autotune.tune_tensor``)."""
     nbytes = sum(_lib.chain_bytes(c, precision) + 4096 for c, _ in configs_and_exps)
     pool = _lib.Pool(len(configs_and_exps), budget_bytes or nbytes, precision=precision,
                      device=device)
@@ -202,6 +204,8 @@ def run_ensemble(configs_and_exps, seconds: float, quantum_us=50000, precision=_
         pool.init_random_field(s)
         if confs is not None:
             pool.set_field(s, confs[j])
+        if tensor is not None:
+            pool.set_tensor_products(bool(tensor[j]), chain=s)
         pool.set_quota(s, 1 << 40)
         slots.append(s)
     pool.run(quantum_us, use_graph)  # stack builds + warm-up slice

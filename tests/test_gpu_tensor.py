@@ -97,3 +97,18 @@ def test_mixed_large_sweeps_track_fp64(pkg, lib, oracle, tensor):
     oc = oracle_chain(oracle, model, param, fld, exps, 21)
     oc.set_conf(h.get_field(0))
     assert maxdiff(h.greens(0), oc.calculate_greens_at(st["current_slice"] - 1)) <= TOL_MIXED
+
+
+def test_tune_tensor_probe(pkg, lib):
+    """The autotuner times a 12 x 12 two-flavour mixed chain with and without
+    the tensor-core products in one probe launch and caches the faster."""
+    from montecarlo_gb300 import autotune
+    m = pkg.HubbardModel(pkg.SquareLattice(12), U=-4.0)
+    spec = [(m, pkg.MagneticHirschField, 2.0, 0.1, 5)]
+    key = autotune.tensor_key(*spec[0][:4])
+    autotune._TC_CACHE.pop(key, None)
+    choice, ratio = autotune.tune_tensor(spec, ks=[5])
+    assert ratio[0] == ratio[0] and ratio[0] > 0
+    assert choice[0] == (ratio[0] > 1.0)
+    assert autotune._TC_CACHE[key] == choice[0]
+    autotune._TC_CACHE.pop(key, None)

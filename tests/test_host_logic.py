@@ -83,3 +83,19 @@ def test_td_arrays_square(pkg):
     assert a["n_form"] == [64, 64]  # directed nearest-neighbour bonds
     assert a["n_current"] == 32     # bonds along +x, two entries each
     assert np.allclose(a["q_cos"] ** 2 + a["q_sin"] ** 2, 1.0)
+
+
+def test_tensor_choice_cache_and_range(pkg):
+    """tune_tensor: kinds outside 96 <= n <= 256 never use the tensor-core
+    products; a cached kind is answered without a device probe."""
+    from montecarlo_gb300 import autotune
+    small = pkg.HubbardModel(pkg.SquareLattice(8), U=4.0)    # n = 64
+    big = pkg.HubbardModel(pkg.SquareLattice(10), U=4.0)     # n = 100
+    specs = [(small, small.choose_field(), 4.0, 0.1, 1), (big, big.choose_field(), 4.0, 0.1, 2)]
+    key = autotune.tensor_key(big, big.choose_field(), 4.0, 0.1)
+    autotune._TC_CACHE[key] = False
+    choice, ratio = autotune.tune_tensor(specs)
+    assert choice == [False, False] and all(r != r for r in ratio)
+    autotune._TC_CACHE[key] = True
+    assert autotune.tune_tensor(specs)[0] == [False, True]
+    autotune._TC_CACHE.pop(key, None)
