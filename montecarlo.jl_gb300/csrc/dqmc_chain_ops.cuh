@@ -1450,11 +1450,31 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
             }
             if (delayed) {
                 // current G[k, j] and G[j, k] with the pending updates applied
+                // (in the order m = 0, 1, ...); the loads of a batch of four
+                // terms are issued together (one L2 round trip per batch, not
+                // per term)
                 const double* U = c.tmp2 + (size_t)b * x.nn;
                 const double* W = c.currU + (size_t)b * x.nn;
-                for (int m = 0; m < pending; ++m) {
-                    gkj = fma(-U[(size_t)m * n + k], W[(size_t)m * n + j], gkj);
-                    gjk = fma(-U[(size_t)m * n + j], W[(size_t)m * n + k], gjk);
+#pragma unroll
+                for (int m0 = 0; m0 < DQMC_DELAY; m0 += 4) {
+                    if (m0 >= pending) break;
+                    double uk[4], wk[4], uj[4], wj[4];
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        const bool on = m0 + m < pending;
+                        const size_t r = (size_t)(m0 + m) * n;
+                        uk[m] = on ? U[r + k] : 0.0;
+                        wk[m] = on ? W[r + k] : 0.0;
+                        uj[m] = on ? U[r + j] : 0.0;
+                        wj[m] = on ? W[r + j] : 0.0;
+                    }
+#pragma unroll
+                    for (int m = 0; m < 4; ++m) {
+                        if (m0 + m < pending) {
+                            gkj = fma(-uk[m], wj[m], gkj);
+                            gjk = fma(-uj[m], wk[m], gjk);
+                        }
+                    }
                 }
             }
             double ig = -gkj;
