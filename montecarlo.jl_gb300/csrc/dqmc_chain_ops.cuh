@@ -52,6 +52,7 @@ struct Smem {
 };
 static_assert(sizeof(double) * 2 * 16 * 64 + sizeof(double) * 2 * 64 * 65 >= DQMC_TC_SMEM,
               "mm_tc staging must fit tiles + arena");
+static_assert(2 * 64 * 65 >= DQMC_QWS, "the blocked Q accumulation's workspace must fit the arena");
 
 // Products of a chain run on the tensor cores (mm_tc) when it is a real,
 // mixed-precision chain with dense hopping and DQMC_TC_NMIN <= n <= 256, its
@@ -265,10 +266,10 @@ __device__ __forceinline__ void udt_one(const Ctx& x, double* U, double* D, doub
                      x.s->arena, x.s->arena + x.n * (x.n + 1), x.s->sv, x.s->sxd);
     else if (x.c->prec == DQMC_PREC_MIXED_ID)  // norms downdated (see udt_pivot_g)
         udt_pivot_g<true>(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
-                          blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->tiles);
+                          blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->tiles, x.s->arena);
     else
         udt_pivot_g<false>(x.n, U, D, In, x.c->pivot + b * x.n, x.c->tempv + b * x.n, apply,
-                           blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->tiles);
+                           blk(x.c->out, x, b), x.s->sv, x.s->sxd, x.s->tiles, x.s->arena);
 }
 
 

@@ -340,12 +340,11 @@ __device__ __noinline__ void mm_dfx(int n, void* __restrict__ Cv, const void* __
 //    when one of its eight columns needs it); the reflector's own norm is
 //    recomputed from its column.  Without DOWNDATE the norms are recomputed
 //    every step as the reference's indmaxcolumn does;
-//  * Q accumulates backwards with the same mapping; the next reflector is
-//    staged in the second half of `xs` during the current step, one barrier
-//    per step.
+//  * Q accumulates in blocks of reflectors (q_blocked).
 // scr: n*n scratch (apply only); sv: n doubles of shared memory (squared
-// norms); sxd, sxi: shared scalars; xs: 2048 doubles of shared memory
-// (reflector buffers at 0 and 512, DOWNDATE reference norms at 1024).
+// norms); sxd: shared scalars; xs: 2048 doubles of shared memory (the
+// reflector at 0, DOWNDATE reference norms at 1024); ws: DQMC_QWS doubles of
+// shared memory.
 // Strided column kernels of udt_pivot_g: rows r, r + 4, r + 8, ... < n of a
 // column in global memory (L2), eight loads in flight per lane (four
 // accumulation chains), which the L2 latency of the two-die part needs to
@@ -402,12 +401,133 @@ __device__ __forceinline__ double axpy_s4(double* a, const double* __restrict__ 
     return (q0 + q1) + (q2 + q3);
 }
 
+// Explicit Q of a Householder QR, Q = H_0 H_1 ... H_{n-1} I (UDT.jl:272-289),
+// accumulated in blocks of DQMC_QB reflectors from the last block to the
+// first: H_k0 ... H_k1-1 = I - V T V^T (compact WY form; Schreiber and Van
+// Loan 1989, T as LAPACK's xLARFT builds it, forward and columnwise), so that
+// each block updates the trailing rows and columns of Q with two products
+// (W = V^T Q, Q -= V (T W)) staged through shared memory, in column passes of
+// DQMC_QC, instead of one rank-1 pass over Q per reflector.  Same Q up to
+// rounding.  In: the reflectors below the diagonal (unit diagonal implied),
+// tau: their factors; ws: DQMC_QWS doubles of shared memory.
+#define DQMC_QB 16
+#define DQMC_QC 64
+#define DQMC_QWS (2 * DQMC_QB * DQMC_QB + 32 * DQMC_QB + 32 * DQMC_QC + 2 * DQMC_QB * DQMC_QC)
+// entry r of reflector k0 + i of a block of nb
+__device__ __forceinline__ double qv(const double* In, int n, int k0, int i, int nb, int r) {
+    const int k = k0 + i;
+    if (i >= nb || r < k) return 0.0;
+    return r == k ? 1.0 : In[(size_t)k * n + r];
+}
+__device__ __noinline__ void q_blocked(int n, double* __restrict__ U, const double* __restrict__ In,
+                                       const double* __restrict__ tau, double* ws) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    double* Y = ws;                          // [QB][QB]: v_p . v_l for p < l
+    double* T = Y + DQMC_QB * DQMC_QB;       // [QB][QB], upper triangular
+    double* Vs = T + DQMC_QB * DQMC_QB;      // [32][QB]: a row slice of V
+    double* Qs = Vs + 32 * DQMC_QB;          // [32][QC]: the same rows of Q's pass
+    double* W = Qs + 32 * DQMC_QC;           // [QB][QC]: V^T Q
+    double* W2 = W + DQMC_QB * DQMC_QC;      // [QB][QC]: T V^T Q
+    ident(n, U);
+    __syncthreads();
+    if (tid == 0) U[(size_t)(n - 1) * n + (n - 1)] -= tau[n - 1];  // the 1 x 1 reflector
+    __syncthreads();
+    for (int k1 = n - 1; k1 > 0;) {
+        const int k0 = ((k1 - 1) / DQMC_QB) * DQMC_QB, nb = k1 - k0;
+        // Y[p][l] = v_p . v_l over the rows >= k0 + l (p < l < nb)
+        for (int pl = warp; pl < DQMC_QB * DQMC_QB; pl += DQMC_NW) {
+            const int p = pl / DQMC_QB, l = pl % DQMC_QB;
+            if (p >= l || l >= nb) continue;
+            double y = 0.0;
+            for (int r = k0 + l + lane; r < n; r += 32)
+                y = fma(qv(In, n, k0, p, nb, r), qv(In, n, k0, l, nb, r), y);
+            y = warp_sum(y);
+            if (lane == 0) Y[p * DQMC_QB + l] = y;
+        }
+        __syncthreads();
+        // T[l][l] = tau_l, T[0:l][l] = -tau_l T[0:l][0:l] Y[0:l][l]; zero elsewhere
+        if (warp == 0) {
+            for (int e = lane; e < DQMC_QB * DQMC_QB; e += 32) T[e] = 0.0;
+            __syncwarp();
+            for (int l = 0; l < nb; ++l) {
+                const double tl = tau[k0 + l];
+                double v = 0.0;
+                if (lane < l) {
+                    for (int p = lane; p < l; ++p) v = fma(T[lane * DQMC_QB + p], Y[p * DQMC_QB + l], v);
+                    v = -tl * v;
+                }
+                __syncwarp();
+                if (lane < l) T[lane * DQMC_QB + l] = v;
+                if (lane == l) T[l * DQMC_QB + l] = tl;
+                __syncwarp();
+            }
+        }
+        __syncthreads();
+        const int wi = tid & (DQMC_QB - 1), wc = (tid >> 4) * 4;  // W outputs (wi, wc..wc+3)
+        for (int c0 = k0; c0 < n; c0 += DQMC_QC) {
+            // W = V^T Q[k0:n, c0:c0+QC]
+            double acc[4] = {0.0, 0.0, 0.0, 0.0};
+            for (int r0 = k0; r0 < n; r0 += 32) {
+                for (int e = tid; e < 32 * DQMC_QB; e += DQMC_NT) {
+                    const int rr = e & 31, i = e >> 5, r = r0 + rr;
+                    Vs[rr * DQMC_QB + i] = r < n ? qv(In, n, k0, i, nb, r) : 0.0;
+                }
+                for (int e = tid; e < 32 * DQMC_QC; e += DQMC_NT) {
+                    const int rr = e & 31, cc = e >> 5, r = r0 + rr, c = c0 + cc;
+                    Qs[rr * DQMC_QC + cc] = (r < n && c < n) ? U[(size_t)c * n + r] : 0.0;
+                }
+                __syncthreads();
+#pragma unroll 8
+                for (int rr = 0; rr < 32; ++rr) {
+                    const double v = Vs[rr * DQMC_QB + wi];
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[q] = fma(v, Qs[rr * DQMC_QC + wc + q], acc[q]);
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int q = 0; q < 4; ++q) W[wi * DQMC_QC + wc + q] = acc[q];
+            __syncthreads();
+            // W2 = T W
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                double sum = 0.0;
+                for (int p = wi; p < DQMC_QB; ++p)
+                    sum = fma(T[wi * DQMC_QB + p], W[p * DQMC_QC + wc + q], sum);
+                W2[wi * DQMC_QC + wc + q] = sum;
+            }
+            __syncthreads();
+            // Q[k0:n, pass] -= V W2: lanes along the rows, eight columns a thread
+            {
+                const int rr = lane, cg = warp * 8;
+                for (int r = k0 + rr; r < n; r += 32) {
+                    double v[DQMC_QB];
+#pragma unroll
+                    for (int i = 0; i < DQMC_QB; ++i) v[i] = qv(In, n, k0, i, nb, r);
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) {
+                        const int cc = cg + q, c = c0 + cc;
+                        if (c < n) {
+                            double sum = U[(size_t)c * n + r];
+#pragma unroll
+                            for (int i = 0; i < DQMC_QB; ++i) sum = fma(-v[i], W2[i * DQMC_QC + cc], sum);
+                            U[(size_t)c * n + r] = sum;
+                        }
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        k1 = k0;
+    }
+}
+
 template <bool DOWNDATE>
 __device__ __noinline__ void udt_pivot_g(int n, double* __restrict__ U, double* __restrict__ D,
                                          double* __restrict__ In, int* __restrict__ piv,
                                          double* __restrict__ tau, bool apply,
                                          double* __restrict__ scr, double* sv, double* sxd,
-                                         double* xs) {
+                                         double* xs, double* ws) {
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const int h = lane >> 3, cl = lane & 7;  // row quarter, column within the group of eight
     const double tol3z = 1.4901161193847656e-08;  // sqrt(2^-52)
@@ -546,43 +666,8 @@ __device__ __noinline__ void udt_pivot_g(int n, double* __restrict__ U, double* 
         }
         __syncthreads();
     }
-    // Calculate Q (UDT.jl:272-289): U = H_0 ... H_{n-1} applied to I backwards;
-    // the reflector of step k is staged in xs + 512 (k & 1), zero in the rows
-    // of its first quartet at or above row k
-    auto stage = [&](int k) {
-        double* dst = xs + 512 * (k & 1);
-        const double* v = In + (size_t)k * n;
-        for (int r = (k & ~3) + tid; r < n; r += DQMC_NT) dst[r] = r > k ? v[r] : 0.0;
-    };
-    ident(n, U);
-    if (n >= 2) stage(n - 2);
-    __syncthreads();
-    if (tid == 0) U[(size_t)(n - 1) * n + (n - 1)] -= tau[n - 1];
-    __syncthreads();
-    for (int k = n - 2; k >= 0; --k) {
-        const double* xv = xs + 512 * (k & 1);
-        const int rb = (k + 1) & ~3;
-        const double t = tau[k];
-        for (int g = k + warp * 8; g < n; g += 8 * DQMC_NW) {
-            const int c = g + cl;
-            const bool act = c < n;
-            double* u = U + (size_t)(act ? c : g) * n;
-            double sdot = act ? dot_s4(xv, u, rb + h, n) : 0.0;
-            sdot += __shfl_xor_sync(0xffffffffu, sdot, 8);
-            sdot += __shfl_xor_sync(0xffffffffu, sdot, 16);
-            const double uk = act ? u[k] : 0.0;
-            const double vB = t * (uk + sdot);
-            if (act) {
-                const int r = rb + h;
-                if (r > k && r < n) u[r] = fma(-xv[r], vB, u[r]);
-                axpy_s4<false>(u, xv, vB, r + 4, n);
-            }
-            __syncwarp();  // every lane has read u[k]
-            if (act && h == 0) u[k] = uk - vB;
-        }
-        if (k >= 1) stage(k - 1);
-        __syncthreads();
-    }
+    // Calculate Q (UDT.jl:272-289)
+    q_blocked(n, U, In, tau, ws);
     // D (UDT.jl:293-301)
     for (int i = tid; i < n; i += DQMC_NT) {
         double xx = fabs(In[(size_t)i * n + i]);
