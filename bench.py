@@ -320,6 +320,48 @@ def unbatched_plain(pkg, _lib, specs, ks, confs, stream, per_class=2):
             "timed_s": timed}
 
 
+def c1_line(pkg, _lib, stream, nsm, seed=1, sweeps=20):
+    """4x4 attractive Hubbard (U_ref = +4), DensityHirschField, beta=4, M=40,
+    safe_mult=10, FP64: an ensemble of 16 chains per SM on the one-warp-per-
+    chain kernel (and 4 per SM on the CTA kernel for comparison), `sweeps`
+    timed sweeps after the stack build and one warm-up sweep."""
+    import torch
+
+    model = pkg.HubbardModel(pkg.SquareLattice(4), U=4.0)
+    param = pkg.DQMCParameters.make(beta=4.0, delta_tau=0.1, safe_mult=10)
+    fld = pkg.DensityHirschField(param, model)
+    exps = pkg.hopping_exponentials(model.hopping_matrix(), param.delta_tau)
+    n, M = len(model.l), param.slices
+    out = {"workload": "4x4 square attractive Hubbard U=4 (reference convention), mu=0, "
+                       "DensityHirschField, beta=4, dtau=0.1 (M=40), safe_mult=10, FP64"}
+
+    def one(n_chains, warp):
+        h = _lib.Handle([_lib.ChainConfig(n, 1, M, 10, fld.kind, 1, fld.alpha, seed + j)
+                         for j in range(n_chains)], precision=_lib.PREC_FP64)
+        h.set_small_chain_kernel(warp)
+        h.set_hopping(-1, exps)
+        h.init_random_field(-1)
+        h.set_stream(stream.cuda_stream)
+        h.initialize_run()
+        h.sweep_async(1)
+        h.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        h.sweep_async(sweeps)
+        e1.record(stream)
+        h.synchronize()
+        torch.cuda.synchronize()
+        t = e0.elapsed_time(e1) / 1e3
+        pe = max(h.stats(i)["max_propagation_error"] for i in range(n_chains))
+        h.close()
+        return {"chains": n_chains, "sweeps_per_s": n_chains * sweeps / t,
+                "max_propagation_error": pe}
+
+    out["warp_kernel"] = one(16 * nsm, True)
+    out["cta_kernel"] = one(4 * nsm, False)
+    return out
+
+
 def c4_line(pkg, _lib, stream, n_chains, seed=4):
     """16x16 repulsive Hubbard U=4 (physics), MagneticHirschField, beta=10,
     M=100, safe_mult=10: an ensemble of n_chains chains, one timed sweep each
@@ -726,6 +768,7 @@ def main():
         extras["served"] = served_c5(pkg, _lib, 48, 5 * args.extra_seconds)
         extras["served_full"] = served_c5(pkg, _lib, 48, 10 * args.extra_seconds, full=True)
         extras["c4"] = c4_line(pkg, _lib, stream, 2 * nsm)
+        extras["c1"] = c1_line(pkg, _lib, stream, nsm)
         # the headline ratios of the metric, lifted to the top level
         b = extras["batched"]
         extras["c3_mixed_sweeps_per_s"] = b["mixed"]["sweeps_per_s"]
