@@ -1037,6 +1037,25 @@ __device__ void flush_delayed(const Ctx& x, int p) {
 // summed exactly-rounded in a float pair (TwoProd by fmaf, TwoSum) with the
 // cross terms in FP32, then added to G with one TwoSum: no FP64 instruction
 // beyond the O(p n) splits.
+// one term u w of flush_delayed_df's sum: the leading products summed
+// exactly rounded in (sh, sl) (TwoProd by fmaf, TwoSum), the cross terms in xx
+__device__ __forceinline__ void df_delay_term(float2 u, float2 w, float& sh, float& sl, float& xx) {
+    const float pr = __fmul_rn(u.x, w.x);
+    const float pe = __fmaf_rn(u.x, w.x, -pr);
+    const float t = __fadd_rn(sh, pr);
+    const float z = __fsub_rn(t, sh);
+    const float er = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(pr, z));
+    sh = t;
+    sl = __fadd_rn(sl, __fadd_rn(er, pe));
+    xx = __fmaf_rn(u.x, w.y, __fmaf_rn(u.y, w.x, xx));
+}
+// (gv.x + gv.y) + (sh + (sl + xx)): TwoSum of the leading parts
+__device__ __forceinline__ float2 df_delay_add(float2 gv, float sh, float sl, float xx) {
+    const float s = __fadd_rn(gv.x, sh);
+    const float z = __fsub_rn(s, gv.x);
+    const float er = __fadd_rn(__fsub_rn(gv.x, __fsub_rn(s, z)), __fsub_rn(sh, z));
+    return df_norm(s, __fadd_rn(__fadd_rn(gv.y, __fadd_rn(sl, xx)), er));
+}
 __device__ void flush_delayed_df(const Ctx& x, int p) {
     const int n = x.n;
     float2* wdf = arena_df(x);  // p * n pairs <= 16 * 256 (32 KB of the arena)
@@ -1051,29 +1070,32 @@ __device__ void flush_delayed_df(const Ctx& x, int p) {
 #pragma unroll
             for (int m = 0; m < DQMC_DELAY; ++m)
                 uk[m] = m < p ? d_to_df(-U[(size_t)m * n + k]) : make_float2(0.f, 0.f);
-            for (int l = threadIdx.x >> 6; l < n; l += DQMC_NT / 64) {
-                float sh = 0.f, sl = 0.f, xx = 0.f;
+            // four columns of the thread's stride at a time: four independent
+            // dependency chains, and their G entries loaded before the sums
+            // (a column past n repeats the first one and is not stored)
+            constexpr int LS = DQMC_NT / 64, NC = 4;
+            for (int l = threadIdx.x >> 6; l < n; l += NC * LS) {
+                int lc[NC];
+                float2 gv[NC];
+                float sh[NC], sl[NC], xx[NC];
+#pragma unroll
+                for (int q = 0; q < NC; ++q) {
+                    lc[q] = l + q * LS < n ? l + q * LS : l;
+                    gv[q] = g[(size_t)k + (size_t)lc[q] * n];
+                    sh[q] = sl[q] = xx[q] = 0.f;
+                }
 #pragma unroll
                 for (int m = 0; m < DQMC_DELAY; ++m) {
                     if (m < p) {
-                        const float2 w = wdf[(size_t)m * n + l];
-                        const float pr = __fmul_rn(uk[m].x, w.x);
-                        const float pe = __fmaf_rn(uk[m].x, w.x, -pr);
-                        const float t = __fadd_rn(sh, pr);
-                        const float z = __fsub_rn(t, sh);
-                        const float er = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, z)), __fsub_rn(pr, z));
-                        sh = t;
-                        sl = __fadd_rn(sl, __fadd_rn(er, pe));
-                        xx = __fmaf_rn(uk[m].x, w.y, __fmaf_rn(uk[m].y, w.x, xx));
+#pragma unroll
+                        for (int q = 0; q < NC; ++q)
+                            df_delay_term(uk[m], wdf[(size_t)m * n + lc[q]], sh[q], sl[q], xx[q]);
                     }
                 }
-                const size_t at = (size_t)k + (size_t)l * n;
-                const float2 gv = g[at];
-                // (gv.x + gv.y) + (sh + (sl + xx)): TwoSum of the leading parts
-                const float s = __fadd_rn(gv.x, sh);
-                const float z = __fsub_rn(s, gv.x);
-                const float er = __fadd_rn(__fsub_rn(gv.x, __fsub_rn(s, z)), __fsub_rn(sh, z));
-                g[at] = df_norm(s, __fadd_rn(__fadd_rn(gv.y, __fadd_rn(sl, xx)), er));
+#pragma unroll
+                for (int q = 0; q < NC; ++q)
+                    if (q == 0 || lc[q] != l)
+                        g[(size_t)k + (size_t)lc[q] * n] = df_delay_add(gv[q], sh[q], sl[q], xx[q]);
             }
         }
         __syncthreads();
