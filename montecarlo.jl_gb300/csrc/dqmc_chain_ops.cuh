@@ -1473,17 +1473,17 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
             }
             if (delayed) {
                 // current G[k, j] and G[j, k] with the pending updates applied
-                // (in the order m = 0, 1, ...); the loads of a batch of four
+                // (in the order m = 0, 1, ...); the loads of a batch of eight
                 // terms are issued together (one L2 round trip per batch, not
                 // per term)
                 const double* U = c.tmp2 + (size_t)b * x.nn;
                 const double* W = c.currU + (size_t)b * x.nn;
 #pragma unroll
-                for (int m0 = 0; m0 < DQMC_DELAY; m0 += 4) {
+                for (int m0 = 0; m0 < DQMC_DELAY; m0 += 8) {
                     if (m0 >= pending) break;
-                    double uk[4], wk[4], uj[4], wj[4];
+                    double uk[8], wk[8], uj[8], wj[8];
 #pragma unroll
-                    for (int m = 0; m < 4; ++m) {
+                    for (int m = 0; m < 8; ++m) {
                         const bool on = m0 + m < pending;
                         const size_t r = (size_t)(m0 + m) * n;
                         uk[m] = on ? U[r + k] : 0.0;
@@ -1492,7 +1492,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                         wj[m] = on ? W[r + j] : 0.0;
                     }
 #pragma unroll
-                    for (int m = 0; m < 4; ++m) {
+                    for (int m = 0; m < 8; ++m) {
                         if (m0 + m < pending) {
                             gkj = fma(-uk[m], wj[m], gkj);
                             gjk = fma(-uj[m], wk[m], gjk);
