@@ -193,6 +193,11 @@ def cpu_baseline_sample(pkg, workload, budget_s):
                       f"(C restatement of the reference, FMA contraction on)"}
 
 
+def nsm_of_device():
+    import torch
+    return torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+
+
 def ensemble_c3(pkg, _lib, n_chains, seconds, stream, seed=3):
     """Batched ensemble of uneven attractive chains: L in {6,8,10,12}, U_phys in
     [-8,-2] (U_ref = -U_phys), beta in {4,8,12}, dtau = 0.1; safe_mult
@@ -212,7 +217,8 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, stream, seed=3):
         specs.append((model, model.choose_field(), beta, 0.1, 1000 + j))
     out = {"workload": f"{n_chains} attractive chains, L in {{6,8,10,12}} square, U in [-8,-2] "
                        "(physics), beta in {4,8,12}, dtau=0.1, safe_mult autotuned per chain "
-                       "(propagation error <= 1e-6), started from thermalised configurations"}
+                       "(propagation error <= 1e-6), started from thermalised configurations",
+           "cta_slots": {"chains": n_chains, "slots": 2 * nsm_of_device()}}
     t = time.perf_counter()
     confs = autotune.thermalize(specs)
     therm_s = time.perf_counter() - t
@@ -248,6 +254,16 @@ def ensemble_c3(pkg, _lib, n_chains, seconds, stream, seed=3):
             if nb == 0:
                 break
         chosen[name] = ks
+        # per (L, beta) class: chains and their mean sweeps/s over the timed run
+        # (the load balance of the uneven ensemble: a launch ends with its
+        # slowest visit, time slices keep every chain's SM busy meanwhile)
+        per_class = {}
+        for (model, _f, beta, _dt, _s), sw in zip(specs, r["per_chain"]):
+            key = f"L={int(round(len(model.l) ** 0.5))},beta={beta:g}"
+            per_class.setdefault(key, []).append(sw / r["wall"])
+        out[name + "_per_class_sweeps_per_s"] = {
+            k: {"chains": len(v), "mean": float(np.mean(v)), "min": float(np.min(v))}
+            for k, v in sorted(per_class.items())}
         out[name] = {"sweeps_per_s": r["sweeps_per_s"],
                      "max_propagation_error": r["max_propagation_error"],
                      "median_chain_propagation_error": float(np.median(pe)),
