@@ -140,6 +140,37 @@ struct DqmcChain {
 // the near-tie window of DqmcChain::n_near_tie
 #define DQMC_NEAR_TIE 1e-12
 #ifdef __CUDACC__
+// The decision `p > 1 || rand() < p` (local_updates.jl:53) with the uniform
+// (w >> 11) 2^-53 built on the integer pipe: the 53-bit integer is exact in
+// a double and the power-of-two scaling is exact, so these are the bits of
+// the same double; the comparisons of non-negative doubles order like their
+// bit patterns (NaN and negative p handled explicitly).  On GB300's narrow
+// FP64 pipe this keeps the conversion and the comparisons off the serial
+// decision chain.
+__device__ __forceinline__ long long uniform_bits(uint64_t w) {
+    const uint64_t m = w >> 11;
+    if (m == 0) return 0;
+    const int sh = __clzll((long long)m) - 11;  // the leading one to bit 52
+    return (long long)(((uint64_t)(1022 - sh) << 52) | ((m << sh) & ((1ull << 52) - 1)));
+}
+__device__ __forceinline__ bool bits_nan(long long P) {
+    return (P & 0x7FFFFFFFFFFFFFFFll) > 0x7FF0000000000000ll;
+}
+// p > 1.0
+__device__ __forceinline__ bool above_one(double p) {
+    const long long P = __double_as_longlong(p);
+    return P > 0x3FF0000000000000ll && !bits_nan(P);
+}
+// p < 0.0
+__device__ __forceinline__ bool below_zero(double p) {
+    const long long P = __double_as_longlong(p);
+    return P < 0 && (P & 0x7FFFFFFFFFFFFFFFll) != 0 && !bits_nan(P);
+}
+// u < p for a uniform's bits U (a double in [0, 1))
+__device__ __forceinline__ bool uniform_below(long long U, double p) {
+    const long long P = __double_as_longlong(p);
+    return !bits_nan(P) && U < P;
+}
 // record the gap between a drawn uniform u and the probability p it is tested
 // against (the decision itself is `u < p`)
 __device__ __forceinline__ void note_tie(DqmcChain& c, double u, double p) {

@@ -1419,20 +1419,22 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                     detratio = __dmul_rn(R0, R0);
                 }
                 if (ghq) detratio = __ddiv_rn(__dmul_rn(detratio, gr), gq);
+                // the uniform's word, drawn only when p <= 1 but computed
+                // ahead (it does not depend on p)
+                const uint64_t wu = dqmc_philox_word(c.key, c.ctr);
                 const double p = __dmul_rn(c.wboson[t], detratio);
-                if (p < 0.0) {
+                if (below_zero(p)) {
                     c.n_neg_p += 1;
                     DQMC_MS_PUSH(c.ms_neg, p);
                 }
                 int accept;
-                if (p > 1.0) {
+                if (above_one(p)) {
                     accept = 1;
                 } else {
-                    const uint64_t w = dqmc_philox_word(c.key, c.ctr);
                     c.ctr += 1;
-                    const double u = dqmc_word_to_uniform(w);
-                    accept = u < p;
-                    note_tie(c, u, p);
+                    const long long ub = uniform_bits(wu);
+                    accept = uniform_below(ub, p);
+                    note_tie(c, __longlong_as_double(ub), p);
                 }
                 c.proposals += 1;
                 if (accept) {
