@@ -601,19 +601,21 @@ __device__ __noinline__ void sweep_spatial(const W& x) {
                 detratio = __dmul_rn(R0, R0);
             }
             if (ghq) detratio = __ddiv_rn(__dmul_rn(detratio, gr), gq);
+            // the uniform's word ahead of p (drawn only when p <= 1); the
+            // uniform and the comparisons on the integer pipe (uniform_bits)
+            const uint64_t wu = dqmc_philox_word(c.key, c.ctr);
             const double p = __dmul_rn(c.wboson[t], detratio);
-            if (p < 0.0) {
+            if (below_zero(p)) {
                 c.n_neg_p += 1;
                 DQMC_MS_PUSH(c.ms_neg, p);
             }
-            if (p > 1.0) {
+            if (above_one(p)) {
                 accept = 1;
             } else {
-                const uint64_t w = dqmc_philox_word(c.key, c.ctr);
                 c.ctr += 1;
-                const double u = dqmc_word_to_uniform(w);
-                accept = u < p;
-                note_tie(c, u, p);
+                const long long ub = uniform_bits(wu);
+                accept = uniform_below(ub, p);
+                note_tie(c, __longlong_as_double(ub), p);
             }
             c.proposals += 1;
             if (accept) {
@@ -682,18 +684,18 @@ __device__ __noinline__ void sweep_spatial_hirsch(const W& x) {
             }
             p = __dmul_rn(c.wboson[t], detratio);
         }
-        const unsigned need = __ballot_sync(FULL, valid && !(p > 1.0));
+        const unsigned need = __ballot_sync(FULL, valid && !above_one(p));
         const unsigned below = (1u << lane) - 1u;  // lanes before this one
         bool acc = false;
         double gap = INFINITY;  // |u - p| of this lane's drawn uniform
         if (valid) {
-            if (p > 1.0) {
+            if (above_one(p)) {
                 acc = true;
             } else {
                 const uint64_t w = dqmc_philox_word(c.key, c.ctr + (uint64_t)__popc(need & below));
-                const double u = dqmc_word_to_uniform(w);
-                acc = u < p;
-                gap = fabs(u - p);
+                const long long ub = uniform_bits(w);
+                acc = uniform_below(ub, p);
+                gap = fabs(__longlong_as_double(ub) - p);
             }
         }
         const unsigned am = __ballot_sync(FULL, acc);
@@ -718,7 +720,7 @@ __device__ __noinline__ void sweep_spatial_hirsch(const W& x) {
             }
         }
         // negative probabilities of the proposals made, in order
-        unsigned neg = __ballot_sync(FULL, valid && p < 0.0) & done;
+        unsigned neg = __ballot_sync(FULL, valid && below_zero(p)) & done;
         while (neg) {
             const int k = __ffs(neg) - 1;
             const double pk = __shfl_sync(FULL, p, k);
