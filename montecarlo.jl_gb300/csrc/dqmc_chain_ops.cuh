@@ -1378,6 +1378,11 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
         const size_t at = (size_t)b * x.nn + (size_t)k * n + k;
         diag[e] = dfg ? df_to_d(gdf[at]) : c.G[at];
     }
+    // the slice's fields as the decisions read them (a shared-memory copy:
+    // the decision loop's serial chain then waits on no global load; `sv` is
+    // free during the local sweep); a site is not read again after it flips
+    int8_t* sc = reinterpret_cast<int8_t*>(x.s->sv);
+    for (int k = tid; k < n; k += DQMC_NT) sc[k] = (int8_t)conf_at(s, k, split(x));
     __syncthreads();
     if (split(x)) pull_peer_diag(x, diag, -1);
     long long acc_count = 0;
@@ -1389,6 +1394,10 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     int pending = 0;
     while (true) {
         if (tid == 0) {
+            // the chain's counters in registers for the loop
+            uint64_t ctr = c.ctr;
+            long long props = c.proposals, ties = c.n_near_tie;
+            double tie_gap = c.min_tie_gap;
             int j = i;
             for (; j < n; ++j) {
                 const double g0 = diag[j];
@@ -1397,16 +1406,16 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 int xnew = 0;
                 double gr = 1.0, gq = 1.0;
                 if (ghq) {
-                    const int xold = conf_at(s, j, split(x));
-                    const uint64_t w = dqmc_philox_word(c.key, c.ctr);
-                    c.ctr += 1;
+                    const int xold = sc[j];
+                    const uint64_t w = dqmc_philox_word(c.key, ctr);
+                    ctr += 1;
                     const int r = dqmc_word_to_choice3(w);
                     xnew = r + (r + 1 >= xold ? 2 : 1);  // choices[x_old, r+1] (fields.jl:534)
                     t = (xold - 1) * 4 + (xnew - 1);
                     gr = c.gam[xnew - 1];
                     gq = c.gam[xold - 1];
                 } else {
-                    t = conf_at(s, j, split(x)) > 0 ? 1 : 0;
+                    t = sc[j] > 0 ? 1 : 0;
                 }
                 const double d0 = c.delta0[t], d1 = c.delta1[t];
                 const double R0 = __dadd_rn(1.0, __dmul_rn(d0, __dsub_rn(1.0, g0)));
@@ -1421,7 +1430,7 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 if (ghq) detratio = __ddiv_rn(__dmul_rn(detratio, gr), gq);
                 // the uniform's word, drawn only when p <= 1 but computed
                 // ahead (it does not depend on p)
-                const uint64_t wu = dqmc_philox_word(c.key, c.ctr);
+                const uint64_t wu = dqmc_philox_word(c.key, ctr);
                 const double p = __dmul_rn(c.wboson[t], detratio);
                 if (below_zero(p)) {
                     c.n_neg_p += 1;
@@ -1431,16 +1440,18 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                 if (above_one(p)) {
                     accept = 1;
                 } else {
-                    c.ctr += 1;
+                    ctr += 1;
                     const long long ub = uniform_bits(wu);
                     accept = uniform_below(ub, p);
-                    note_tie(c, __longlong_as_double(ub), p);
+                    const double gap = fabs(__longlong_as_double(ub) - p);  // note_tie
+                    if (gap < DQMC_NEAR_TIE) ties += 1;
+                    if (gap < tie_gap) tie_gap = gap;
                 }
-                c.proposals += 1;
+                props += 1;
                 if (accept) {
                     x.s->sxd[0] = __ddiv_rn(d0, R0);
                     x.s->sxd[1] = twoflv ? __ddiv_rn(d1, R1) : 0.0;
-                    const int8_t flipped = ghq ? (int8_t)xnew : (int8_t)(-conf_at(s, j, split(x)));
+                    const int8_t flipped = ghq ? (int8_t)xnew : (int8_t)(-sc[j]);
                     // a flavour-split chain flips after the partner has read
                     // the site (rank 0 alone writes the configuration)
                     if (split(x)) x.s->xflip_val = (int)flipped;
@@ -1449,6 +1460,10 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
                     break;
                 }
             }
+            c.ctr = ctr;
+            c.proposals = props;
+            c.n_near_tie = ties;
+            c.min_tie_gap = tie_gap;
             // double-buffered slot: thread 0 writes the next round's slot
             // while slow threads may still read this one
             x.s->sxi[2 + (round & 1)] = j;
