@@ -1393,7 +1393,101 @@ __device__ __noinline__ long long sweep_spatial(const Ctx& x) {
     const int kcap = n < DQMC_DELAY ? n : DQMC_DELAY;  // U, W columns fit the n*n scratch
     int pending = 0;
     while (true) {
-        if (tid == 0) {
+        if (!ghq && warp == 0) {
+            // Hirsch fields: warp 0 evaluates up to 32 proposals at once.  From
+            // site i on, lane k computes the ratio of site i + k on the current
+            // diagonal (valid for every site up to the first acceptance, which
+            // alone changes it), takes its uniform at the counter the
+            // sequential loop would reach (a ballot and prefix count of the
+            // proposals with p <= 1 before it), and the first accepting lane
+            // wins: the sequential loop's decisions and draws exactly.
+            uint64_t ctr = c.ctr;
+            long long props = c.proposals, ties = c.n_near_tie;
+            double tie_gap = c.min_tie_gap;
+            int j = i, win = n;
+            const unsigned FULL = 0xffffffffu, below = (1u << lane) - 1u;
+            while (j < n) {
+                const int jj = j + lane;
+                const bool valid = jj < n;
+                double p = 0.0, R0 = 1.0, R1 = 1.0, d0 = 0.0, d1 = 0.0;
+                if (valid) {
+                    const int t = sc[jj] > 0 ? 1 : 0;
+                    d0 = c.delta0[t];
+                    d1 = c.delta1[t];
+                    R0 = __dadd_rn(1.0, __dmul_rn(d0, __dsub_rn(1.0, diag[jj])));
+                    double detratio;
+                    if (twoflv) {
+                        R1 = __dadd_rn(1.0, __dmul_rn(d1, __dsub_rn(1.0, diag[n + jj])));
+                        detratio = __dmul_rn(R0, R1);
+                    } else {
+                        detratio = __dmul_rn(R0, R0);
+                    }
+                    p = __dmul_rn(c.wboson[t], detratio);
+                }
+                const unsigned need = __ballot_sync(FULL, valid && !above_one(p));
+                bool acc = false;
+                double gap = INFINITY;  // |u - p| of this lane's drawn uniform
+                if (valid) {
+                    if (above_one(p)) {
+                        acc = true;
+                    } else {
+                        const uint64_t w = dqmc_philox_word(c.key, ctr + (uint64_t)__popc(need & below));
+                        const long long ub = uniform_bits(w);
+                        acc = uniform_below(ub, p);
+                        gap = fabs(__longlong_as_double(ub) - p);
+                    }
+                }
+                const unsigned am = __ballot_sync(FULL, acc);
+                const unsigned vm = __ballot_sync(FULL, valid);
+                const int last = am ? __ffs(am) - 1 : 31 - __clz(vm);  // last proposal made
+                const unsigned done = last == 31 ? FULL : ((2u << last) - 1u);
+                // near ties and the smallest gap of the proposals made (the
+                // gaps' bit patterns compared on the integer pipe)
+                ties += __popc(__ballot_sync(FULL, gap < DQMC_NEAR_TIE) & done);
+                long long gb = ((done >> lane) & 1u) ? __double_as_longlong(gap)
+                                                     : __double_as_longlong(INFINITY);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    const long long og = __shfl_xor_sync(FULL, gb, o);
+                    gb = og < gb ? og : gb;
+                }
+                const double gmin = __longlong_as_double(gb);
+                if (gmin < tie_gap) tie_gap = gmin;
+                // negative probabilities of the proposals made, in order
+                unsigned neg = __ballot_sync(FULL, valid && below_zero(p)) & done;
+                while (neg) {
+                    const int k = __ffs(neg) - 1;
+                    const double pk = __shfl_sync(FULL, p, k);
+                    if (lane == 0) {
+                        c.n_neg_p += 1;
+                        DQMC_MS_PUSH(c.ms_neg, pk);
+                    }
+                    neg &= neg - 1u;
+                }
+                ctr += (uint64_t)__popc(need & done);
+                props += __popc(vm & done);
+                if (am) {
+                    win = j + last;
+                    if (lane == last) {  // accept_local! of site `win`
+                        x.s->sxd[0] = __ddiv_rn(d0, R0);
+                        x.s->sxd[1] = twoflv ? __ddiv_rn(d1, R1) : 0.0;
+                        const int8_t flipped = (int8_t)(-sc[win]);
+                        if (split(x)) x.s->xflip_val = (int)flipped;
+                        else s[win] = flipped;
+                        c.accepted += 1;
+                    }
+                    break;
+                }
+                j += 32;
+            }
+            if (lane == 0) {
+                c.ctr = ctr;
+                c.proposals = props;
+                c.n_near_tie = ties;
+                c.min_tie_gap = tie_gap;
+                x.s->sxi[2 + (round & 1)] = win;
+            }
+        } else if (tid == 0) {
             // the chain's counters in registers for the loop
             uint64_t ctr = c.ctr;
             long long props = c.proposals, ties = c.n_near_tie;
