@@ -95,9 +95,10 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
     // sets up the mbarriers; released after the operation
     const bool use_tc = DQMC_TC_BUILD && tc_eligible(s->c, arena_cap);
 #if DQMC_TC_BUILD
-    // a CTA of this build that will not allocate TMEM gives up its allocation
-    // permit at once: an SM admits the next CTA of a kernel that may allocate
-    // TMEM only after the resident one has allocated or relinquished
+    // a CTA of the tensor-core variant that will not allocate TMEM gives up
+    // its allocation permit at once: an SM admits the next CTA of a kernel that
+    // may allocate TMEM only after the resident one has allocated or
+    // relinquished
     if (!use_tc && (threadIdx.x >> 5) == 0)
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
 #endif

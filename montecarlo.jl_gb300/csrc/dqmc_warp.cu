@@ -700,7 +700,7 @@ __device__ __noinline__ void sweep_spatial_hirsch(const W& x) {
         }
         const unsigned am = __ballot_sync(FULL, acc);
         const unsigned vm = __ballot_sync(FULL, valid);
-        const int last = am ? __ffs(am) - 1 : 31 - __clz(vm);  // last proposal of this round
+        const int last = am ? __ffs(am) - 1 : 31 - __clz(vm);  // last proposal of this pass
         const unsigned done = last == 31 ? FULL : ((2u << last) - 1u);
         {
             // near ties among the proposals made; the smallest gap by the bit
