@@ -398,8 +398,8 @@ int dqmc_pool_set_quota(dqmc_handle* h, int slot, int64_t n_sweeps);
  * visits).  use_graph = 1 replays the step (descriptor upload, launch,
  * download) as one captured CUDA graph. */
 int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph);
-/* enable = 1: a two-flavour chain of the pool (real field, dense hopping, no
- * device measurements, global updates or replica exchange) runs its two
+/* enable = 1: a two-flavour chain of the pool (at least 48 sites, real field,
+ * dense hopping, no device measurements, global updates or replica exchange) runs its two
  * flavour blocks on two CTAs of a two-CTA cluster, i.e. on two SMs, which
  * roughly halves its time per sweep when SMs are free (served streams at light
  * load).  Results are bit-identical to the chain on one CTA.  Default 0. */

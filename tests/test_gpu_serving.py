@@ -130,11 +130,12 @@ def test_pool_time_slice_is_work_conserving(pkg, lib, use_graph):
                                     ("mixed", 12)])
 def test_flavour_split_chain_equals_one_cta(pkg, lib, prec, L):
     """A two-flavour chain whose flavour blocks run on the two CTAs of a
-    two-CTA cluster (n = 16 and 64: shared-memory QR and G; n = 100: G in
-    global memory with delayed updates; mixed n = 144: tensor-core products
-    and float-pair G) gives bit-identical fields, Green's function and
-    counters to the chain on one CTA; a one-flavour chain in the same pool
-    runs on one CTA of its pair."""
+    two-CTA cluster (n = 64: shared-memory QR and G; n = 100: G in global
+    memory with delayed updates; mixed n = 144: tensor-core products and
+    float-pair G) gives bit-identical fields, Green's function and counters
+    to the chain on one CTA; a one-flavour chain in the same pool, and a
+    two-flavour chain too small to split (n = 16), run on one CTA of their
+    pair."""
     precision = lib.PREC_MIXED if prec == "mixed" else lib.PREC_FP64
     two = make_setup(pkg, L=L, U=-4.0, beta=2.0 if L <= 8 else 1.0, safe_mult=5,
                      field=pkg.MagneticHirschField)
