@@ -99,7 +99,11 @@ def poisson_stream(n, rate, seed, lattices=("square", "honeycomb"), Ls=(4, 6, 8,
 
 
 class Server:
-    """Serves requests from one pool with time-sliced launches."""
+    """Serves requests from one pool with time-sliced launches.  ``tol``: a
+    propagation-error bound under which requests of kinds the autotuner has
+    seen run at its safe_mult; ``flavour_split``: two-flavour requests of 48
+    sites or more run their flavour blocks on two SMs (bit-identical
+    results)."""
 
     def __init__(self, max_slots=304, budget_bytes=8 << 30, precision=_lib.PREC_FP64,
                  quantum_us=20000, use_graph=True, device=0, tol=None, flavour_split=True):
