@@ -99,3 +99,37 @@ def test_tensor_choice_cache_and_range(pkg):
     autotune._TC_CACHE[key] = True
     assert autotune.tune_tensor(specs)[0] == [False, True]
     autotune._TC_CACHE.pop(key, None)
+
+
+def _uniform_bits(w):
+    """numpy mirror of the device's uniform_bits: the IEEE bits of
+    (w >> 11) * 2^-53 assembled with integer operations."""
+    m = (w >> np.uint64(11)).astype(np.uint64)
+    out = np.zeros_like(m)
+    nz = m != 0
+    mm = m[nz]
+    # leading zeros of a 64-bit value (m < 2^53: at least 11)
+    lz = np.full(mm.shape, 64, dtype=np.int64)
+    for b in range(63, -1, -1):
+        hit = ((mm >> np.uint64(b)) & np.uint64(1)).astype(bool) & (lz == 64)
+        lz[hit] = 63 - b
+    sh = (lz - 11).astype(np.uint64)
+    mant = (mm << sh) & np.uint64((1 << 52) - 1)
+    out[nz] = ((np.uint64(1022) - sh) << np.uint64(52)) | mant
+    return out
+
+
+def test_uniform_bits_equal_the_double_formula():
+    """The decision loop builds the uniform (w >> 11) 2^-53 on the integer
+    pipe; the bits equal those of the floating-point formula for random words
+    and for the extremes (m = 0, 1, 2^52, 2^53 - 1)."""
+    rng = np.random.default_rng(11)
+    w = rng.integers(0, 2 ** 63, size=20000, dtype=np.int64).astype(np.uint64) * np.uint64(2)
+    w = np.concatenate([w, np.array([0, 1 << 11, 1 << 63, 0xFFFFFFFFFFFFFFFF, (1 << 52) << 11],
+                                    dtype=np.uint64)])
+    ref = ((w >> np.uint64(11)).astype(np.float64) * 2.0 ** -53).view(np.uint64)
+    assert np.array_equal(_uniform_bits(w), ref)
+    # ordering of non-negative doubles by their bits: the comparisons u < p
+    p = rng.random(5000)
+    u = rng.random(5000)
+    assert np.array_equal(u.view(np.int64) < p.view(np.int64), u < p)
