@@ -106,7 +106,7 @@ class Server:
     results)."""
 
     def __init__(self, max_slots=304, budget_bytes=8 << 30, precision=_lib.PREC_FP64,
-                 quantum_us=20000, use_graph=True, device=0, tol=None, flavour_split=True):
+                 quantum_us=50000, use_graph=True, device=0, tol=None, flavour_split=True):
         self.pool = _lib.Pool(max_slots, budget_bytes, precision=precision, device=device)
         # two-flavour requests run their flavour blocks on two SMs (same results)
         self.pool.set_flavour_split(flavour_split)
