@@ -43,7 +43,7 @@
 extern "C" {
 #endif
 
-#define DQMC_GB300_ABI_VERSION 9
+#define DQMC_GB300_ABI_VERSION 10
 
 /* status codes */
 #define DQMC_OK 0
@@ -404,6 +404,14 @@ int dqmc_pool_run(dqmc_handle* h, int budget_us, int use_graph);
  * roughly halves its time per sweep when SMs are free (served streams at light
  * load).  Results are bit-identical to the chain on one CTA.  Default 0. */
 int dqmc_pool_set_flavour_split(dqmc_handle* h, int enable);
+/* Test hook of the flavour split's failure path (no counterpart in the
+ * reference).  The two CTAs of a split chain meet at rendezvous, each waiting
+ * at most 2 s for its partner; after a time-out the chain's status becomes 9
+ * (dqmc_pool_run returns DQMC_ERR_NUMERICAL naming the slot) and both CTAs
+ * finish the launch without further waits.  from_epoch > 0 makes the second
+ * CTA of the slot's chain stop announcing itself from that rendezvous on, so
+ * that the wait runs out; 0 (the default) turns the hook off. */
+int dqmc_pool_set_split_silence(dqmc_handle* h, int slot, int from_epoch);
 int dqmc_pool_slot(dqmc_handle* h, int slot, int64_t* sweeps_done, int64_t* sweeps_left,
                    int32_t* active);
 int64_t dqmc_pool_free_bytes(dqmc_handle* h);

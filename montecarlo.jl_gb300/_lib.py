@@ -96,6 +96,7 @@ EXPORTS = [
     "dqmc_get_stack", "dqmc_set_stream", "dqmc_get_timers", "dqmc_calculate_greens_noalloc",
     "dqmc_pool_create", "dqmc_pool_admit", "dqmc_pool_release", "dqmc_pool_set_quota",
     "dqmc_pool_run", "dqmc_pool_slot", "dqmc_pool_free_bytes", "dqmc_pool_set_flavour_split",
+    "dqmc_pool_set_split_silence",
     "dqmc_set_measurements", "dqmc_reset_measurements", "dqmc_get_measurements",
     "dqmc_global_update", "dqmc_set_global_schedule", "dqmc_replica_exchange",
     "dqmc_get_global_stats", "dqmc_calculate_greens_kl", "dqmc_set_checkerboard",
@@ -164,6 +165,7 @@ def load(path: str = LIB_PATH):
     L.dqmc_pool_set_quota.argtypes = [P, C.c_int, C.c_int64]
     L.dqmc_pool_run.argtypes = [P, C.c_int, C.c_int]
     L.dqmc_pool_set_flavour_split.argtypes = [P, C.c_int]
+    L.dqmc_pool_set_split_silence.argtypes = [P, C.c_int, C.c_int]
     L.dqmc_pool_slot.argtypes = [P, C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
                                  C.POINTER(C.c_int32)]
     L.dqmc_pool_free_bytes.argtypes = [P]
@@ -563,6 +565,12 @@ class Pool(Handle):
         """Two-flavour chains run their flavour blocks on two CTAs (two SMs)
         of a two-CTA cluster; results are bit-identical."""
         check(load().dqmc_pool_set_flavour_split(self.h, int(bool(enable))))
+
+    def set_split_silence(self, slot, from_epoch):
+        """Test hook: the second CTA of the slot's flavour-split chain stops
+        announcing itself from rendezvous `from_epoch` on (0: off), so that
+        the first one's bounded wait runs out and the chain reports status 9."""
+        check(load().dqmc_pool_set_split_silence(self.h, int(slot), int(from_epoch)))
 
     def slot(self, slot):
         d, l, a = C.c_int64(), C.c_int64(), C.c_int32()

@@ -1565,6 +1565,16 @@ int dqmc_pool_set_flavour_split(dqmc_handle* h, int enable) {
     return DQMC_OK;
 }
 
+int dqmc_pool_set_split_silence(dqmc_handle* h, int slot, int from_epoch) {
+    if (int st = check_chain(h, slot)) return st;
+    if (!h->pool) return fail(DQMC_ERR_INVALID, "dqmc_pool_set_split_silence: not a pool");
+    if (from_epoch < 0) return fail(DQMC_ERR_INVALID, "dqmc_pool_set_split_silence: from_epoch < 0");
+    if (h->busy) if (int st = dqmc_synchronize(h)) return st;
+    h->host[slot].x_silent_from = from_epoch;
+    h->host_dirty = true;
+    return DQMC_OK;
+}
+
 int dqmc_pool_set_quota(dqmc_handle* h, int slot, int64_t n_sweeps) {
     if (int st = check_chain(h, slot)) return st;
     if (n_sweeps < 0) return fail(DQMC_ERR_INVALID, "dqmc_pool_set_quota: n_sweeps < 0");

@@ -134,6 +134,10 @@ struct DqmcChain {
     // budget} of the current launch (shared by the pool's chains, zeroed
     // before every launch); NULL outside pools
     unsigned int* run_sync;
+    // test hook of a flavour-split chain's rendezvous time-out: from this
+    // rendezvous epoch on, the second CTA no longer publishes its epoch, so
+    // that the first one's bounded wait runs out (0: never)
+    int x_silent_from, pad5;
 };
 
 

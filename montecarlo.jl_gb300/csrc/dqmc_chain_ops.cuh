@@ -166,14 +166,19 @@ __device__ __forceinline__ void st_release_cluster(uint32_t a, unsigned int v) {
 // epoch with a cluster-scope release and waits (bounded: 2 s of the global
 // timer or 2^28 polls) until the partner has published the same epoch; after
 // a time-out the chain's status is set, further rendezvous return at once
-// and false, and the callers skip the partner's data (no read of a CTA that
-// may have left).  Executed by all threads of both CTAs the same number of
-// times (both run the same control flow: the decisions are identical).
+// and false, and the callers skip the partner's data.  Executed by all
+// threads of both CTAs the same number of times (both run the same control
+// flow: the decisions are identical) unless one of them timed out.  Neither
+// CTA leaves the kernel before the other has passed its last rendezvous
+// (a cluster barrier ends the chain's launch; every wait before it is
+// bounded), so a partner's shared memory is never read after it has left.
 __device__ bool xsync(const Ctx& x) {
     __syncthreads();
     if (threadIdx.x == 0 && !x.s->xdead) {
         const unsigned int e = ++x.s->xepoch;
-        st_release_cluster(peer_addr(&x.s->xflag, (int)cluster_rank()), e);
+        const int quiet = x.c->x_silent_from;
+        if (!(quiet > 0 && x.b0 == 1 && e >= (unsigned int)quiet))
+            st_release_cluster(peer_addr(&x.s->xflag, (int)cluster_rank()), e);
         const uint32_t pa = peer_addr(&x.s->xflag, x.peer);
         unsigned long long t0;
         asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t0));

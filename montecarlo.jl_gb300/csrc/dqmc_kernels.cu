@@ -260,8 +260,9 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
 #endif
     }
     if (fsplit) {
-        // rank 0 takes over its partner's status; then both leave (no CTA
-        // reads the shared memory of one that has left)
+        // rank 0 takes over its partner's status; then both leave together
+        // (also after a rendezvous time-out: no CTA leaves while its partner
+        // may still read its shared memory)
         if (xsync(x)) {
             if (threadIdx.x == 0 && rank == 0) {
                 const int st = peer_ld_s32(peer_addr(&s->c.status, x.peer));
@@ -269,6 +270,7 @@ __global__ void __launch_bounds__(DQMC_NT, MINB) chain_kernel(DqmcChain* chains,
             }
             xsync(x);
         }
+        cluster_barrier();
         if (rank == 1) return;
     }
     // write back the mutable state

@@ -38,7 +38,7 @@ def test_library_exports_every_declared_symbol(pkg):
     missing = [n for n in declared_functions() if not hasattr(lib, n)]
     assert not missing, missing
     lib.dqmc_abi_version.restype = C.c_int
-    assert lib.dqmc_abi_version() == 9
+    assert lib.dqmc_abi_version() == 10
 
 
 def test_create_without_gpu_fails_loudly(pkg):

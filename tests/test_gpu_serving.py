@@ -136,6 +136,10 @@ def test_flavour_split_chain_equals_one_cta(pkg, lib, prec, L):
     to the chain on one CTA; a one-flavour chain in the same pool, and a
     two-flavour chain too small to split (n = 16), run on one CTA of their
     pair."""
+    split_equals_one_cta(pkg, lib, prec, L)
+
+
+def split_equals_one_cta(pkg, lib, prec, L):
     precision = lib.PREC_MIXED if prec == "mixed" else lib.PREC_FP64
     two = make_setup(pkg, L=L, U=-4.0, beta=2.0 if L <= 8 else 1.0, safe_mult=5,
                      field=pkg.MagneticHirschField)
@@ -167,3 +171,33 @@ def test_flavour_split_chain_equals_one_cta(pkg, lib, prec, L):
         assert np.array_equal(g0, g1)
         for k in ("accepted", "proposals", "near_ties", "max_propagation_error"):
             assert s0[k] == s1[k], k
+
+
+def test_flavour_split_rendezvous_time_out(pkg, lib):
+    """The two CTAs of a flavour-split chain wait at most 2 s for each other
+    at a rendezvous.  When the second CTA stops announcing itself (the test
+    hook: a flag that nothing sets any more), the first one's wait runs out:
+    the chain reports status 9, dqmc_pool_run fails naming the slot, the
+    launch ends within seconds (both CTAs finish without further waits), and
+    the device stays usable: the next pools on it give bit-identical results
+    split and unsplit."""
+    import time
+
+    two = make_setup(pkg, L=8, U=-4.0, beta=2.0, safe_mult=5, field=pkg.MagneticHirschField)
+    model, param, fld, exps = two
+    pool = lib.Pool(2, 1 << 30, precision=lib.PREC_FP64)
+    pool.set_flavour_split(True)
+    s = pool.admit(chain_config(lib, model, param, fld, 31))
+    pool.set_hopping(s, exps)
+    pool.init_random_field(s)
+    pool.set_quota(s, 2)
+    pool.set_split_silence(s, 5)
+    t0 = time.perf_counter()
+    with pytest.raises(lib.DQMCError) as err:
+        pool.run(30_000_000, True)
+    elapsed = time.perf_counter() - t0
+    assert "status 9" in str(err.value), str(err.value)
+    assert elapsed < 30.0, elapsed
+    assert pool.stats(s)["status"] == 9
+    pool.close()
+    split_equals_one_cta(pkg, lib, "fp64", 8)
