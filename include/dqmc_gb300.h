@@ -93,6 +93,12 @@ typedef struct {
     int64_t negative_probability; /* proposals with p < 0 */
     double max_propagation_error; /* max over all stabilisations of max|dG| */
     double max_reported_error;    /* max of the errors counted above */
+    /* status: 0 ok; 1 invalid chain (size out of range, or an operation the
+     * chain was not set up for); 2 non-finite Green's function at a
+     * stabilisation; 7 a tensor-core product's bounded wait ran out (the chain
+     * continues on the FP32-pipe product); 9 the partner CTA of a
+     * flavour-split chain stopped answering at a rendezvous.  A nonzero status
+     * makes the call that ran the chain return DQMC_ERR_NUMERICAL. */
     int32_t current_slice, current_range, direction, status;
     int64_t imaginary_probability; /* proposals with |imag(p)| > 1e-6 (complex chains) */
     double max_imaginary_probability; /* max |imag(p)| of those */
