@@ -129,3 +129,25 @@ def test_complex_matrix_buffers_round_trip(pkg):
     assert np.array_equal(back, G)
     cfg = _lib.ChainConfig(16, 1, 10, 5, 0, 1, 0.0, 1, 0.6)
     assert _lib.is_complex(cfg) and not _lib.is_complex(_lib.ChainConfig(16, 1, 10, 5, 0, 1, 0.5, 1))
+
+
+def test_julia_shim_buffer_sizes_match_the_header(pkg):
+    """The Julia shim of the integration guide allocates the dqmc_stats
+    buffer and names the struct sizes it mirrors: they must be the header's
+    (a smaller buffer would be overrun by dqmc_sweep)."""
+    import re
+    from montecarlo_gb300 import _lib
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    m = re.search(r"Vector\{UInt8\}\(undef, (\d+)\)\s+# dqmc_stats \(ABI (\d+), (\d+) bytes\)", text)
+    assert m, "the shim's dqmc_stats buffer line is missing"
+    assert int(m.group(1)) == int(m.group(3)) == C.sizeof(_lib.Stats)
+    assert int(m.group(2)) == _header_abi()
+    m = re.search(r"# dqmc_chain_config \(ABI (\d+), (\d+) bytes\)", text)
+    assert m, "the shim's dqmc_chain_config line is missing"
+    assert int(m.group(1)) == _header_abi() and int(m.group(2)) == C.sizeof(_lib.ChainConfig)
+
+
+def _header_abi():
+    import re
+    hdr = open(os.path.join(ROOT, "include", "dqmc_gb300.h")).read()
+    return int(re.search(r"#define DQMC_GB300_ABI_VERSION (\d+)", hdr).group(1))
