@@ -52,7 +52,16 @@ WORKLOADS = {
     "c4": (16, -4.0, 10.0, 10, "MagneticHirschField",
            "16x16 square repulsive Hubbard U=4 (physics), mu=0, MagneticHirschField, beta=10, "
            "dtau=0.1 (M=100), safe_mult=10, FP64"),
+    # the field-timing case of the reference's documentation (docs/src/DQMC/fields.md:49-56:
+    # 6x6 square, beta = 1, 10 000 sweeps; 6.8 s and 17 s there, hardware not stated)
+    "docs6_density": (6, 1.0, 1.0, 10, "DensityHirschField",
+                      "6x6 square attractive Hubbard U=-1 (physics; U=+1 reference convention), "
+                      "mu=0, DensityHirschField, beta=1, dtau=0.1 (M=10), safe_mult=10, FP64"),
+    "docs6_magnetic": (6, -1.0, 1.0, 10, "MagneticHirschField",
+                       "6x6 square repulsive Hubbard U=1 (physics; U=-1 reference convention), "
+                       "mu=0, MagneticHirschField, beta=1, dtau=0.1 (M=10), safe_mult=10, FP64"),
 }
+L2_BYTES = 129 * 1000 * 1000  # GB300 L2
 
 
 def sweep_flops(n, nf, M, nr, acc):
@@ -808,6 +817,8 @@ def main():
         if tr.get("workload") == args.workload:
             traffic = tr["dram_bytes_per_launch"] * B_chains / tr["chains_captured"]
 
+    chain_bytes = int(_lib.load().dqmc_chain_bytes(_lib.ChainConfig(
+        n, nf, M, param.safe_mult, fld.kind, 1, fld.alpha, 0), 0))
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_sample(pkg, args.workload, args.cpu_budget)
@@ -823,9 +834,11 @@ def main():
                        "path": ("plain FP64" if args.precision == "fp64" else "mixed") +
                                " (value); mixed, batched, served below",
                        "chains_per_gpu": B_chains, "parallelism": f"replicas{world}",
-                       "l2": "working set larger than L2 (no flush needed)",
-                       "chain_bytes": int(_lib.load().dqmc_chain_bytes(_lib.ChainConfig(
-                           n, nf, M, param.safe_mult, fld.kind, 1, fld.alpha, 0), 0))},
+                       "l2": ("working set larger than L2 (no flush needed)"
+                              if B_chains * chain_bytes > L2_BYTES else
+                              "working set fits in L2 (not flushed: every sweep re-reads each "
+                              "chain's state many times within the launch)"),
+                       "chain_bytes": chain_bytes},
             "e2e": {"value": world * B_chains * args.steps / e2e_s, "unit": "sweeps/s",
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "includes": "hopping + field upload, stack build, sweeps, per-sweep download "
