@@ -125,6 +125,7 @@ class Server:
         queue: List[Request] = []
         active = {}  # slot -> (req, admitted_time, last_block_time, blocks_done, latencies)
         results = {}
+        configs = {}  # rid -> (chain config, hopping exponentials), built once per request
         t0 = time.perf_counter()
         launches = 0
         total_sweeps = 0
@@ -137,7 +138,9 @@ class Server:
             # admission: every queued request that fits the slots and budget
             still = []
             for req in queue:
-                cfg, exps = request_config(req, self.precision, self.tol)
+                if req.rid not in configs:
+                    configs[req.rid] = request_config(req, self.precision, self.tol)
+                cfg, exps = configs[req.rid]
                 slot = self.pool.admit(cfg)
                 if slot is None:
                     still.append(req)
@@ -145,6 +148,7 @@ class Server:
                 self.pool.set_hopping(slot, exps)
                 self.pool.init_random_field(slot)
                 self.pool.set_quota(slot, req.sweeps)
+                del configs[req.rid]
                 t_adm = time.perf_counter() - t0
                 active[slot] = [req, t_adm, t_adm, 0, []]
             queue = still

@@ -1,6 +1,7 @@
 """Host-side logic without a GPU: the autotuner's cache and back-off, the
-serving path's reuse of cached choices, and the by-distance slots of the
-time-displaced measurements (the reference's EachSitePairByDistance)."""
+serving path's reuse of cached choices and its bookkeeping (on a fake pool),
+and the by-distance slots of the time-displaced measurements (the
+reference's EachSitePairByDistance)."""
 import numpy as np
 
 
@@ -133,3 +134,95 @@ def test_uniform_bits_equal_the_double_formula():
     p = rng.random(5000)
     u = rng.random(5000)
     assert np.array_equal(u.view(np.int64) < p.view(np.int64), u < p)
+
+
+class _FakePool:
+    """Host-side stand-in for _lib.Pool: `slots` slots, every admitted chain
+    advances `per_run` sweeps per time slice."""
+
+    def __init__(self, slots, per_run):
+        self.slots, self.per_run = slots, per_run
+        self.quota, self.done, self.runs, self.split = {}, {}, 0, None
+
+    def set_flavour_split(self, on):
+        self.split = on
+
+    def admit(self, cfg):
+        free = [s for s in range(self.slots) if s not in self.quota]
+        if not free:
+            return None
+        self.quota[free[0]], self.done[free[0]] = 0, 0
+        return free[0]
+
+    def set_hopping(self, slot, exps):
+        assert slot in self.quota
+
+    def init_random_field(self, slot):
+        assert slot in self.quota
+
+    def set_quota(self, slot, n):
+        self.quota[slot] = n
+
+    def run(self, quantum_us, use_graph):
+        self.runs += 1
+        for s in self.quota:
+            self.done[s] = min(self.quota[s], self.done[s] + self.per_run)
+
+    def slot(self, slot):
+        return self.done[slot], self.quota[slot] - self.done[slot], True
+
+    def get_field(self, slot):
+        return np.zeros(1, dtype=np.int8)
+
+    def greens(self, slot):
+        return np.zeros(1)
+
+    def stats(self, slot):
+        return {"status": 0}
+
+    def release(self, slot):
+        del self.quota[slot], self.done[slot]
+
+    def close(self):
+        pass
+
+
+def test_server_admission_blocks_and_percentiles(pkg, monkeypatch):
+    """The server's bookkeeping on a fake pool: requests beyond the free
+    slots wait and are admitted as others finish, each request's chain
+    configuration is built once however long it waits, every request
+    reports one latency per 10-sweep block, and the throughput counts every
+    requested sweep."""
+    from montecarlo_gb300 import serving
+    pool = _FakePool(slots=2, per_run=7)
+    monkeypatch.setattr(serving._lib, "Pool", lambda *a, **k: pool)
+    built = []
+    real = serving.request_config
+
+    def counting(req, precision=None, tol=None):
+        built.append(req.rid)
+        return real(req, precision, tol)
+
+    monkeypatch.setattr(serving, "request_config", counting)
+    reqs = [serving.Request(i, "square", 4, 4.0, 1.0, sw, 10 + i)
+            for i, sw in enumerate((30, 25, 40, 12, 20))]
+    srv = serving.Server(max_slots=2, quantum_us=1000)
+    out = srv.serve(reqs, realtime=False)
+    srv.close()
+    assert pool.split is True
+    assert sorted(built) == [0, 1, 2, 3, 4]  # once per request, not once per slice waited
+    assert set(out["results"]) == {0, 1, 2, 3, 4} and out["unfinished"] == 0
+    for r in reqs:
+        res = out["results"][r.rid]
+        assert len(res.block_latencies) == r.sweeps // serving.BLOCK
+        assert all(x >= 0.0 for x in res.block_latencies)
+        assert res.finished >= res.admitted
+    assert out["sweeps"] == sum(r.sweeps for r in reqs)
+    assert out["blocks"] == sum(r.sweeps // serving.BLOCK for r in reqs)
+    # two slots at 7 sweeps a slice each: at least total / 14 slices, and at
+    # least the longest request's sweeps / 7
+    total = sum(r.sweeps for r in reqs)
+    assert out["launches"] >= max(-(-total // 14), -(-40 // 7))
+    lat = [x for res in out["results"].values() for x in res.block_latencies]
+    assert out["p50_block_s"] == float(np.percentile(lat, 50))
+    assert out["p99_block_s"] == float(np.percentile(lat, 99))
