@@ -226,3 +226,87 @@ def test_server_admission_blocks_and_percentiles(pkg, monkeypatch):
     lat = [x for res in out["results"].values() for x in res.block_latencies]
     assert out["p50_block_s"] == float(np.percentile(lat, 50))
     assert out["p99_block_s"] == float(np.percentile(lat, 99))
+
+
+class _FakeHandle:
+    """Host-side stand-in for a one-chain _lib.Handle: counts sweeps and
+    returns a field whose first sites spell the sweep count in binary."""
+
+    def __init__(self, configs, precision=None, device=0):
+        c = configs[0]
+        self.n, self.M, self.swept, self.calls = c.n_sites, c.slices, 0, []
+
+    def set_hopping(self, chain, exps):
+        pass
+
+    def init_random_field(self, chain):
+        pass
+
+    def set_field(self, chain, conf):
+        pass
+
+    def initialize_run(self):
+        pass
+
+    def sweep(self, k):
+        self.calls.append(k)
+        self.swept += k
+
+    def get_field(self, chain):
+        conf = -np.ones((self.n, self.M), dtype=np.int8, order="F")
+        for b in range(self.n):
+            if (self.swept >> b) & 1:
+                conf[b, 0] = 1
+        return conf
+
+    def greens(self, chain, physical=False):
+        return np.zeros((1, self.n, self.n))
+
+    def stats(self, chain):
+        return {k: 0 for k in (
+            "accepted", "proposals", "propagation_errors", "max_propagation_error",
+            "negative_probability", "imaginary_probability", "max_imaginary_probability",
+            "min_reported_error", "mean_reported_error", "max_reported_error",
+            "min_negative_probability", "mean_negative_probability",
+            "max_negative_probability", "min_imaginary_probability",
+            "mean_imaginary_probability", "current_slice")}
+
+    def global_stats(self, chain):
+        return (0, 0)
+
+
+def test_run_measures_and_records_like_sweep_once(pkg, monkeypatch):
+    """run! (DQMC.jl:252-394 with sweep_once!, :200-225) on a fake handle: the
+    sweeps run in launches of at most max_sweeps_per_launch, measurements
+    happen after exactly the sweeps i > thermalization with i % measure_rate
+    == 0, and the recorder holds the configurations after exactly the sweeps
+    i > thermalization with i % recording_rate == 0, whatever the launch
+    boundaries."""
+    from montecarlo_gb300 import dqmc
+    monkeypatch.setattr(dqmc._lib, "Handle", _FakeHandle)
+
+    class Obs:
+        def __init__(self):
+            self.at = []
+
+        def measure(self, G, mc):
+            self.at.append(mc.last_sweep)
+
+    model = pkg.HubbardModel(pkg.SquareLattice(4), U=4.0)
+    for th, sw, rate, rec, cap in ((7, 30, 4, 6, 5), (10, 25, 10, 3, 50), (0, 13, 1, 2, 4),
+                                   (5, 12, 7, 7, 1)):
+        obs = Obs()
+        mc = dqmc.DQMC(model, beta=1.0, thermalization=th, sweeps=sw, measure_rate=rate,
+                       recording_rate=rec, device_measurements=False, measurements={"m": obs},
+                       seed=1)
+        mc.max_sweeps_per_launch = cap
+        assert mc.run() == dqmc.ExitCode.SUCCESS
+        total = th + sw
+        assert mc.last_sweep == total and mc.handle.swept == total
+        assert max(mc.handle.calls) <= cap
+        assert obs.at == [i for i in range(th + 1, total + 1) if i % rate == 0]
+        want = [i for i in range(th + 1, total + 1) if i % rec == 0]
+        assert len(mc.recorder) == len(want)
+        for j, i in enumerate(want):
+            conf = mc.recorder[j]
+            assert sum(1 << b for b in range(16) if conf[b, 0] == 1) == i
