@@ -14,6 +14,16 @@
  * which replaces Julia's global RNG: draw d of a chain with seed s is
  * philox(ctr = {d_lo, d_hi, 0, 0}, key = {s_lo, s_hi}); the 64-bit word is
  * (out0 << 32) | out1.  Draws are consumed in the reference's order.
+ *
+ * What pins this restatement: the reference's own known-answer recipes,
+ * restated (the analytic U = 0 Green's function and the direct pivoted-QR
+ * chain of test/testfunctions.jl, exact diagonalisation of test/ED on 2x2,
+ * the global-update and rank-1 identities of test/updates.jl and
+ * test/fields.jl), with the fixtures under tests/golden.  It is not pinned
+ * against outputs of the reference itself: Julia is absent and the reference
+ * ships no golden vectors.  Its accept/reject sequences follow this file's
+ * Philox stream, so parity of decision sequences with the reference's Julia
+ * RNG is unpinned.
  */
 #include "dqmc_oracle.h"
 
