@@ -310,3 +310,68 @@ def test_run_measures_and_records_like_sweep_once(pkg, monkeypatch):
         for j, i in enumerate(want):
             conf = mc.recorder[j]
             assert sum(1 << b for b in range(16) if conf[b, 0] == 1) == i
+
+
+def test_tune_safe_mult_picks_largest_stable_interval(pkg, monkeypatch):
+    """tune_safe_mult on a fake device whose propagation error grows with the
+    stabilisation interval k as err(k) = c * 10^k (c per chain): each chain gets the
+    largest candidate (capped at its slice count) with err <= safety * tol,
+    the smallest candidate when none is, one probe launch covers every
+    uncached chain x candidate, and cached kinds are not probed again."""
+    from montecarlo_gb300 import autotune
+
+    launches = []
+    BASE = {1: 1e-18, 2: 1e-16, 3: 1e-18, 4: 1.0}  # by seed: c of err(k) = c * 10^k
+
+    class Probe:
+        def __init__(self, cfgs, precision=None, device=0):
+            self.cfgs = cfgs
+            launches.append(len(cfgs))
+
+        def set_hopping(self, r, exps):
+            pass
+
+        def init_random_field(self, r):
+            pass
+
+        def set_field(self, r, conf):
+            assert conf.shape == (self.cfgs[r].n_sites, self.cfgs[r].slices)
+
+        def initialize_run(self):
+            pass
+
+        def sweep(self, n):
+            return [{"max_propagation_error": BASE[c.seed] * 10.0 ** c.safe_mult}
+                    for c in self.cfgs]
+
+        def close(self):
+            pass
+
+    monkeypatch.setattr(autotune._lib, "Handle", Probe)
+    weak = pkg.HubbardModel(pkg.SquareLattice(4), U=2.0)
+    strong = pkg.HubbardModel(pkg.SquareLattice(4), U=8.0)
+    short = pkg.HubbardModel(pkg.SquareLattice(6), U=2.0)
+    wild = pkg.HubbardModel(pkg.SquareLattice(6), U=7.0)
+    specs = [(weak, weak.choose_field(), 4.0, 0.1, 1), (strong, strong.choose_field(), 4.0, 0.1, 2),
+             (short, short.choose_field(), 0.5, 0.1, 3), (wild, wild.choose_field(), 2.0, 0.1, 4)]
+    for m, f, b, dt, s in specs:
+        autotune._CACHE.pop(autotune.cache_key(m, f, b, dt, autotune._lib.PREC_FP64, 1e-6), None)
+    confs = []
+    for m, f, b, dt, s in specs:
+        M = pkg.DQMCParameters.make(beta=b, delta_tau=dt).slices
+        confs.append(np.ones((len(m.l), M), dtype=np.int8))
+    ks, errs = autotune.tune_safe_mult(specs, tol=1e-6, confs=confs, safety=0.1)
+    bound = 0.1 * 1e-6
+    for (m, f, b, dt, s), k, e in zip(specs, ks, errs):
+        M = pkg.DQMCParameters.make(beta=b, delta_tau=dt).slices
+        err = {c: BASE[s] * 10.0 ** c for c in {min(c, M) for c in autotune.CANDIDATES}}
+        ok = [c for c, v in err.items() if v <= bound]
+        assert k == (max(ok) if ok else min(err)) and e == err[k]
+        assert k <= M
+    assert ks == [10, 8, 5, 2]  # largest under 1e-7; five slices; none stable: the smallest
+    assert len(launches) == 1
+    # all cached now: no probe launch, NaN errors
+    ks2, errs2 = autotune.tune_safe_mult(specs, tol=1e-6, confs=confs)
+    assert ks2 == ks and all(np.isnan(errs2)) and len(launches) == 1
+    for m, f, b, dt, s in specs:
+        autotune._CACHE.pop(autotune.cache_key(m, f, b, dt, autotune._lib.PREC_FP64, 1e-6), None)
