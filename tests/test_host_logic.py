@@ -375,3 +375,24 @@ def test_tune_safe_mult_picks_largest_stable_interval(pkg, monkeypatch):
     assert ks2 == ks and all(np.isnan(errs2)) and len(launches) == 1
     for m, f, b, dt, s in specs:
         autotune._CACHE.pop(autotune.cache_key(m, f, b, dt, autotune._lib.PREC_FP64, 1e-6), None)
+
+
+def test_neighbour_partners_alternate_even_and_odd_pairs(pkg):
+    """Replica exchange rounds pair neighbours (0,1), (2,3), ... and then
+    (1,2), (3,4), ...; partners are mutual, a replica without a partner
+    sits the round out (-1), and two rounds give every neighbour pair one
+    attempt."""
+    from montecarlo_gb300.tempering import neighbour_partners
+    for n in range(1, 9):
+        seen = set()
+        for odd in (False, True):
+            p = neighbour_partners(n, odd)
+            assert p.dtype == np.int32 and p.shape == (n,)
+            for a in range(n):
+                if p[a] >= 0:
+                    assert p[p[a]] == a and abs(p[a] - a) == 1
+                    assert (min(a, p[a]) % 2 == 1) == odd
+                    seen.add(min(a, p[a]))
+        assert seen == set(range(n - 1))
+    assert neighbour_partners(5, False).tolist() == [1, 0, 3, 2, -1]
+    assert neighbour_partners(5, True).tolist() == [-1, 2, 1, 4, 3]
