@@ -1,7 +1,9 @@
-"""Host-side logic without a GPU: the autotuner's cache and back-off, the
-serving path's reuse of cached choices and its bookkeeping (on a fake pool),
-and the by-distance slots of the time-displaced measurements (the
-reference's EachSitePairByDistance)."""
+"""Host-side logic without a GPU: the autotuner's cache, back-off and
+safe_mult choice (on a fake device), the serving path's reuse of cached
+choices and its bookkeeping (on a fake pool), run!'s measurement and
+recording schedule (on a fake handle), the replica-exchange pairing, and the
+by-distance slots of the time-displaced measurements (the reference's
+EachSitePairByDistance)."""
 import numpy as np
 
 
