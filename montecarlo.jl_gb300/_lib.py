@@ -13,6 +13,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libdqmc_gb300.so")
 
 DQMC_OK = 0
+DQMC_ERR_NUMERICAL = 4
 DQMC_ERR_NOT_READY = 5
 PREC_FP64 = 0
 PREC_MIXED = 1

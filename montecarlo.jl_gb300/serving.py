@@ -60,6 +60,10 @@ class Result:
     admitted: float
     finished: float
     block_latencies: List[float] = field(default_factory=list)
+    # a chain that reported a nonzero status (non-finite G, a partner CTA
+    # that stopped answering, ...): the error text; its conf / greens are
+    # the state it stopped in
+    error: Optional[str] = None
 
 
 def request_config(req: Request, precision=None, tol=None):
@@ -129,6 +133,7 @@ class Server:
         t0 = time.perf_counter()
         launches = 0
         total_sweeps = 0
+        failed = 0
         while pending or queue or active:
             now = time.perf_counter() - t0
             if max_wall is not None and now > max_wall:
@@ -156,7 +161,25 @@ class Server:
                 if pending and realtime:
                     time.sleep(max(0.0, pending[0].arrival - (time.perf_counter() - t0)))
                 continue
-            self.pool.run(self.quantum_us, self.use_graph)
+            try:
+                self.pool.run(self.quantum_us, self.use_graph)
+            except _lib.DQMCError as err:
+                # a chain that reported a nonzero status fails its request
+                # alone: release it and keep serving the others (the slice's
+                # work of every other chain is kept); anything else is raised
+                if err.code != _lib.DQMC_ERR_NUMERICAL:
+                    raise
+                bad = [sl for sl in active if self.pool.stats(sl)["status"] != 0]
+                if not bad:
+                    raise
+                tnow = time.perf_counter() - t0
+                for sl in bad:
+                    req, t_adm, _tl, _nb, lats = active.pop(sl)
+                    results[req.rid] = Result(req.rid, self.pool.get_field(sl),
+                                              self.pool.greens(sl), self.pool.stats(sl),
+                                              t_adm, tnow, lats, error=str(err))
+                    failed += 1
+                    self.pool.release(sl)
             launches += 1
             tnow = time.perf_counter() - t0
             for slot in list(active):
@@ -189,7 +212,7 @@ class Server:
                     sweeps_per_s=total_sweeps / wall if wall > 0 else math.nan,
                     p50_block_s=float(np.percentile(lat, 50)) if lat else None,
                     p99_block_s=float(np.percentile(lat, 99)) if lat else None,
-                    unfinished=len(active) + len(queue) + len(pending))
+                    unfinished=len(active) + len(queue) + len(pending), failed=failed)
 
 
 def run_ensemble(configs_and_exps, seconds: float, quantum_us=50000, precision=_lib.PREC_FP64,

@@ -5,6 +5,7 @@ recording schedule (on a fake handle), the replica-exchange pairing, and the
 by-distance slots of the time-displaced measurements (the reference's
 EachSitePairByDistance)."""
 import numpy as np
+import pytest
 
 
 def test_autotune_back_off_and_cache(pkg):
@@ -398,3 +399,61 @@ def test_neighbour_partners_alternate_even_and_odd_pairs(pkg):
         assert seen == set(range(n - 1))
     assert neighbour_partners(5, False).tolist() == [1, 0, 3, 2, -1]
     assert neighbour_partners(5, True).tolist() == [-1, 2, 1, 4, 3]
+
+
+def test_server_fails_one_request_and_serves_the_rest(pkg, monkeypatch):
+    """A chain that reports a nonzero status during a time slice (the pool run
+    returns DQMC_ERR_NUMERICAL) fails its own request only: the server
+    records it with the error, releases its slot, admits the next request
+    into it and finishes every other request; any other error is raised."""
+    from montecarlo_gb300 import serving, _lib
+
+    class Failing(_FakePool):
+        def __init__(self):
+            super().__init__(slots=2, per_run=7)
+            self.status = {}
+
+        def admit(self, cfg):
+            s = super().admit(cfg)
+            if s is not None:
+                self.status[s] = 0
+                self.seed = getattr(self, "seed", {})
+                self.seed[s] = cfg.seed
+            return s
+
+        def run(self, quantum_us, use_graph):
+            super().run(quantum_us, use_graph)
+            for s in self.quota:
+                if self.seed[s] == 11 and self.done[s] >= 21:  # request 1 breaks
+                    self.status[s] = 9
+                    raise _lib.DQMCError(_lib.DQMC_ERR_NUMERICAL, f"slot {s} reported status 9")
+
+        def stats(self, slot):
+            return {"status": self.status[slot]}
+
+        def release(self, slot):
+            super().release(slot)
+            del self.status[slot], self.seed[slot]
+
+    pool = Failing()
+    monkeypatch.setattr(serving._lib, "Pool", lambda *a, **k: pool)
+    reqs = [serving.Request(i, "square", 4, 4.0, 1.0, sw, 10 + i)
+            for i, sw in enumerate((30, 40, 25, 12))]
+    srv = serving.Server(max_slots=2, quantum_us=1000)
+    out = srv.serve(reqs, realtime=False)
+    assert out["failed"] == 1 and out["unfinished"] == 0
+    bad = out["results"][1]
+    assert bad.error and "status 9" in bad.error and bad.stats["status"] == 9
+    assert len(bad.block_latencies) == 1  # the block finished in an earlier slice counts
+    for rid in (0, 2, 3):
+        r = out["results"][rid]
+        assert r.error is None and len(r.block_latencies) == reqs[rid].sweeps // serving.BLOCK
+
+    class Broken(_FakePool):
+        def run(self, quantum_us, use_graph):
+            raise _lib.DQMCError(2, "CUDA error")
+
+    monkeypatch.setattr(serving._lib, "Pool", lambda *a, **k: Broken(2, 7))
+    srv = serving.Server(max_slots=2, quantum_us=1000)
+    with pytest.raises(_lib.DQMCError):
+        srv.serve(reqs[:1], realtime=False)
