@@ -151,3 +151,9 @@ def _header_abi():
     import re
     hdr = open(os.path.join(ROOT, "include", "dqmc_gb300.h")).read()
     return int(re.search(r"#define DQMC_GB300_ABI_VERSION (\d+)", hdr).group(1))
+
+
+def test_python_binding_covers_the_header(pkg):
+    """The ctypes layer binds exactly the entry points the header declares."""
+    from montecarlo_gb300 import _lib
+    assert sorted(_lib.EXPORTS) == declared_functions()
