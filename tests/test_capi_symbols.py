@@ -157,3 +157,49 @@ def test_python_binding_covers_the_header(pkg):
     """The ctypes layer binds exactly the entry points the header declares."""
     from montecarlo_gb300 import _lib
     assert sorted(_lib.EXPORTS) == declared_functions()
+
+
+def _build_c_host(tmp_path):
+    import shutil
+    import subprocess
+    from montecarlo_gb300 import build, _lib
+
+    if shutil.which("gcc") is None:  # pragma: no cover
+        pytest.skip("gcc unavailable")
+    build.build()
+    exe = tmp_path / "c_host_example"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "c_host_example.c"), "-L", libdir,
+                    "-ldqmc_gb300", "-lm", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    return exe
+
+
+def test_c_host_links_and_fails_loudly_without_gpu(pkg, tmp_path):
+    """A pure C host (tests/c_host_example.c: the pool calls of the serving
+    loop) compiles against the header and links against the library; without
+    a device its first call reports the CUDA error (no CPU fallback)."""
+    import subprocess
+    import torch
+
+    exe = _build_c_host(tmp_path)
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present (the GPU test runs the example)")
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 3, (r.returncode, r.stdout, r.stderr)
+    assert "dqmc_pool_create" in r.stdout
+
+
+@pytest.mark.gpu
+def test_c_host_runs_a_pool(pkg, tmp_path):
+    """The pure C host on the GPU: admits a 4x4 chain, runs 50 ms time slices
+    until its 5 sweeps are done, and reads a sane acceptance and propagation
+    error."""
+    import subprocess
+
+    exe = _build_c_host(tmp_path)
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stdout, r.stderr)
+    parts = r.stdout.split()
+    assert parts[0] == "sweeps" and int(parts[1]) == 5
+    assert 0.0 < float(parts[3]) < 1.0 and float(parts[5]) < 1e-6
